@@ -1,0 +1,135 @@
+/*
+ * csadv -- cubed-sphere tracer advection on NVIDIA GB300 (sm_103a).
+ *
+ * C ABI of the GPU implementation of the advection time step of luanfs/py-cubed-sphere.
+ * The reference is pure Python and has no FFI; its seam is a set of Python calls
+ * (advection_sphere.py, advection_timestep.py, advection_vars.py, diagnostics.py,
+ * errors.py).  Each entry point below names the reference call it replaces.  The Python
+ * shim in py-cubed-sphere_gb300/csadv binds these with ctypes and re-exposes the
+ * reference's function names and signatures.
+ *
+ * Conventions
+ *  - Every function returns an int status (CSADV_OK == 0, negative on error) and never
+ *    exits the process (the reference prints and calls exit(); the Python shim maps the
+ *    codes back to the reference's behaviour).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).  Work is
+ *    enqueued on it; functions that return host values synchronise it.
+ *  - Host arrays are float64 in the reference layout A[i][j][p] (p fastest), either the
+ *    full array with 4 ghost cells per side, shape (N+8, N+8, 6)  (CSADV_LAYOUT_FULL),
+ *    or the interior only, shape (N, N, 6)                      (CSADV_LAYOUT_INTERIOR).
+ *  - A plan is not thread-safe; use one plan per host thread/stream.
+ */
+#ifndef CSADV_H
+#define CSADV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define CSADV_OK 0
+#define CSADV_ERR_OPTION (-1)      /* unknown option code; reference: print + exit(), advection_ic.py:61-166 */
+#define CSADV_ERR_OPTION_PAIR (-2) /* split/metric pair the reference cannot run (UnboundLocalError,
+                                      discrete_operators.py:49-73): AVLT/L04 need MT-0, PL07 needs MT-PL07 */
+#define CSADV_ERR_ARG (-3)         /* bad argument (NULL, size, tracer index, N < 8 ...) */
+#define CSADV_ERR_OOM (-4)         /* device or pinned-host allocation failed */
+#define CSADV_ERR_CUDA (-5)        /* a CUDA runtime call failed */
+#define CSADV_ERR_NONFINITE (-6)   /* NaN/Inf found in the state */
+#define CSADV_ERR_BLOWUP (-7)      /* Linf error > 100; reference: print + exit(), output.py:44-47 */
+#define CSADV_ERR_UNSUPPORTED (-8) /* option combination not implemented by the requested engine */
+#define CSADV_ERR_TOO_LARGE (-9)   /* request exceeds a fixed capacity */
+
+#define CSADV_LAYOUT_FULL 0
+#define CSADV_LAYOUT_INTERIOR 1
+
+/* engines */
+#define CSADV_ENGINE_AUTO 0   /* fused when the scheme allows it, else staged */
+#define CSADV_ENGINE_STAGED 1 /* one kernel per reference stage; every option combination */
+#define CSADV_ENGINE_FUSED 2  /* one tile kernel per step (ET-DG, MF-0/MF-PR) */
+
+/* wind codes: 1-4 are the reference's vf (advection_ic.py:287-313); the others are the
+   parameterised benchmark winds (wind_param meaning in brackets) */
+#define CSADV_WIND_SOLID 101     /* solid-body rotation [alpha, u0]               (static)  */
+#define CSADV_WIND_DEFORM 102    /* Nair-Lauritzen 2010 case 4 [k, T]             (time-dependent) */
+#define CSADV_WIND_SOLID_DIV 103 /* solid body + eps*u0 divergent part [alpha, u0, eps] (static) */
+
+/* initial-condition codes: 1-4 are the reference's ic (advection_ic.py:215-281, exact
+   solution depends on the wind code exactly as in the reference); the others: */
+#define CSADV_IC_HILL 101         /* exp(-b0 |x - xc|^2) [lon_c, lat_c, b0] */
+#define CSADV_IC_BELLS 102        /* 0.1 + 0.9 * two cosine bells of radius 1/2 at lon 5pi/6, 7pi/6 */
+#define CSADV_IC_SMOOTH_BELLS 103 /* 0.95 + 0.05 * the same bells */
+
+typedef struct csadv_options {
+    int recon;     /* advection.par "Reconstruction": 1 PPM-0, 2 PPM-CW84, 3 PPM-PL07, 4 PPM-L04 */
+    int dp;        /* "Departure point scheme": 1 RK1, 2 RK2 */
+    int opsplit;   /* "Operator splitting": 1 SP-AVLT, 2 SP-L04, 3 SP-PL07 */
+    int et;        /* "Edge treatment": 1 ET-S72, 2 ET-PL07, 3 ET-DG */
+    int mt;        /* "Metric tensor treatment": 1 MT-0, 2 MT-PL07 */
+    int mf;        /* "Mass fixer": 1 MF-0, 2 MF-AF, 3 MF-PR */
+    int vf;        /* wind code (see above) */
+    int precision; /* 64: state in float64 ("plain form"); 32: state/PPM/fluxes in float32 */
+    int engine;    /* CSADV_ENGINE_* */
+    int reserved;
+    double wind_param[4];
+} csadv_options;
+
+typedef struct csadv_plan csadv_plan;
+
+/* ---------------------------------------------------------------- library */
+const char *csadv_version(void);
+const char *csadv_status_string(int status);
+/* Select the CUDA device used by plans created afterwards on this host thread. */
+int csadv_set_device(int device);
+
+/* ---------------------------------------------------------------- plan (one solve) */
+/* Replaces cubed_sphere(N, "gnomonic_equiangular", ...) (cs_datastruct.py:25-541),
+ * adv_simulation_par(...) (advection_ic.py:21-203) and init_vars_adv (advection_vars.py:19-107):
+ * builds the FP64 grid and Lagrange tables on the device, allocates the tracer state and
+ * scratch, and computes the t = 0 winds, wind halo and departure-point winds.
+ * Tracers start at zero; set them with csadv_init_tracer / csadv_set_tracer.
+ * Errors: CSADV_ERR_OPTION, CSADV_ERR_OPTION_PAIR, CSADV_ERR_ARG, CSADV_ERR_OOM. */
+int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, void *stream,
+                      csadv_plan **out);
+int csadv_plan_destroy(csadv_plan *plan);
+
+/* q0_adv (advection_ic.py:208-210) evaluated on the device at the interior cell centres
+ * (the reference's Q0 is a point value, advection_vars.py:105). */
+int csadv_init_tracer(csadv_plan *plan, int tracer, int ic, const double *ic_param, void *stream);
+/* simulation.Q = host array  /  host array = simulation.Q */
+int csadv_set_tracer(csadv_plan *plan, int tracer, const double *host, int layout, void *stream);
+int csadv_get_tracer(csadv_plan *plan, int tracer, double *host, int layout, void *stream);
+
+/* adv_time_step(cs_grid, simulation, k, t) (advection_timestep.py:19-43) for every tracer. */
+int csadv_time_step(csadv_plan *plan, int k, void *stream);
+/* update_adv(cs_grid, simulation, t) (advection_timestep.py:48-75). */
+int csadv_update_winds(csadv_plan *plan, double t, void *stream);
+/* nsteps iterations of the time loop of adv_sphere (advection_sphere.py:45-57):
+ * time step k then update_adv(k*dt), k = current_step+1 ... current_step+nsteps. */
+int csadv_advance(csadv_plan *plan, int nsteps, void *stream);
+
+/* mass_computation (diagnostics.py:14-26): sum over the interior of Q*sqrt(g)*dx*dy, FP64. */
+int csadv_mass(csadv_plan *plan, int tracer, double *mass, void *stream);
+/* compute_errors(Q, qexact_adv(lon, lat, t)) (errors.py:99-113, advection_ic.py:215-281):
+ * out = {Linf, L1, L2}, FP64 reductions.  Returns CSADV_ERR_BLOWUP when Linf > 100
+ * (output.py:44-47) after writing out. */
+int csadv_errors(csadv_plan *plan, int tracer, int ic, const double *ic_param, double t,
+                 double out[3], void *stream);
+/* simulation.CFL (advection_vars.py:89-98). */
+int csadv_get_cfl(const csadv_plan *plan, double *cfl);
+/* number of completed steps */
+int csadv_get_step(const csadv_plan *plan, int *k);
+/* divergence(cs_grid, simulation) (discrete_operators.py:18-101) of one tracer at the
+ * current state, written as an interior (N, N, 6) array; the state is not advanced. */
+int csadv_divergence(csadv_plan *plan, int tracer, double *host_div, void *stream);
+
+/* ---------------------------------------------------------------- pinned host memory */
+int csadv_host_alloc(void **ptr, size_t bytes);
+int csadv_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CSADV_H */

@@ -1,0 +1,125 @@
+"""Object wrapper over one csadv plan (one solve: grid + winds + tracers on the GPU)."""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Plan:
+    """A solve resident on the GPU.
+
+    Parameters mirror the reference's ``adv_simulation_par`` option codes (advection.par):
+    recon 1-4, dp 1-2, opsplit 1-3, et 1-3, mt 1-2, mf 1-3, and ``vf`` (reference wind
+    codes 1-4 or the benchmark winds 101-103 with ``wind_param``).  ``precision`` is 64
+    (plain form) or 32 (state, PPM and fluxes in float32).
+    """
+
+    def __init__(self, N, dt, recon=3, dp=1, opsplit=1, et=3, mt=1, mf=3, vf=1, ntracers=1, precision=64,
+                 engine=L.ENGINE_AUTO, wind_param=(0.0, 0.0, 0.0, 0.0), stream=None):
+        self.N, self.dt, self.ntracers, self.precision = int(N), float(dt), int(ntracers), int(precision)
+        self.options = dict(recon=recon, dp=dp, opsplit=opsplit, et=et, mt=mt, mf=mf, vf=vf)
+        self.stream = L.stream_handle(stream)
+        o = L.Options()
+        o.recon, o.dp, o.opsplit, o.et, o.mt, o.mf, o.vf = recon, dp, opsplit, et, mt, mf, vf
+        o.precision, o.engine = precision, engine
+        for c in range(4):
+            o.wind_param[c] = float(wind_param[c]) if c < len(wind_param) else 0.0
+        self._opts = o
+        h = ctypes.c_void_p()
+        L.check(L.lib().csadv_plan_create(self.N, self.dt, self.ntracers, ctypes.byref(o), self.stream,
+                                          ctypes.byref(h)), "csadv_plan_create")
+        self._h = h
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            L.lib().csadv_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------------ state
+    @property
+    def n(self):
+        return self.N + 8
+
+    def init_tracer(self, ic, ic_param=None, tracer=0):
+        prm = None
+        if ic_param is not None:
+            arr = (ctypes.c_double * 4)(*([float(x) for x in ic_param] + [0.0] * (4 - len(ic_param))))
+            prm = ctypes.cast(arr, ctypes.POINTER(ctypes.c_double))
+        L.check(L.lib().csadv_init_tracer(self._h, tracer, int(ic), prm, self.stream), "csadv_init_tracer")
+
+    def set_tracer(self, Q, tracer=0):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        if Q.shape == (self.n, self.n, 6):
+            layout = L.LAYOUT_FULL
+        elif Q.shape == (self.N, self.N, 6):
+            layout = L.LAYOUT_INTERIOR
+        else:
+            raise ValueError("Q must have shape (N+8, N+8, 6) or (N, N, 6)")
+        L.check(L.lib().csadv_set_tracer(self._h, tracer, Q.ctypes.data, layout, self.stream), "csadv_set_tracer")
+
+    def get_tracer(self, tracer=0, full=False, out=None):
+        shp = (self.n, self.n, 6) if full else (self.N, self.N, 6)
+        if out is None:
+            out = np.empty(shp, dtype=np.float64)
+        L.check(L.lib().csadv_get_tracer(self._h, tracer, out.ctypes.data,
+                                         L.LAYOUT_FULL if full else L.LAYOUT_INTERIOR, self.stream),
+                "csadv_get_tracer")
+        return out
+
+    # ------------------------------------------------------------------ stepping
+    def time_step(self, k):
+        L.check(L.lib().csadv_time_step(self._h, int(k), self.stream), "csadv_time_step")
+
+    def update_winds(self, t):
+        L.check(L.lib().csadv_update_winds(self._h, float(t), self.stream), "csadv_update_winds")
+
+    def advance(self, nsteps):
+        L.check(L.lib().csadv_advance(self._h, int(nsteps), self.stream), "csadv_advance")
+
+    @property
+    def step(self):
+        k = ctypes.c_int()
+        L.check(L.lib().csadv_get_step(self._h, ctypes.byref(k)))
+        return k.value
+
+    @property
+    def cfl(self):
+        c = ctypes.c_double()
+        L.check(L.lib().csadv_get_cfl(self._h, ctypes.byref(c)))
+        return c.value
+
+    # ------------------------------------------------------------------ diagnostics
+    def mass(self, tracer=0):
+        m = ctypes.c_double()
+        L.check(L.lib().csadv_mass(self._h, tracer, ctypes.byref(m), self.stream), "csadv_mass")
+        return m.value
+
+    def errors(self, ic, t, ic_param=None, tracer=0, raise_blowup=False):
+        out = (ctypes.c_double * 3)()
+        prm = None
+        if ic_param is not None:
+            arr = (ctypes.c_double * 4)(*([float(x) for x in ic_param] + [0.0] * (4 - len(ic_param))))
+            prm = ctypes.cast(arr, ctypes.POINTER(ctypes.c_double))
+        rc = L.lib().csadv_errors(self._h, tracer, int(ic), prm, float(t), out, self.stream)
+        if rc not in (L.OK, L.ERR_BLOWUP) or (rc == L.ERR_BLOWUP and raise_blowup):
+            L.check(rc, "csadv_errors")
+        return out[0], out[1], out[2]
+
+    def divergence(self, tracer=0):
+        out = np.empty((self.N, self.N, 6), dtype=np.float64)
+        L.check(L.lib().csadv_divergence(self._h, tracer, out.ctypes.data, self.stream), "csadv_divergence")
+        return out

@@ -1,0 +1,366 @@
+// C ABI of csadv (declared in include/csadv.h): plan lifecycle and step orchestration.
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/csadv.h"
+#include "cases.cuh"
+#include "common.cuh"
+#include "internal.h"
+
+namespace csadv {
+
+static thread_local int g_device = -1;
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+    if (getenv("CSADV_DEBUG")) fprintf(stderr, "csadv: %s failed: %s (%s:%d)\n", what, cudaGetErrorString(e), file, line);
+    (void)cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? CSADV_ERR_OOM : CSADV_ERR_CUDA;
+}
+
+int validate_options(const csadv_options *o, Options &out) {
+    if (!o) return CSADV_ERR_ARG;
+    if (o->recon < 1 || o->recon > 4 || o->dp < 1 || o->dp > 2 || o->opsplit < 1 || o->opsplit > 3 || o->et < 1 ||
+        o->et > 3 || o->mt < 1 || o->mt > 2 || o->mf < 1 || o->mf > 3)
+        return CSADV_ERR_OPTION;
+    if (!((o->vf >= 1 && o->vf <= 4) || o->vf == CSADV_WIND_SOLID || o->vf == CSADV_WIND_DEFORM ||
+          o->vf == CSADV_WIND_SOLID_DIV))
+        return CSADV_ERR_OPTION;
+    if (o->precision != 64 && o->precision != 32) return CSADV_ERR_OPTION;
+    if (o->engine < CSADV_ENGINE_AUTO || o->engine > CSADV_ENGINE_FUSED) return CSADV_ERR_OPTION;
+    // discrete_operators.py:49-73: SP-AVLT / SP-L04 need MT-0, SP-PL07 needs MT-PL07
+    if ((o->opsplit == SP_PL07) != (o->mt == MT_PL07)) return CSADV_ERR_OPTION_PAIR;
+    out.recon = o->recon;
+    out.dp = o->dp;
+    out.opsplit = o->opsplit;
+    out.et = o->et;
+    out.mt = o->mt;
+    out.mf = o->mf;
+    out.vf = o->vf;
+    out.precision = o->precision;
+    out.engine = o->engine;
+    for (int c = 0; c < 4; ++c) out.wp[c] = o->wind_param[c];
+    return CSADV_OK;
+}
+
+bool wind_time_dependent(const Options &o) { return wind_is_time_dependent(o.vf); }
+
+}  // namespace csadv
+
+using namespace csadv;
+
+struct csadv_plan {
+    Options opt;
+    int N = 0, T = 0;
+    double dt = 0.0;
+    DeviceArena mem;
+    Grid grid;
+    Winds w;
+    void *Q = nullptr;  // T fields of `real`
+    Scratch s{};
+    double *partials = nullptr;
+    int npart = 0;
+    double *scal = nullptr;
+    double *stage = nullptr;
+    double *tmp = nullptr;
+    int k = 0;
+    double cfl = 0.0;
+    int device = 0;
+    size_t esize() const { return opt.precision == 64 ? sizeof(double) : sizeof(float); }
+    void *tracer(int t) const { return (char *)Q + (size_t)t * grid.d.field * esize(); }
+};
+
+namespace {
+
+cudaStream_t S(void *stream) { return (cudaStream_t)stream; }
+
+template <class real>
+int scalar_halo(csadv_plan *pl, real *Q, cudaStream_t st) {
+    if (pl->opt.et == ET_DG) return launch_halo_dg<real>(Q, pl->grid, st);
+    return launch_halo_adjacent<real>(Q, Q, pl->grid, st);
+}
+
+template <class real>
+int time_step(csadv_plan *pl, cudaStream_t st, bool update, int only_tracer) {
+    int rc;
+    for (int t = 0; t < pl->T; ++t) {
+        if (only_tracer >= 0 && t != only_tracer) continue;
+        rc = scalar_halo<real>(pl, (real *)pl->tracer(t), st);
+        if (rc) return rc;
+    }
+    if (wind_time_dependent(pl->opt)) {
+        rc = wind_halo(pl->opt, pl->grid, pl->w, st);
+        if (rc) return rc;
+        rc = wind_average(pl->opt, pl->grid, pl->w, pl->dt, st);
+        if (rc) return rc;
+    }
+    for (int t = 0; t < pl->T; ++t) {
+        if (only_tracer >= 0 && t != only_tracer) continue;
+        real *Q = (real *)pl->tracer(t);
+        rc = staged_divergence<real>(pl->opt, pl->grid, pl->w, pl->dt, Q, pl->s, pl->partials, pl->npart, st);
+        if (rc) return rc;
+        rc = staged_update<real>(pl->opt, pl->grid, pl->dt, update ? Q : nullptr, pl->s, pl->partials, pl->npart,
+                                 pl->scal, st);
+        if (rc) return rc;
+    }
+    return CSADV_OK;
+}
+
+int do_time_step(csadv_plan *pl, cudaStream_t st) {
+    return pl->opt.precision == 64 ? time_step<double>(pl, st, true, -1) : time_step<float>(pl, st, true, -1);
+}
+
+int do_update_winds(csadv_plan *pl, double t, cudaStream_t st) {
+    if (!wind_time_dependent(pl->opt)) return CSADV_OK;
+    return wind_interior(pl->opt, pl->grid, pl->w, t, true, st);
+}
+
+int select_device(csadv_plan *pl) {
+    int cur = -1;
+    CSADV_CUDA(cudaGetDevice(&cur));
+    if (cur != pl->device) CSADV_CUDA(cudaSetDevice(pl->device));
+    return CSADV_OK;
+}
+
+IcParams ic_params(const csadv_plan *pl, const double *ic_param) {
+    IcParams p{};
+    if (ic_param)
+        for (int c = 0; c < 4; ++c) p.ic[c] = ic_param[c];
+    for (int c = 0; c < 4; ++c) p.wind[c] = pl->opt.wp[c];
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *csadv_version(void) { return "csadv 0.1 (sm_103a)"; }
+
+const char *csadv_status_string(int s) {
+    switch (s) {
+        case CSADV_OK: return "ok";
+        case CSADV_ERR_OPTION: return "invalid option code";
+        case CSADV_ERR_OPTION_PAIR: return "unsupported splitting / metric-tensor pair";
+        case CSADV_ERR_ARG: return "invalid argument";
+        case CSADV_ERR_OOM: return "out of memory";
+        case CSADV_ERR_CUDA: return "CUDA error";
+        case CSADV_ERR_NONFINITE: return "non-finite value in the state";
+        case CSADV_ERR_BLOWUP: return "error norm above 100 (blow-up)";
+        case CSADV_ERR_UNSUPPORTED: return "option combination not supported by this engine";
+        case CSADV_ERR_TOO_LARGE: return "request exceeds a fixed capacity";
+        default: return "unknown status";
+    }
+}
+
+int csadv_set_device(int device) {
+    int n = 0;
+    CSADV_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return CSADV_ERR_ARG;
+    CSADV_CUDA(cudaSetDevice(device));
+    g_device = device;
+    return CSADV_OK;
+}
+
+int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, void *stream, csadv_plan **out) {
+    if (!out) return CSADV_ERR_ARG;
+    *out = nullptr;
+    Options o;
+    int rc = validate_options(opt, o);
+    if (rc) return rc;
+    if (N < 8 || N > 16384 || ntracers < 1 || ntracers > 64 || !(dt > 0.0)) return CSADV_ERR_ARG;
+    if (o.engine == CSADV_ENGINE_FUSED) return CSADV_ERR_UNSUPPORTED;
+    csadv_plan *pl = new (std::nothrow) csadv_plan();
+    if (!pl) return CSADV_ERR_OOM;
+    pl->opt = o;
+    pl->N = N;
+    pl->T = ntracers;
+    pl->dt = dt;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        delete pl;
+        return CSADV_ERR_CUDA;
+    }
+    pl->device = dev;
+    cudaStream_t st = S(stream);
+    rc = build_grid(N, pl->mem, pl->grid, st);
+    if (rc) {
+        delete pl;
+        return rc;
+    }
+    const Dims d = pl->grid.d;
+    const long long F = d.field;
+    double **wa[] = {&pl->w.u_pu, &pl->w.v_pv, &pl->w.u_old, &pl->w.v_old, &pl->w.u_avg, &pl->w.v_avg,
+                     &pl->w.ulon_pc, &pl->w.vlat_pc};
+    for (double **p : wa) *p = pl->mem.alloc<double>(F);
+    const size_t es = pl->esize();
+    pl->Q = pl->mem.alloc<char>((long long)ntracers * F * es);
+    void **sa[] = {&pl->s.Qx, &pl->s.Qy, &pl->s.qLx, &pl->s.qRx, &pl->s.qLy, &pl->s.qRy, &pl->s.fx, &pl->s.fy, &pl->s.div};
+    for (void **p : sa) *p = pl->mem.alloc<char>(F * es);
+    pl->npart = staged_partial_count(pl->grid);
+    pl->partials = pl->mem.alloc<double>(pl->npart);
+    pl->scal = pl->mem.alloc<double>(8);
+    pl->stage = pl->mem.alloc<double>((long long)NFACE * d.n * d.n);
+    pl->tmp = pl->mem.alloc<double>(3LL * diag_partials(pl->grid) + 8);
+    if (!pl->mem.ok()) {
+        delete pl;
+        return CSADV_ERR_OOM;
+    }
+    bool ok = true;
+    for (double **p : wa) ok = ok && cudaMemsetAsync(*p, 0, F * sizeof(double), st) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(pl->Q, 0, (size_t)ntracers * F * es, st) == cudaSuccess;
+    for (void **p : sa) ok = ok && cudaMemsetAsync(*p, 0, F * es, st) == cudaSuccess;
+    if (!ok) {
+        delete pl;
+        return CSADV_ERR_CUDA;
+    }
+    // init_vars_adv (advection_vars.py:19-107): t = 0 winds, wind halo, old <- current,
+    // departure-point winds, CFL
+    rc = wind_interior(o, pl->grid, pl->w, 0.0, false, st);
+    if (!rc) rc = wind_halo(o, pl->grid, pl->w, st);
+    if (!rc && cudaMemcpyAsync(pl->w.u_old, pl->w.u_pu, F * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        rc = CSADV_ERR_CUDA;
+    if (!rc && cudaMemcpyAsync(pl->w.v_old, pl->w.v_pv, F * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        rc = CSADV_ERR_CUDA;
+    if (!rc) rc = wind_average(o, pl->grid, pl->w, dt, st);
+    if (!rc) rc = wind_cfl(pl->grid, pl->w, dt, pl->tmp, pl->cfl, st);
+    if (rc) {
+        delete pl;
+        return rc;
+    }
+    *out = pl;
+    return CSADV_OK;
+}
+
+int csadv_plan_destroy(csadv_plan *plan) {
+    if (!plan) return CSADV_ERR_ARG;
+    select_device(plan);
+    cudaDeviceSynchronize();
+    delete plan;
+    return CSADV_OK;
+}
+
+int csadv_init_tracer(csadv_plan *pl, int tracer, int ic, const double *ic_param, void *stream) {
+    if (!pl || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    if (!((ic >= 1 && ic <= 4) || (ic >= CSADV_IC_HILL && ic <= CSADV_IC_SMOOTH_BELLS))) return CSADV_ERR_OPTION;
+    if (ic == CSADV_IC_HILL && !ic_param) return CSADV_ERR_ARG;
+    IcParams p = ic_params(pl, ic_param);
+    if (pl->opt.precision == 64) return init_tracer<double>(pl->grid, ic, pl->opt.vf, p, (double *)pl->tracer(tracer), S(stream));
+    return init_tracer<float>(pl->grid, ic, pl->opt.vf, p, (float *)pl->tracer(tracer), S(stream));
+}
+
+int csadv_set_tracer(csadv_plan *pl, int tracer, const double *host, int layout, void *stream) {
+    if (!pl || !host || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    if (layout != CSADV_LAYOUT_FULL && layout != CSADV_LAYOUT_INTERIOR) return CSADV_ERR_ARG;
+    const Dims d = pl->grid.d;
+    const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
+    cudaStream_t st = S(stream);
+    CSADV_CUDA(cudaMemcpyAsync(pl->stage, host, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (pl->opt.precision == 64) return tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, true, st);
+    return tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, true, st);
+}
+
+int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void *stream) {
+    if (!pl || !host || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    if (layout != CSADV_LAYOUT_FULL && layout != CSADV_LAYOUT_INTERIOR) return CSADV_ERR_ARG;
+    const Dims d = pl->grid.d;
+    const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
+    cudaStream_t st = S(stream);
+    int rc = pl->opt.precision == 64
+                 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, false, st)
+                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, false, st);
+    if (rc) return rc;
+    CSADV_CUDA(cudaMemcpyAsync(host, pl->stage, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CSADV_CUDA(cudaStreamSynchronize(st));
+    return CSADV_OK;
+}
+
+int csadv_time_step(csadv_plan *pl, int k, void *stream) {
+    if (!pl) return CSADV_ERR_ARG;
+    int rc = do_time_step(pl, S(stream));
+    if (rc) return rc;
+    pl->k = k;
+    return CSADV_OK;
+}
+
+int csadv_update_winds(csadv_plan *pl, double t, void *stream) {
+    if (!pl) return CSADV_ERR_ARG;
+    return do_update_winds(pl, t, S(stream));
+}
+
+int csadv_advance(csadv_plan *pl, int nsteps, void *stream) {
+    if (!pl || nsteps < 0) return CSADV_ERR_ARG;
+    cudaStream_t st = S(stream);
+    for (int s = 0; s < nsteps; ++s) {
+        int k = pl->k + 1;
+        int rc = do_time_step(pl, st);
+        if (rc) return rc;
+        rc = do_update_winds(pl, k * pl->dt, st);
+        if (rc) return rc;
+        pl->k = k;
+    }
+    return CSADV_OK;
+}
+
+int csadv_mass(csadv_plan *pl, int tracer, double *mass, void *stream) {
+    if (!pl || !mass || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    if (pl->opt.precision == 64) return diag_mass<double>(pl->grid, (const double *)pl->tracer(tracer), pl->tmp, *mass, S(stream));
+    return diag_mass<float>(pl->grid, (const float *)pl->tracer(tracer), pl->tmp, *mass, S(stream));
+}
+
+int csadv_errors(csadv_plan *pl, int tracer, int ic, const double *ic_param, double t, double out[3], void *stream) {
+    if (!pl || !out || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    if (!((ic >= 1 && ic <= 4) || (ic >= CSADV_IC_HILL && ic <= CSADV_IC_SMOOTH_BELLS))) return CSADV_ERR_OPTION;
+    if (ic == CSADV_IC_HILL && !ic_param) return CSADV_ERR_ARG;
+    IcParams p = ic_params(pl, ic_param);
+    int rc = pl->opt.precision == 64
+                 ? diag_errors<double>(pl->grid, (const double *)pl->tracer(tracer), ic, pl->opt.vf, p, t, pl->tmp, out, S(stream))
+                 : diag_errors<float>(pl->grid, (const float *)pl->tracer(tracer), ic, pl->opt.vf, p, t, pl->tmp, out, S(stream));
+    if (rc) return rc;
+    if (!(out[0] == out[0])) return CSADV_ERR_NONFINITE;
+    if (out[0] > 100.0) return CSADV_ERR_BLOWUP;
+    return CSADV_OK;
+}
+
+int csadv_get_cfl(const csadv_plan *pl, double *cfl) {
+    if (!pl || !cfl) return CSADV_ERR_ARG;
+    *cfl = pl->cfl;
+    return CSADV_OK;
+}
+
+int csadv_get_step(const csadv_plan *pl, int *k) {
+    if (!pl || !k) return CSADV_ERR_ARG;
+    *k = pl->k;
+    return CSADV_OK;
+}
+
+int csadv_divergence(csadv_plan *pl, int tracer, double *host_div, void *stream) {
+    if (!pl || !host_div || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    cudaStream_t st = S(stream);
+    int rc = pl->opt.precision == 64 ? time_step<double>(pl, st, false, tracer) : time_step<float>(pl, st, false, tracer);
+    if (rc) return rc;
+    rc = pl->opt.precision == 64 ? tracer_io<double>(pl->grid, (double *)pl->s.div, pl->stage, CSADV_LAYOUT_INTERIOR, false, st)
+                                 : tracer_io<float>(pl->grid, (float *)pl->s.div, pl->stage, CSADV_LAYOUT_INTERIOR, false, st);
+    if (rc) return rc;
+    const Dims d = pl->grid.d;
+    CSADV_CUDA(cudaMemcpyAsync(host_div, pl->stage, (size_t)NFACE * d.N * d.N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CSADV_CUDA(cudaStreamSynchronize(st));
+    return CSADV_OK;
+}
+
+int csadv_host_alloc(void **ptr, size_t bytes) {
+    if (!ptr) return CSADV_ERR_ARG;
+    if (cudaMallocHost(ptr, bytes) != cudaSuccess) {
+        (void)cudaGetLastError();
+        *ptr = nullptr;
+        return CSADV_ERR_OOM;
+    }
+    return CSADV_OK;
+}
+
+int csadv_host_free(void *ptr) {
+    if (!ptr) return CSADV_ERR_ARG;
+    CSADV_CUDA(cudaFreeHost(ptr));
+    return CSADV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,263 @@
+// Grid generation: gnomonic equiangular cubed sphere, FP64, on the device.
+//
+// Restates cs_datastruct.py:197-493 (points, tangent vectors, metric tensor, lat-lon /
+// contravariant coefficients) with cs_transform.py:41-96 (equiangular map), :245-397
+// (tangent vectors) and sphgeo.py:29-33, 72-88.  The 1-D angular coordinates follow
+// numpy.linspace exactly (host side) so every later rounding matches the reference's
+// sequence of operations; transcendental functions are CUDA's (within 2 ulp of libm).
+//
+// The Lagrange ghost-cell tables (lagrange.py:28-163) are built on the host from the
+// same formulas (they are tiny: 4 x (N+8) entries).
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace csadv {
+
+
+
+// numpy.linspace(start, stop, num): arange(num) * step + start, last element = stop
+std::vector<double> linspace(double start, double stop, int num) {
+    std::vector<double> y(num);
+    double step = (stop - start) / (double)(num - 1);
+    for (int i = 0; i < num; ++i) y[i] = (double)i * step + start;
+    y[num - 1] = stop;
+    return y;
+}
+
+void angular_axes(int N, std::vector<double> &xc, std::vector<double> &xe, double &dx) {
+    const double a = M_PI / 4.0;
+    dx = (a - (-a)) / N;
+    xe = linspace(-a - NG * dx, a + NG * dx, N + 1 + 2 * NG);
+    xc = linspace(-a + dx / 2.0 - NG * dx, a - dx / 2.0 + NG * dx, N + 2 * NG);
+}
+
+// ---------------------------------------------------------------- device geometry
+__host__ __device__ inline void panel_xyz(int p, double invD, double XoD, double YoD, double &X, double &Y,
+                                          double &Z) {
+    switch (p) {  // cs_transform.py:63-91
+        case 0: X = invD; Y = XoD; Z = YoD; break;
+        case 1: X = -XoD; Y = invD; Z = YoD; break;
+        case 2: X = -invD; Y = -XoD; Z = YoD; break;
+        case 3: X = XoD; Y = -invD; Z = YoD; break;
+        case 4: X = -YoD; Y = XoD; Z = invD; break;
+        default: X = YoD; Y = XoD; Z = -invD; break;
+    }
+}
+
+// equiangular tangent vectors (cs_transform.py:245-397): the equidistant tangent at
+// (a tan x, a tan y) scaled by a / cos^2
+__device__ inline void tangents(int p, double x, double y, double ex[3], double ey[3]) {
+    const double a = 1.0 / sqrt(3.0);
+    double xe = a * tan(x), ye = a * tan(y);
+    double r2 = a * a + xe * xe + ye * ye;
+    double invr = 1.0 / pow(sqrt(r2), 3.0);
+    double a2 = a * a, ax = a * xe, ay = a * ye, xy = xe * ye;
+    double bx = (a2 + ye * ye) * invr, by = (a2 + xe * xe) * invr;
+    double axr = ax * invr, ayr = ay * invr, xyr = xy * invr;
+    switch (p) {
+        case 0: ex[0] = -axr; ex[1] = bx; ex[2] = -xyr; ey[0] = -ayr; ey[1] = -xyr; ey[2] = by; break;
+        case 1: ex[0] = -bx; ex[1] = -axr; ex[2] = -xyr; ey[0] = xyr; ey[1] = -ayr; ey[2] = by; break;
+        case 2: ex[0] = axr; ex[1] = -bx; ex[2] = -xyr; ey[0] = ayr; ey[1] = xyr; ey[2] = by; break;
+        case 3: ex[0] = bx; ex[1] = axr; ex[2] = -xyr; ey[0] = -xyr; ey[1] = ayr; ey[2] = by; break;
+        case 4: ex[0] = xyr; ex[1] = bx; ex[2] = -axr; ey[0] = -by; ey[1] = -xyr; ey[2] = -ayr; break;
+        default: ex[0] = -xyr; ex[1] = bx; ex[2] = axr; ey[0] = by; ey[1] = -xyr; ey[2] = ayr; break;
+    }
+    double cx = cos(x), cy = cos(y);
+    double c2x = cx * cx, c2y = cy * cy;
+    for (int c = 0; c < 3; ++c) {
+        ex[c] = a * ex[c] / c2x;
+        ey[c] = a * ey[c] / c2y;
+    }
+}
+
+struct PointOut {
+    double *lon, *lat;   // 6 planes
+    double *coef[5];     // ex.elon ex.elat ey.elon ey.elat det (det may be null)
+    double *metric;      // single plane
+};
+
+__global__ void k_grid_points(Dims d, const double *__restrict__ xs, int nx, const double *__restrict__ ys, int ny,
+                              PointOut out) {
+    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long total = (long long)NFACE * nx * ny;
+    if (tid >= total) return;
+    int j = (int)(tid % ny);
+    int i = (int)((tid / ny) % nx);
+    int p = (int)(tid / ((long long)nx * ny));
+    double x = xs[i], y = ys[j];
+    double tx = tan(x), ty = tan(y);
+    double D = sqrt(1.0 + tx * tx + ty * ty);
+    double invD = 1.0 / D;
+    double X, Y, Z;
+    panel_xyz(p, invD, invD * tx, invD * ty, X, Y, Z);
+    double lon = atan2(Y, X);
+    double lat = atan2(Z, hypot(X, Y));
+    long long o = at(d, p, i, j);
+    out.lon[o] = lon;
+    out.lat[o] = lat;
+    double ex[3], ey[3];
+    tangents(p, x, y, ex, ey);
+    double sl = sin(lon), cl = cos(lon), sp = sin(lat), cp = cos(lat);
+    double elon[3] = {-sl, cl, 0.0};
+    double elat[3] = {-sp * cl, -sp * sl, cp};
+    double exlon = ex[0] * elon[0] + ex[1] * elon[1] + ex[2] * elon[2];
+    double exlat = ex[0] * elat[0] + ex[1] * elat[1] + ex[2] * elat[2];
+    double eylon = ey[0] * elon[0] + ey[1] * elon[1] + ey[2] * elon[2];
+    double eylat = ey[0] * elat[0] + ey[1] * elat[1] + ey[2] * elat[2];
+    out.coef[0][o] = exlon;
+    out.coef[1][o] = exlat;
+    out.coef[2][o] = eylon;
+    out.coef[3][o] = eylat;
+    if (out.coef[4]) out.coef[4][o] = exlon * eylat - eylon * exlat;
+    if (p == 0) {  // metric tensor of panel 0, used for every panel (cs_datastruct.py:407-446)
+        double dot = ex[0] * ey[0] + ex[1] * ey[1] + ex[2] * ey[2];
+        double nx2 = ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2];
+        double ny2 = ey[0] * ey[0] + ey[1] * ey[1] + ey[2] * ey[2];
+        out.metric[at2(d, i, j)] = sqrt(-(dot * dot) + nx2 * ny2);
+    }
+}
+
+// sum of g_pc^2 over the interior of all panels (discrete_operators.py:99), fixed order
+__global__ void k_sum_g2(Dims d, const double *__restrict__ g, double *out) {
+    __shared__ double red[1024];
+    double acc = 0.0;
+    long long cnt = (long long)d.N * d.N;
+    for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+        int i = d.i0 + (int)(t / d.N), j = d.i0 + (int)(t % d.N);
+        double v = g[at2(d, i, j)];
+        acc += v * v;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = 6.0 * red[0];
+}
+
+// ---------------------------------------------------------------- Lagrange tables (host)
+// lagrange.py:28-163: degree-3 weights at the ghost-cell centres of panel 0's east side,
+// in panel 1's angular coordinate, reused for every panel and side.
+int lagrange_tables(int N, const std::vector<double> &xc, double dx, std::vector<double> &w, std::vector<int> &kmin) {
+    const int n = N + 2 * NG, i0 = NG, iend = NG + N, order = 4, degree = 3;
+    std::vector<double> yg(NG * n), ysup(NG * n);
+    for (int g = 0; g < NG; ++g) {
+        for (int k = 0; k < n; ++k) {
+            // ghost centre of panel 0 (x = xc[iend+g], y = xc[k]); panel-1 inverse tan y = Z/Y
+            double tx = tan(xc[iend + g]), ty = tan(xc[k]);
+            double invD = 1.0 / sqrt(1.0 + tx * tx + ty * ty);
+            yg[g * n + k] = atan((invD * ty) / (invD * tx));
+            // support centre of panel 1 (x = xc[i0+g], y = xc[k]): Y = invD, Z = invD tan y
+            tx = tan(xc[i0 + g]);
+            invD = 1.0 / sqrt(1.0 + tx * tx + ty * ty);
+            ysup[g * n + k] = atan((invD * ty) / invD);
+        }
+    }
+    w.assign((size_t)NG * n * order, 0.0);
+    kmin.assign((size_t)NG * n, 0);
+    for (int g = 0; g < NG; ++g) {
+        for (int k = 0; k < n; ++k) {
+            double K = (yg[g * n + k] - ysup[g * n + 0]) / dx;
+            double kmax = K + 2.0;  // ceil(order / 2)
+            double kmn = kmax - order + 1;
+            if (k >= i0 && k < iend) {
+                if (kmax >= iend) {
+                    kmax = iend - 1;
+                    kmn = kmax - order + 1;
+                } else if (kmn < i0) {
+                    kmn = i0;
+                    kmax = kmn + order - 1;
+                }
+            } else if (k >= iend) {
+                if (kmax >= n) {
+                    kmax = n - 1;
+                    kmn = kmax - order + 1;
+                }
+            } else if (kmn < 0) {
+                kmn = 0;
+                kmax = kmn + order - 1;
+            }
+            int a = (int)kmn, b = (int)kmax;  // truncation, as ndarray.astype(int)
+            if (b - a != degree || a < 0 || b >= n) return CSADV_ERR_ARG;
+            if (k >= i0 && k < iend && (a < i0 || b > iend)) return CSADV_ERR_ARG;
+            kmin[g * n + k] = a;
+            const double x = yg[g * n + k];
+            for (int l = 0; l < order; ++l) {
+                double L = 1.0;
+                for (int m = 0; m < order; ++m)
+                    if (m != l) L = L * (x - ysup[g * n + a + m]) / (ysup[g * n + a + l] - ysup[g * n + a + m]);
+                w[((size_t)g * n + k) * order + l] = L;
+            }
+        }
+    }
+    return CSADV_OK;
+}
+
+// Build every FP64 geometry array of resolution N into `mem` (device) and fill `grid`.
+int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
+    Dims d = make_dims(N);
+    grid.d = d;
+    std::vector<double> xc, xe;
+    double dx;
+    angular_axes(N, xc, xe, dx);
+    grid.dx = dx;
+    const long long P1 = d.plane, P6 = d.field;
+    double *g_pc = mem.alloc<double>(P1), *g_pu = mem.alloc<double>(P1), *g_pv = mem.alloc<double>(P1);
+    double *lon_pc = mem.alloc<double>(P6), *lat_pc = mem.alloc<double>(P6);
+    double *lon_pu = mem.alloc<double>(P6), *lat_pu = mem.alloc<double>(P6);
+    double *lon_pv = mem.alloc<double>(P6), *lat_pv = mem.alloc<double>(P6);
+    double *cu[5], *cv[5], *cc[4];
+    for (int c = 0; c < 5; ++c) { cu[c] = mem.alloc<double>(P6); cv[c] = mem.alloc<double>(P6); }
+    for (int c = 0; c < 4; ++c) cc[c] = mem.alloc<double>(P6);
+    double *xs_dev = mem.alloc<double>(xc.size() + xe.size());
+    double *a2 = mem.alloc<double>(1);
+    std::vector<double> lw;
+    std::vector<int> lk;
+    int rc = lagrange_tables(N, xc, dx, lw, lk);
+    if (rc != CSADV_OK) return rc;
+    double *lag_w = mem.alloc<double>(lw.size());
+    int *lag_k = mem.alloc<int>(lk.size());
+    if (!mem.ok()) return CSADV_ERR_OOM;
+    for (double *g : {g_pc, g_pu, g_pv}) CSADV_CUDA(cudaMemsetAsync(g, 0, P1 * sizeof(double), st));
+    CSADV_CUDA(cudaMemcpyAsync(xs_dev, xc.data(), xc.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaMemcpyAsync(xs_dev + xc.size(), xe.data(), xe.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaMemcpyAsync(lag_w, lw.data(), lw.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaMemcpyAsync(lag_k, lk.data(), lk.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    const double *xcd = xs_dev, *xed = xs_dev + xc.size();
+    const int n = d.n;
+    PointOut o;
+    o.lon = lon_pc; o.lat = lat_pc; o.metric = g_pc;
+    for (int c = 0; c < 4; ++c) o.coef[c] = cc[c];
+    o.coef[4] = nullptr;
+    long long tot = (long long)NFACE * n * n;
+    k_grid_points<<<ceil_div(tot, 128), 128, 0, st>>>(d, xcd, n, xcd, n, o);
+    o.lon = lon_pu; o.lat = lat_pu; o.metric = g_pu;
+    for (int c = 0; c < 5; ++c) o.coef[c] = cu[c];
+    tot = (long long)NFACE * (n + 1) * n;
+    k_grid_points<<<ceil_div(tot, 128), 128, 0, st>>>(d, xed, n + 1, xcd, n, o);
+    o.lon = lon_pv; o.lat = lat_pv; o.metric = g_pv;
+    for (int c = 0; c < 5; ++c) o.coef[c] = cv[c];
+    k_grid_points<<<ceil_div(tot, 128), 128, 0, st>>>(d, xcd, n, xed, n + 1, o);
+    k_sum_g2<<<1, 1024, 0, st>>>(d, g_pc, a2);
+    CSADV_CUDA(cudaGetLastError());
+    double a2h = 0.0;
+    CSADV_CUDA(cudaMemcpyAsync(&a2h, a2, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CSADV_CUDA(cudaStreamSynchronize(st));
+    grid.g_pc = g_pc; grid.g_pu = g_pu; grid.g_pv = g_pv;
+    grid.lon_pc = lon_pc; grid.lat_pc = lat_pc;
+    grid.lon_pu = lon_pu; grid.lat_pu = lat_pu;
+    grid.lon_pv = lon_pv; grid.lat_pv = lat_pv;
+    for (int c = 0; c < 5; ++c) { grid.cu[c] = cu[c]; grid.cv[c] = cv[c]; }
+    for (int c = 0; c < 4; ++c) grid.cc[c] = cc[c];
+    grid.lag_w = lag_w;
+    grid.lag_k = lag_k;
+    grid.a2 = a2h;
+    return CSADV_OK;
+}
+
+}  // namespace csadv

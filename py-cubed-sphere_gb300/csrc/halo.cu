@@ -1,0 +1,126 @@
+// Ghost cells of cell-centred fields across the cube edges.
+//
+// k_halo_dg       -- ET-DG: degree-3 Lagrange interpolation along the neighbour panel's
+//                    edge (interpolation.py:154-314 with halo_data.py:15-185).  The
+//                    reference fills the four side strips first and then the 4x4 corner
+//                    blocks from the refreshed halo of the east/west neighbours.  Here one
+//                    launch does both: a corner thread recomputes the neighbour's side-strip
+//                    values it needs (same operations, same bits) instead of waiting for
+//                    them, so no grid-wide barrier is needed and no thread reads a ghost cell
+//                    that another thread writes.
+// k_halo_adjacent -- ET-S72 / ET-PL07: copy of the neighbour's cells (interpolation.py:320-340,
+//                    halo_data.py:191-400).  Only the strips along the interior of each edge
+//                    are written; the reference also writes the corner blocks, but with
+//                    these edge treatments no corner value reaches an interior result.
+//
+// Both are compiled without FMA contraction: each product and sum is rounded as in numpy,
+// so the FP64 form reproduces the reference's halo values bit for bit.
+#include "common.cuh"
+#include "internal.h"
+
+namespace csadv {
+
+// value of the ghost cell at depth `dep` outside side s of panel p, along index k
+// (k inside the edge's interior range); computed in FP64 from interior cells only
+template <class real>
+__device__ double side_ghost(const real *__restrict__ F, const Dims &d, const double *__restrict__ W,
+                             const int *__restrict__ K, int p, int s, int dep, int k) {
+    const Conn c = c_conn[p][s];
+    const int n = d.n;
+    const int k0 = K[dep * n + k];
+    const double *w = W + ((long long)dep * n + k) * 4;
+    double prod[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        int kk = k0 + m;
+        int along = c.rev ? n - 1 - kk : kk;
+        int i, j;
+        inside_ij(d, c.qs, dep, along, i, j);
+        prod[m] = (double)F[at(d, c.q, i, j)] * w[m];
+    }
+    return ((prod[0] + prod[1]) + prod[2]) + prod[3];
+}
+
+// value of cell (i, j) of panel q where (i, j) is interior or in a side strip (not a corner)
+template <class real>
+__device__ double cell_or_side_ghost(const real *__restrict__ F, const Dims &d, const double *__restrict__ W,
+                                     const int *__restrict__ K, int q, int i, int j) {
+    if (i >= d.iend) return (double)(real)side_ghost(F, d, W, K, q, SIDE_E, i - d.iend, j);
+    if (i < d.i0) return (double)(real)side_ghost(F, d, W, K, q, SIDE_W, d.i0 - 1 - i, j);
+    if (j >= d.iend) return (double)(real)side_ghost(F, d, W, K, q, SIDE_N, j - d.iend, i);
+    if (j < d.i0) return (double)(real)side_ghost(F, d, W, K, q, SIDE_S, d.i0 - 1 - j, i);
+    return (double)F[at(d, q, i, j)];
+}
+
+template <class real>
+__global__ void k_halo_dg(real *F, Dims d, const double *__restrict__ W, const int *__restrict__ K) {
+    const int n = d.n;
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= NFACE * 4 * NG * n) return;
+    int k = tid % n;
+    int dep = (tid / n) % NG;
+    int s = (tid / (n * NG)) % 4;
+    int p = tid / (n * NG * 4);
+    int gi, gj;
+    ghost_ij(d, s, dep, k, gi, gj);
+    if (is_interior(d, k)) {
+        F[at(d, p, gi, gj)] = (real)side_ghost(F, d, W, K, p, s, dep, k);
+        return;
+    }
+    if (s == SIDE_N || s == SIDE_S) return;  // corner blocks are filled from the E/W sides
+    const Conn c = c_conn[p][s];
+    const int k0 = K[dep * n + k];
+    const double *w = W + ((long long)dep * n + k) * 4;
+    double prod[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        int kk = k0 + m;
+        int along = c.rev ? n - 1 - kk : kk;
+        int i, j;
+        inside_ij(d, c.qs, dep, along, i, j);
+        prod[m] = cell_or_side_ghost(F, d, W, K, c.q, i, j) * w[m];
+    }
+    F[at(d, p, gi, gj)] = (real)(((prod[0] + prod[1]) + prod[2]) + prod[3]);
+}
+
+template <class real>
+__global__ void k_halo_adjacent(real *Qx, real *Qy, Dims d) {
+    const int N = d.N;
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= NFACE * 4 * NG * N) return;
+    int k = d.i0 + tid % N;
+    int dep = (tid / N) % NG;
+    int s = (tid / (N * NG)) % 4;
+    int p = tid / (N * NG * 4);
+    const Conn c = c_conn[p][s];
+    real *dst = (s == SIDE_E || s == SIDE_W) ? Qy : Qx;
+    const real *src = (c.qs == SIDE_E || c.qs == SIDE_W) ? Qy : Qx;
+    int along = c.rev ? d.n - 1 - k : k;
+    int si, sj, gi, gj;
+    inside_ij(d, c.qs, dep, along, si, sj);
+    ghost_ij(d, s, dep, k, gi, gj);
+    dst[at(d, p, gi, gj)] = src[at(d, c.q, si, sj)];
+}
+
+template <class real>
+int launch_halo_dg(real *F, const Grid &g, cudaStream_t st) {
+    int tot = NFACE * 4 * NG * g.d.n;
+    k_halo_dg<real><<<ceil_div(tot, 128), 128, 0, st>>>(F, g.d, g.lag_w, g.lag_k);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+template <class real>
+int launch_halo_adjacent(real *Qx, real *Qy, const Grid &g, cudaStream_t st) {
+    int tot = NFACE * 4 * NG * g.d.N;
+    k_halo_adjacent<real><<<ceil_div(tot, 128), 128, 0, st>>>(Qx, Qy, g.d);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+template int launch_halo_dg<double>(double *, const Grid &, cudaStream_t);
+template int launch_halo_dg<float>(float *, const Grid &, cudaStream_t);
+template int launch_halo_adjacent<double>(double *, double *, const Grid &, cudaStream_t);
+template int launch_halo_adjacent<float>(float *, float *, const Grid &, cudaStream_t);
+
+}  // namespace csadv

@@ -1,0 +1,110 @@
+// Internal (non-ABI) declarations shared by the csadv translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "../../include/csadv.h"
+#include "common.cuh"
+
+namespace csadv {
+
+// Record the first CUDA error and turn it into CSADV_ERR_CUDA.
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+#define CSADV_CUDA(call)                                                          \
+    do {                                                                          \
+        cudaError_t _e = (call);                                                  \
+        if (_e != cudaSuccess) return ::csadv::cuda_fail(_e, #call, __FILE__, __LINE__); \
+    } while (0)
+
+// Owner of a plan's device allocations (one cudaMalloc per array, freed together).
+class DeviceArena {
+   public:
+    template <class T>
+    T *alloc(long long count) {
+        if (failed_) return nullptr;
+        void *p = nullptr;
+        size_t bytes = (size_t)(count > 0 ? count : 1) * sizeof(T);
+        if (cudaMalloc(&p, bytes) != cudaSuccess) {
+            (void)cudaGetLastError();
+            failed_ = true;
+            return nullptr;
+        }
+        ptrs_.push_back(p);
+        bytes_ += bytes;
+        return static_cast<T *>(p);
+    }
+    bool ok() const { return !failed_; }
+    size_t bytes() const { return bytes_; }
+    void release() {
+        for (void *p : ptrs_) cudaFree(p);
+        ptrs_.clear();
+        bytes_ = 0;
+        failed_ = false;
+    }
+    ~DeviceArena() { release(); }
+
+   private:
+    std::vector<void *> ptrs_;
+    size_t bytes_ = 0;
+    bool failed_ = false;
+};
+
+struct Options {
+    int recon, dp, opsplit, et, mt, mf, vf, precision, engine;
+    double wp[4];
+};
+
+enum { ET_S72 = 1, ET_PL07 = 2, ET_DG = 3 };
+enum { MF_0 = 1, MF_AF = 2, MF_PR = 3 };
+enum { SP_AVLT = 1, SP_L04 = 2, SP_PL07 = 3 };
+enum { MT_0 = 1, MT_PL07 = 2 };
+enum { REC_PPM0 = 1, REC_CW84 = 2, REC_PL07 = 3, REC_L04 = 4 };
+
+// IC parameters (meaning per IC code) and the wind parameters the exact solution needs
+struct IcParams {
+    double ic[4];
+    double wind[4];
+};
+
+int validate_options(const csadv_options *o, Options &out);
+bool wind_time_dependent(const Options &o);
+
+// grid.cu
+int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st);
+std::vector<double> linspace(double start, double stop, int num);
+
+// Per-tracer scratch of the staged engine (type-erased; element type = real)
+struct Scratch {
+    void *Qx, *Qy, *qLx, *qRx, *qLy, *qRy, *fx, *fy, *div;
+};
+
+// Launch wrappers (defined in the .cu files)
+template <class real> int launch_halo_dg(real *F, const Grid &g, cudaStream_t st);
+template <class real> int launch_halo_adjacent(real *Qx, real *Qy, const Grid &g, cudaStream_t st);
+template <class real>
+int staged_divergence(const Options &o, const Grid &g, const Winds &w, double dt, real *Q, const Scratch &s,
+                      double *partials, int npart, cudaStream_t st);
+template <class real>
+int staged_update(const Options &o, const Grid &g, double dt, real *Q, const Scratch &s, double *partials,
+                  int npart, double *scal, cudaStream_t st);
+int staged_partial_count(const Grid &g);
+
+int wind_interior(const Options &o, const Grid &g, Winds &w, double t, bool keep_old, cudaStream_t st);
+int wind_halo(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
+int wind_average(const Options &o, const Grid &g, Winds &w, double dt, cudaStream_t st);
+int wind_cfl(const Grid &g, const Winds &w, double dt, double *dev_tmp, double &cfl, cudaStream_t st);
+
+int diag_partials(const Grid &g);
+template <class real>
+int init_tracer(const Grid &g, int ic, int vf, const IcParams &prm, real *Q, cudaStream_t st);
+template <class real>
+int tracer_io(const Grid &g, real *Q, double *dev_stage, int layout, bool to_native, cudaStream_t st);
+template <class real>
+int diag_mass(const Grid &g, const real *Q, double *dev_tmp, double &mass, cudaStream_t st);
+template <class real>
+int diag_errors(const Grid &g, const real *Q, int ic, int vf, const IcParams &prm, double t, double *dev_tmp,
+                double out[3], cudaStream_t st);
+
+}  // namespace csadv

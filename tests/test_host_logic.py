@@ -1,0 +1,72 @@
+"""Host-side logic of the drop-in layer (CPU only): parameter files, option decoding, errors."""
+import os
+
+import numpy as np
+import pytest
+
+import csadv
+from csadv import advection, configuration
+from oracle.solver import check_options, OptionError
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_par_files_parse_like_the_reference(golden_dir):
+    z = np.load(os.path.join(golden_dir, "par.npz"))
+    conf = configuration.get_parameters(os.path.join(ROOT, "par"), verbose=False)
+    adv = configuration.get_advection_parameters(os.path.join(ROOT, "par"), verbose=False)
+    assert [str(x) for x in conf] == list(z["configuration"])
+    assert [repr(x) for x in adv] == list(z["advection"])
+
+
+def test_par_file_errors_exit(tmp_path):
+    (tmp_path / "configuration.par").write_text("#t\n#N\n16\n#grid\n9\n#l\n0\n#s\n0\n#tc\n5\n#m\n2\n")
+    with pytest.raises(SystemExit):
+        configuration.get_parameters(str(tmp_path), verbose=False)
+    with pytest.raises(SystemExit):
+        configuration.get_advection_parameters(str(tmp_path / "missing"), verbose=False)
+
+
+@pytest.mark.parametrize("bad", [dict(ic=9), dict(vf=7), dict(recon=5), dict(dp=3), dict(opsplit=0), dict(et=4),
+                                 dict(mt=3), dict(mf=0), dict(tc=3)])
+def test_invalid_option_codes_exit_like_the_reference(bad, capsys):
+    g = advection.cubed_sphere(16)
+    args = dict(dt=0.01, Tf=5.0, ic=2, vf=1, tc=1, recon=3, dp=1, opsplit=1, et=3, mt=1, mf=3)
+    args.update(bad)
+    with pytest.raises(SystemExit):
+        advection.adv_simulation_par(g, **args)
+    assert "invalid" in capsys.readouterr().out.lower()
+
+
+def test_option_pairs_match_the_oracle_and_reference():
+    # SP-AVLT / SP-L04 need MT-0; SP-PL07 needs MT-PL07 (discrete_operators.py:49-73)
+    for sp in (1, 2, 3):
+        for mt in (1, 2):
+            ok = (sp in (1, 2)) == (mt == 1)
+            if ok:
+                check_options(3, 1, sp, 3, mt, 3)
+            else:
+                with pytest.raises(OptionError):
+                    check_options(3, 1, sp, 3, mt, 3)
+
+
+def test_unsupported_splitting_is_an_unbound_local_error():
+    assert issubclass(advection.UnsupportedSplitting, UnboundLocalError)
+
+
+def test_only_the_equiangular_grid_is_built():
+    with pytest.raises(SystemExit):
+        advection.cubed_sphere(16, "gnomonic_equidistant")
+    g = advection.cubed_sphere(24)
+    assert (g.i0, g.iend, g.ng) == (4, 28, 8)
+    assert g.dx == (np.pi / 4 - (-np.pi / 4)) / 24
+
+
+def test_compute_errors_host():
+    a = np.zeros((4, 4, 6))
+    b = np.ones((4, 4, 6)) * 2.0
+    b[0, 0, 0] = 5.0
+    linf, l1, l2 = csadv.compute_errors(a, b)
+    assert linf == 5.0
+    assert l1 == pytest.approx((95 * 2 + 5) / 96)
+    assert l2 == pytest.approx(np.sqrt((95 * 4 + 25) / 96))
