@@ -72,7 +72,7 @@ typedef struct csadv_options {
     int vf;        /* wind code (see above) */
     int precision; /* 64: state in float64 ("plain form"); 32: state/PPM/fluxes in float32 */
     int engine;    /* CSADV_ENGINE_* */
-    int reserved;
+    int tile;      /* fused engine tile shape: 0 default, 1..4 = 16x32, 32x32, 32x64, 64x32 cells */
     double wind_param[4];
 } csadv_options;
 
@@ -124,6 +124,29 @@ int csadv_get_step(const csadv_plan *plan, int *k);
 /* divergence(cs_grid, simulation) (discrete_operators.py:18-101) of one tracer at the
  * current state, written as an interior (N, N, 6) array; the state is not advanced. */
 int csadv_divergence(csadv_plan *plan, int tracer, double *host_div, void *stream);
+
+/* ---------------------------------------------------------------- execution control and statistics */
+/* Steps run as CUDA graphs by default: one graph per step kind and buffer parity is
+ * captured on first use and replayed on the caller's stream.  enable = 0 launches the
+ * kernels directly. */
+int csadv_set_graphs(csadv_plan *plan, int enable);
+/* Record CUDA events around every launch of the plan's main step kernel (the fused
+ * kernel; the whole step for the staged engine) and accumulate their durations in
+ * csadv_stats.main_ms.  Profiled steps launch directly (no graph) and synchronise. */
+int csadv_set_profiling(csadv_plan *plan, int enable);
+typedef struct csadv_stats {
+    long long steps;            /* steps advanced */
+    long long kernel_launches;  /* kernels launched by steps (graph kernel nodes count once per replay) */
+    long long main_launches;    /* timed launches of the main kernel */
+    double main_ms;             /* their total device time */
+    int kernels_per_step;       /* kernel launches of one step (from the captured graph; 0 if none yet) */
+    int engine;                 /* CSADV_ENGINE_STAGED or CSADV_ENGINE_FUSED */
+    int tile;                   /* fused tile shape in use (1..4), 0 for staged */
+    int reserved;
+    size_t device_bytes;        /* device memory held by the plan */
+} csadv_stats;
+int csadv_get_stats(csadv_plan *plan, csadv_stats *out);
+int csadv_reset_stats(csadv_plan *plan);
 
 /* ---------------------------------------------------------------- pinned host memory */
 int csadv_host_alloc(void **ptr, size_t bytes);

@@ -41,7 +41,15 @@ class Options(ctypes.Structure):
     _fields_ = [
         ("recon", ctypes.c_int), ("dp", ctypes.c_int), ("opsplit", ctypes.c_int), ("et", ctypes.c_int),
         ("mt", ctypes.c_int), ("mf", ctypes.c_int), ("vf", ctypes.c_int), ("precision", ctypes.c_int),
-        ("engine", ctypes.c_int), ("reserved", ctypes.c_int), ("wind_param", ctypes.c_double * 4),
+        ("engine", ctypes.c_int), ("tile", ctypes.c_int), ("wind_param", ctypes.c_double * 4),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("steps", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong), ("main_launches", ctypes.c_longlong),
+        ("main_ms", ctypes.c_double), ("kernels_per_step", ctypes.c_int), ("engine", ctypes.c_int),
+        ("tile", ctypes.c_int), ("reserved", ctypes.c_int), ("device_bytes", ctypes.c_size_t),
     ]
 
 
@@ -66,6 +74,10 @@ _SIGS = {
     "csadv_get_cfl": ([_vp, _dp], _c_int),
     "csadv_get_step": ([_vp, ctypes.POINTER(_c_int)], _c_int),
     "csadv_divergence": ([_vp, _c_int, _vp, _vp], _c_int),
+    "csadv_set_graphs": ([_vp, _c_int], _c_int),
+    "csadv_set_profiling": ([_vp, _c_int], _c_int),
+    "csadv_get_stats": ([_vp, ctypes.POINTER(Stats)], _c_int),
+    "csadv_reset_stats": ([_vp], _c_int),
     "csadv_host_alloc": ([ctypes.POINTER(_vp), ctypes.c_size_t], _c_int),
     "csadv_host_free": ([_vp], _c_int),
 }

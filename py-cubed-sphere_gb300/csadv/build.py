@@ -33,6 +33,9 @@ UNITS = {
     "wind.cu": False,
     "staged.cu": False,
     "io.cu": False,
+    "fused_host.cu": False,
+    "fused_f32.cu": True,
+    "fused_f64.cu": False,
 }
 
 

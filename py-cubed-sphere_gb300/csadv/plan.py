@@ -16,13 +16,13 @@ class Plan:
     """
 
     def __init__(self, N, dt, recon=3, dp=1, opsplit=1, et=3, mt=1, mf=3, vf=1, ntracers=1, precision=64,
-                 engine=L.ENGINE_AUTO, wind_param=(0.0, 0.0, 0.0, 0.0), stream=None):
+                 engine=L.ENGINE_AUTO, wind_param=(0.0, 0.0, 0.0, 0.0), stream=None, tile=0):
         self.N, self.dt, self.ntracers, self.precision = int(N), float(dt), int(ntracers), int(precision)
         self.options = dict(recon=recon, dp=dp, opsplit=opsplit, et=et, mt=mt, mf=mf, vf=vf)
         self.stream = L.stream_handle(stream)
         o = L.Options()
         o.recon, o.dp, o.opsplit, o.et, o.mt, o.mf, o.vf = recon, dp, opsplit, et, mt, mf, vf
-        o.precision, o.engine = precision, engine
+        o.precision, o.engine, o.tile = precision, engine, tile
         for c in range(4):
             o.wind_param[c] = float(wind_param[c]) if c < len(wind_param) else 0.0
         self._opts = o
@@ -118,6 +118,21 @@ class Plan:
         if rc not in (L.OK, L.ERR_BLOWUP) or (rc == L.ERR_BLOWUP and raise_blowup):
             L.check(rc, "csadv_errors")
         return out[0], out[1], out[2]
+
+    # ------------------------------------------------------------------ execution control
+    def set_graphs(self, enable):
+        L.check(L.lib().csadv_set_graphs(self._h, int(bool(enable))), "csadv_set_graphs")
+
+    def set_profiling(self, enable):
+        L.check(L.lib().csadv_set_profiling(self._h, int(bool(enable))), "csadv_set_profiling")
+
+    def stats(self):
+        st = L.Stats()
+        L.check(L.lib().csadv_get_stats(self._h, ctypes.byref(st)), "csadv_get_stats")
+        return {name: getattr(st, name) for name, _ in L.Stats._fields_ if name != "reserved"}
+
+    def reset_stats(self):
+        L.check(L.lib().csadv_reset_stats(self._h), "csadv_reset_stats")
 
     def divergence(self, tracer=0):
         out = np.empty((self.N, self.N, 6), dtype=np.float64)

@@ -2,6 +2,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "../../include/csadv.h"
 #include "cases.cuh"
@@ -28,6 +29,7 @@ int validate_options(const csadv_options *o, Options &out) {
         return CSADV_ERR_OPTION;
     if (o->precision != 64 && o->precision != 32) return CSADV_ERR_OPTION;
     if (o->engine < CSADV_ENGINE_AUTO || o->engine > CSADV_ENGINE_FUSED) return CSADV_ERR_OPTION;
+    if (o->tile < 0 || o->tile > 4) return CSADV_ERR_OPTION;
     // discrete_operators.py:49-73: SP-AVLT / SP-L04 need MT-0, SP-PL07 needs MT-PL07
     if ((o->opsplit == SP_PL07) != (o->mt == MT_PL07)) return CSADV_ERR_OPTION_PAIR;
     out.recon = o->recon;
@@ -39,6 +41,7 @@ int validate_options(const csadv_options *o, Options &out) {
     out.vf = o->vf;
     out.precision = o->precision;
     out.engine = o->engine;
+    out.tile = o->tile;
     for (int c = 0; c < 4; ++c) out.wp[c] = o->wind_param[c];
     return CSADV_OK;
 }
@@ -66,8 +69,34 @@ struct csadv_plan {
     int k = 0;
     double cfl = 0.0;
     int device = 0;
+    FusedState f;  // fused engine (f.on) : Q double-buffered in f.Qbuf[cur]
+    int cur = 0;
+    // execution: CUDA graphs of one step, keyed by [kind: 0 time step, 1 time step + wind update][parity]
+    bool graphs = true;
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int gkernels[2][2] = {{0, 0}, {0, 0}};
+    // profiling of the main kernel
+    bool prof = false;
+    cudaEvent_t pev[2] = {nullptr, nullptr};
+    csadv_stats stats{};
+    void drop_graphs() {
+        for (auto &row : gexec)
+            for (auto &e : row)
+                if (e) {
+                    cudaGraphExecDestroy(e);
+                    e = nullptr;
+                }
+    }
+    ~csadv_plan() {
+        drop_graphs();
+        if (cap) cudaStreamDestroy(cap);
+        for (auto &e : pev)
+            if (e) cudaEventDestroy(e);
+    }
     size_t esize() const { return opt.precision == 64 ? sizeof(double) : sizeof(float); }
-    void *tracer(int t) const { return (char *)Q + (size_t)t * grid.d.field * esize(); }
+    void *state() const { return f.on ? f.Qbuf[cur] : Q; }
+    void *tracer(int t) const { return (char *)state() + (size_t)t * grid.d.field * esize(); }
 };
 
 namespace {
@@ -107,12 +136,96 @@ int time_step(csadv_plan *pl, cudaStream_t st, bool update, int only_tracer) {
 }
 
 int do_time_step(csadv_plan *pl, cudaStream_t st) {
-    return pl->opt.precision == 64 ? time_step<double>(pl, st, true, -1) : time_step<float>(pl, st, true, -1);
+    if (!pl->f.on) {
+        if (pl->prof) CSADV_CUDA(cudaEventRecord(pl->pev[0], st));
+        int rc = pl->opt.precision == 64 ? time_step<double>(pl, st, true, -1) : time_step<float>(pl, st, true, -1);
+        if (!rc && pl->prof) CSADV_CUDA(cudaEventRecord(pl->pev[1], st));
+        return rc;
+    }
+    if (wind_time_dependent(pl->opt)) {
+        int rc = wind_halo(pl->opt, pl->grid, pl->w, st);
+        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
+        if (rc) return rc;
+    }
+    return fused_step(pl->opt, pl->grid, pl->dt, pl->T, pl->f, pl->cur, st, pl->prof ? pl->pev[0] : nullptr,
+                      pl->prof ? pl->pev[1] : nullptr);
 }
 
-int do_update_winds(csadv_plan *pl, double t, cudaStream_t st) {
-    if (!wind_time_dependent(pl->opt)) return CSADV_OK;
-    return wind_interior(pl->opt, pl->grid, pl->w, t, true, st);
+// the stored state equals the true state (no pending MF-PR correction)
+int settle(csadv_plan *pl, cudaStream_t st) {
+    if (!pl->f.on) return CSADV_OK;
+    return fused_materialize(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
+}
+
+// tick: the device clock advances one step (csadv_advance); else it is set to (k, t)
+int do_update_winds(csadv_plan *pl, bool tick, long long k, double t, cudaStream_t st) {
+    return wind_update(pl->opt, pl->grid, pl->w, tick, k, t, st);
+}
+
+// the work of one step: adv_time_step, and for kind 1 also update_adv(k * dt) via the clock
+int step_work(csadv_plan *pl, int kind, cudaStream_t st) {
+    int rc = do_time_step(pl, st);
+    if (!rc && kind == 1) rc = do_update_winds(pl, true, 0, 0.0, st);
+    return rc;
+}
+
+int count_kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return 0;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+    int k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+// one step (kind 0: time step; kind 1: time step + wind update), replayed from a graph
+int run_step(csadv_plan *pl, int kind, cudaStream_t st) {
+    const int par = pl->cur;
+    const bool use_graph = pl->graphs && !pl->prof;  // profiled steps launch directly (events on the stream)
+    if (use_graph && !pl->gexec[kind][par]) {
+        if (!pl->cap) CSADV_CUDA(cudaStreamCreateWithFlags(&pl->cap, cudaStreamNonBlocking));
+        CSADV_CUDA(cudaStreamBeginCapture(pl->cap, cudaStreamCaptureModeThreadLocal));
+        int rc = step_work(pl, kind, pl->cap);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(pl->cap, &g);
+        pl->cur = par;  // the captured work has not run yet
+        if (rc || e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            pl->graphs = false;  // fall back to direct launches
+        } else {
+            pl->gkernels[kind][par] = count_kernel_nodes(g);
+            e = cudaGraphInstantiate(&pl->gexec[kind][par], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                pl->gexec[kind][par] = nullptr;
+                pl->graphs = false;
+            }
+        }
+    }
+    if (use_graph && pl->graphs && pl->gexec[kind][par]) {
+        CSADV_CUDA(cudaGraphLaunch(pl->gexec[kind][par], st));
+        if (pl->f.on) pl->cur = 1 - par;
+        pl->stats.kernel_launches += pl->gkernels[kind][par];
+        pl->stats.kernels_per_step = pl->gkernels[kind][par];
+    } else {
+        int rc = step_work(pl, kind, st);
+        if (rc) return rc;
+    }
+    pl->stats.steps += 1;
+    if (pl->prof) {
+        CSADV_CUDA(cudaEventSynchronize(pl->pev[1]));
+        float ms = 0.f;
+        CSADV_CUDA(cudaEventElapsedTime(&ms, pl->pev[0], pl->pev[1]));
+        pl->stats.main_ms += ms;
+        pl->stats.main_launches += 1;
+    }
+    return CSADV_OK;
 }
 
 int select_device(csadv_plan *pl) {
@@ -168,7 +281,8 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     int rc = validate_options(opt, o);
     if (rc) return rc;
     if (N < 8 || N > 16384 || ntracers < 1 || ntracers > 64 || !(dt > 0.0)) return CSADV_ERR_ARG;
-    if (o.engine == CSADV_ENGINE_FUSED) return CSADV_ERR_UNSUPPORTED;
+    if (o.engine == CSADV_ENGINE_FUSED && !fused_supported(o)) return CSADV_ERR_UNSUPPORTED;
+    const bool fused = o.engine == CSADV_ENGINE_FUSED || (o.engine == CSADV_ENGINE_AUTO && fused_supported(o));
     csadv_plan *pl = new (std::nothrow) csadv_plan();
     if (!pl) return CSADV_ERR_OOM;
     pl->opt = o;
@@ -191,7 +305,9 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     const long long F = d.field;
     double **wa[] = {&pl->w.u_pu, &pl->w.v_pv, &pl->w.u_old, &pl->w.v_old, &pl->w.u_avg, &pl->w.v_avg,
                      &pl->w.ulon_pc, &pl->w.vlat_pc};
-    for (double **p : wa) *p = pl->mem.alloc<double>(F);
+    for (int c = 0; c < 6; ++c) *wa[c] = pl->mem.alloc<double>(F);
+    pl->w.ulon_pc = pl->mem.alloc<double>(2 * F);  // ulon_pc and vlat_pc in one allocation
+    pl->w.vlat_pc = pl->w.ulon_pc ? pl->w.ulon_pc + F : nullptr;
     const size_t es = pl->esize();
     pl->Q = pl->mem.alloc<char>((long long)ntracers * F * es);
     void **sa[] = {&pl->s.Qx, &pl->s.Qy, &pl->s.qLx, &pl->s.qRx, &pl->s.qLy, &pl->s.qRy, &pl->s.fx, &pl->s.fy, &pl->s.div};
@@ -205,6 +321,16 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
         delete pl;
         return CSADV_ERR_OOM;
     }
+    if (fused) {
+        pl->f.Qbuf[0] = pl->Q;
+        pl->f.tile = o.tile > 0 ? o.tile - 1 : 1;
+        rc = fused_prepare(o, pl->f.tile);
+        if (!rc) rc = fused_alloc(o, pl->grid, ntracers, pl->mem, pl->f, st);
+        if (rc) {
+            delete pl;
+            return rc;
+        }
+    }
     bool ok = true;
     for (double **p : wa) ok = ok && cudaMemsetAsync(*p, 0, F * sizeof(double), st) == cudaSuccess;
     ok = ok && cudaMemsetAsync(pl->Q, 0, (size_t)ntracers * F * es, st) == cudaSuccess;
@@ -215,7 +341,8 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     }
     // init_vars_adv (advection_vars.py:19-107): t = 0 winds, wind halo, old <- current,
     // departure-point winds, CFL
-    rc = wind_interior(o, pl->grid, pl->w, 0.0, false, st);
+    rc = wind_setup(o, pl->grid, pl->w, pl->mem, dt, st);
+    if (!rc) rc = wind_initial(o, pl->grid, pl->w, st);
     if (!rc) rc = wind_halo(o, pl->grid, pl->w, st);
     if (!rc && cudaMemcpyAsync(pl->w.u_old, pl->w.u_pu, F * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         rc = CSADV_ERR_CUDA;
@@ -223,6 +350,7 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
         rc = CSADV_ERR_CUDA;
     if (!rc) rc = wind_average(o, pl->grid, pl->w, dt, st);
     if (!rc) rc = wind_cfl(pl->grid, pl->w, dt, pl->tmp, pl->cfl, st);
+    if (!rc && fused) rc = fused_prep_winds(o, pl->grid, pl->w, dt, pl->f, st);
     if (rc) {
         delete pl;
         return rc;
@@ -254,6 +382,8 @@ int csadv_set_tracer(csadv_plan *pl, int tracer, const double *host, int layout,
     const Dims d = pl->grid.d;
     const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
     cudaStream_t st = S(stream);
+    int rc = settle(pl, st);
+    if (rc) return rc;
     CSADV_CUDA(cudaMemcpyAsync(pl->stage, host, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyHostToDevice, st));
     if (pl->opt.precision == 64) return tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, true, st);
     return tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, true, st);
@@ -265,7 +395,15 @@ int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void 
     const Dims d = pl->grid.d;
     const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
     cudaStream_t st = S(stream);
-    int rc = pl->opt.precision == 64
+    int rc = settle(pl, st);
+    if (rc) return rc;
+    // the full array carries the ghost cells filled at the start of the last step, as the
+    // reference's Q does; the fused engine keeps them in its other buffer
+    if (layout == CSADV_LAYOUT_FULL && pl->f.on && pl->k > 0) {
+        rc = fused_ghosts_to_current(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
+        if (rc) return rc;
+    }
+    rc = pl->opt.precision == 64
                  ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, false, st)
                  : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, false, st);
     if (rc) return rc;
@@ -276,7 +414,7 @@ int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void 
 
 int csadv_time_step(csadv_plan *pl, int k, void *stream) {
     if (!pl) return CSADV_ERR_ARG;
-    int rc = do_time_step(pl, S(stream));
+    int rc = run_step(pl, 0, S(stream));
     if (rc) return rc;
     pl->k = k;
     return CSADV_OK;
@@ -284,25 +422,24 @@ int csadv_time_step(csadv_plan *pl, int k, void *stream) {
 
 int csadv_update_winds(csadv_plan *pl, double t, void *stream) {
     if (!pl) return CSADV_ERR_ARG;
-    return do_update_winds(pl, t, S(stream));
+    return do_update_winds(pl, false, pl->k, t, S(stream));
 }
 
 int csadv_advance(csadv_plan *pl, int nsteps, void *stream) {
     if (!pl || nsteps < 0) return CSADV_ERR_ARG;
     cudaStream_t st = S(stream);
     for (int s = 0; s < nsteps; ++s) {
-        int k = pl->k + 1;
-        int rc = do_time_step(pl, st);
+        int rc = run_step(pl, 1, st);
         if (rc) return rc;
-        rc = do_update_winds(pl, k * pl->dt, st);
-        if (rc) return rc;
-        pl->k = k;
+        pl->k += 1;
     }
     return CSADV_OK;
 }
 
 int csadv_mass(csadv_plan *pl, int tracer, double *mass, void *stream) {
     if (!pl || !mass || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    int rc = settle(pl, S(stream));
+    if (rc) return rc;
     if (pl->opt.precision == 64) return diag_mass<double>(pl->grid, (const double *)pl->tracer(tracer), pl->tmp, *mass, S(stream));
     return diag_mass<float>(pl->grid, (const float *)pl->tracer(tracer), pl->tmp, *mass, S(stream));
 }
@@ -312,7 +449,9 @@ int csadv_errors(csadv_plan *pl, int tracer, int ic, const double *ic_param, dou
     if (!((ic >= 1 && ic <= 4) || (ic >= CSADV_IC_HILL && ic <= CSADV_IC_SMOOTH_BELLS))) return CSADV_ERR_OPTION;
     if (ic == CSADV_IC_HILL && !ic_param) return CSADV_ERR_ARG;
     IcParams p = ic_params(pl, ic_param);
-    int rc = pl->opt.precision == 64
+    int rc = settle(pl, S(stream));
+    if (rc) return rc;
+    rc = pl->opt.precision == 64
                  ? diag_errors<double>(pl->grid, (const double *)pl->tracer(tracer), ic, pl->opt.vf, p, t, pl->tmp, out, S(stream))
                  : diag_errors<float>(pl->grid, (const float *)pl->tracer(tracer), ic, pl->opt.vf, p, t, pl->tmp, out, S(stream));
     if (rc) return rc;
@@ -336,7 +475,9 @@ int csadv_get_step(const csadv_plan *pl, int *k) {
 int csadv_divergence(csadv_plan *pl, int tracer, double *host_div, void *stream) {
     if (!pl || !host_div || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
     cudaStream_t st = S(stream);
-    int rc = pl->opt.precision == 64 ? time_step<double>(pl, st, false, tracer) : time_step<float>(pl, st, false, tracer);
+    int rc = settle(pl, st);
+    if (rc) return rc;
+    rc = pl->opt.precision == 64 ? time_step<double>(pl, st, false, tracer) : time_step<float>(pl, st, false, tracer);
     if (rc) return rc;
     rc = pl->opt.precision == 64 ? tracer_io<double>(pl->grid, (double *)pl->s.div, pl->stage, CSADV_LAYOUT_INTERIOR, false, st)
                                  : tracer_io<float>(pl->grid, (float *)pl->s.div, pl->stage, CSADV_LAYOUT_INTERIOR, false, st);
@@ -344,6 +485,38 @@ int csadv_divergence(csadv_plan *pl, int tracer, double *host_div, void *stream)
     const Dims d = pl->grid.d;
     CSADV_CUDA(cudaMemcpyAsync(host_div, pl->stage, (size_t)NFACE * d.N * d.N * sizeof(double), cudaMemcpyDeviceToHost, st));
     CSADV_CUDA(cudaStreamSynchronize(st));
+    return CSADV_OK;
+}
+
+int csadv_set_graphs(csadv_plan *pl, int enable) {
+    if (!pl) return CSADV_ERR_ARG;
+    pl->drop_graphs();
+    pl->graphs = enable != 0;
+    return CSADV_OK;
+}
+
+int csadv_set_profiling(csadv_plan *pl, int enable) {
+    if (!pl) return CSADV_ERR_ARG;
+    if (enable && !pl->pev[0]) {
+        CSADV_CUDA(cudaEventCreate(&pl->pev[0]));
+        CSADV_CUDA(cudaEventCreate(&pl->pev[1]));
+    }
+    pl->prof = enable != 0;
+    return CSADV_OK;
+}
+
+int csadv_get_stats(csadv_plan *pl, csadv_stats *out) {
+    if (!pl || !out) return CSADV_ERR_ARG;
+    *out = pl->stats;
+    out->engine = pl->f.on ? CSADV_ENGINE_FUSED : CSADV_ENGINE_STAGED;
+    out->tile = pl->f.on ? pl->f.tile + 1 : 0;
+    out->device_bytes = pl->mem.bytes();
+    return CSADV_OK;
+}
+
+int csadv_reset_stats(csadv_plan *pl) {
+    if (!pl) return CSADV_ERR_ARG;
+    pl->stats = csadv_stats{};
     return CSADV_OK;
 }
 

@@ -113,7 +113,10 @@ struct Winds {
     double *u_pu, *v_pv;          // contravariant wind at x-edges / y-edges
     double *u_old, *v_old;        // previous step (RK2)
     double *u_avg, *v_avg;        // departure-point (time-averaged) winds
-    double *ulon_pc, *vlat_pc;    // lat-lon wind at centres (ET-DG wind halo)
+    double *ulon_pc, *vlat_pc;    // lat-lon wind at centres (ET-DG wind halo), contiguous fields
+    double *tab[2] = {nullptr, nullptr};  // time-independent wind coefficients (x-, y-edges)
+    int tkind = 0;                // 0: static wind, 1: deformational (6 coefs), 2: separable (1 coef)
+    void *clock = nullptr;        // device clock (step count, time of the current wind)
 };
 
 __host__ __device__ __forceinline__ int ceil_div(long long a, int b) { return (int)((a + b - 1) / b); }

@@ -1,0 +1,155 @@
+// Host side of the fused engine: buffers, wind preparation, step sequencing, and the
+// lazy MF-PR correction.
+#include "fused.cuh"
+#include "internal.h"
+
+namespace csadv {
+
+int fused_supported(const Options &o) { return o.et == ET_DG && o.mf != MF_AF; }
+
+__global__ void k_plane_to_float(const double *__restrict__ src, float *dst, long long n) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (float)src[t];
+}
+
+// Q* + g corr on interior cells of every tracer (the true state); blockIdx.y = tracer
+template <class real>
+__global__ void k_materialize(real *Q0, Dims d, const real *__restrict__ g, const double *__restrict__ corr) {
+    const int N = d.N;
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)NFACE * N * N) return;
+    int j = d.i0 + (int)(t % N), i = d.i0 + (int)((t / N) % N), p = (int)(t / ((long long)N * N));
+    real *Q = Q0 + blockIdx.y * d.field;
+    long long o = at(d, p, i, j);
+    Q[o] = Q[o] + g[at2(d, i, j)] * (real)corr[blockIdx.y];
+}
+
+// copy every non-interior cell of the n x n cell planes from `src` to `dst` (all tracers)
+template <class real>
+__global__ void k_copy_ghosts(const real *__restrict__ src, real *dst, Dims d) {
+    const int n = d.n;
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)NFACE * n * n) return;
+    int j = (int)(t % n), i = (int)((t / n) % n), p = (int)(t / ((long long)n * n));
+    if (i >= d.i0 && i < d.iend && j >= d.i0 && j < d.iend) return;
+    long long o = at(d, p, i, j) + blockIdx.y * d.field;
+    dst[o] = src[o];
+}
+
+int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
+    const Dims d = g.d;
+    dim3 grid(ceil_div((long long)NFACE * d.n * d.n, 256), T);
+    if (o.precision == 64)
+        k_copy_ghosts<double><<<grid, 256, 0, st>>>((const double *)f.Qbuf[1 - cur], (double *)f.Qbuf[cur], d);
+    else
+        k_copy_ghosts<float><<<grid, 256, 0, st>>>((const float *)f.Qbuf[1 - cur], (float *)f.Qbuf[cur], d);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedState &f, cudaStream_t st) {
+    const Dims d = g.d;
+    const size_t es = o.precision == 64 ? sizeof(double) : sizeof(float);
+    f.on = true;
+    f.Qbuf[1] = mem.alloc<char>((long long)T * d.field * es);
+    for (int b = 0; b < 2; ++b) f.corr[b] = mem.alloc<double>(T);
+    int maxb = 0;
+    for (int c = 0; c < FUSED_NTILE_CFG; ++c) maxb = maxb > fused_blocks(d, c) ? maxb : fused_blocks(d, c);
+    f.partials = mem.alloc<double>((long long)T * maxb);
+    f.counter = mem.alloc<unsigned int>(1);
+    f.ua = mem.alloc<char>(d.field * es);
+    f.va = mem.alloc<char>(d.field * es);
+    f.wpitch = d.pitch / 32;
+    long long words = (long long)NFACE * (d.n + 1) * f.wpitch;
+    f.upos = mem.alloc<uint32_t>(words);
+    f.vpos = mem.alloc<uint32_t>(words);
+    if (o.precision == 64) {
+        f.g_pc = g.g_pc;
+        f.g_pu = g.g_pu;
+        f.g_pv = g.g_pv;
+    } else {
+        float *gs[3];
+        for (int c = 0; c < 3; ++c) gs[c] = mem.alloc<float>(d.plane);
+        if (!mem.ok()) return CSADV_ERR_OOM;
+        const double *src[3] = {g.g_pc, g.g_pu, g.g_pv};
+        for (int c = 0; c < 3; ++c) k_plane_to_float<<<ceil_div(d.plane, 256), 256, 0, st>>>(src[c], gs[c], d.plane);
+        f.g_pc = gs[0];
+        f.g_pu = gs[1];
+        f.g_pv = gs[2];
+    }
+    if (!mem.ok()) return CSADV_ERR_OOM;
+    CSADV_CUDA(cudaMemsetAsync(f.Qbuf[1], 0, (size_t)T * d.field * es, st));
+    for (int b = 0; b < 2; ++b) CSADV_CUDA(cudaMemsetAsync(f.corr[b], 0, T * sizeof(double), st));
+    CSADV_CUDA(cudaMemsetAsync(f.counter, 0, sizeof(unsigned int), st));
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, cudaStream_t st) {
+    if (o.precision == 64)
+        return wind_avgprep<double>(o, g, w, dt, (double *)f.ua, (double *)f.va, f.upos, f.vpos, f.wpitch, st);
+    return wind_avgprep<float>(o, g, w, dt, (float *)f.ua, (float *)f.va, f.upos, f.vpos, f.wpitch, st);
+}
+
+int fused_prepare(const Options &o, int tile) {
+    FusedArgs a{};
+    return o.precision == 64 ? fused_launch<double>(a, o.recon, tile, (cudaStream_t)-1)
+                             : fused_launch<float>(a, o.recon, tile, (cudaStream_t)-1);
+}
+
+int fused_step(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
+               cudaEvent_t ev0, cudaEvent_t ev1) {
+    const bool pr = o.mf == MF_PR;
+    int rc;
+    if (o.precision == 64)
+        rc = launch_halo_dg_tracers<double>((double *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
+                                            (const double *)f.g_pc, st);
+    else
+        rc = launch_halo_dg_tracers<float>((float *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
+                                           (const float *)f.g_pc, st);
+    if (rc) return rc;
+    FusedArgs a{};
+    a.d = g.d;
+    a.T = T;
+    a.dt = dt;
+    a.dx = g.dx;
+    a.a2 = g.a2;
+    a.Qin = f.Qbuf[cur];
+    a.Qout = f.Qbuf[1 - cur];
+    a.corr_in = pr ? f.corr[cur] : nullptr;
+    a.corr_out = pr ? f.corr[1 - cur] : nullptr;
+    a.partials = f.partials;
+    a.counter = f.counter;
+    a.ua = f.ua;
+    a.va = f.va;
+    a.upos = f.upos;
+    a.vpos = f.vpos;
+    a.g_pc = f.g_pc;
+    a.g_pu = f.g_pu;
+    a.g_pv = f.g_pv;
+    a.split = o.opsplit;
+    a.mt = o.mt;
+    a.mfpr = pr ? 1 : 0;
+    a.wpitch = f.wpitch;
+    if (ev0) CSADV_CUDA(cudaEventRecord(ev0, st));
+    rc = o.precision == 64 ? fused_launch<double>(a, o.recon, f.tile, st) : fused_launch<float>(a, o.recon, f.tile, st);
+    if (rc) return rc;
+    if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
+    cur = 1 - cur;
+    return CSADV_OK;
+}
+
+int fused_materialize(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
+    if (o.mf != MF_PR) return CSADV_OK;
+    const Dims d = g.d;
+    dim3 grid(ceil_div((long long)NFACE * d.N * d.N, 256), T);
+    if (o.precision == 64)
+        k_materialize<double><<<grid, 256, 0, st>>>((double *)f.Qbuf[cur], d, (const double *)f.g_pc, f.corr[cur]);
+    else
+        k_materialize<float><<<grid, 256, 0, st>>>((float *)f.Qbuf[cur], d, (const float *)f.g_pc, f.corr[cur]);
+    CSADV_CUDA(cudaGetLastError());
+    CSADV_CUDA(cudaMemsetAsync(f.corr[cur], 0, T * sizeof(double), st));
+    return CSADV_OK;
+}
+
+}  // namespace csadv

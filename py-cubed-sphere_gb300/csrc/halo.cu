@@ -20,10 +20,26 @@
 
 namespace csadv {
 
+// Source values of the ghost-cell interpolation.  With a pending MF-PR correction
+// (fused engine) the stored interior value is Q* and the true value is Q* + g corr,
+// formed in the state's precision exactly as the fused kernel forms it on load.
+template <class real>
+struct Src {
+    const real *F;
+    const real *g;  // metric plane (real), used only with corr
+    real corr;
+    bool has_corr;
+    __device__ __forceinline__ double interior(const Dims &d, int q, int i, int j) const {
+        real v = F[at(d, q, i, j)];
+        if (has_corr) v = v + g[at2(d, i, j)] * corr;
+        return (double)v;
+    }
+};
+
 // value of the ghost cell at depth `dep` outside side s of panel p, along index k
 // (k inside the edge's interior range); computed in FP64 from interior cells only
 template <class real>
-__device__ double side_ghost(const real *__restrict__ F, const Dims &d, const double *__restrict__ W,
+__device__ double side_ghost(const Src<real> &S, const Dims &d, const double *__restrict__ W,
                              const int *__restrict__ K, int p, int s, int dep, int k) {
     const Conn c = c_conn[p][s];
     const int n = d.n;
@@ -36,27 +52,31 @@ __device__ double side_ghost(const real *__restrict__ F, const Dims &d, const do
         int along = c.rev ? n - 1 - kk : kk;
         int i, j;
         inside_ij(d, c.qs, dep, along, i, j);
-        prod[m] = (double)F[at(d, c.q, i, j)] * w[m];
+        prod[m] = S.interior(d, c.q, i, j) * w[m];
     }
     return ((prod[0] + prod[1]) + prod[2]) + prod[3];
 }
 
 // value of cell (i, j) of panel q where (i, j) is interior or in a side strip (not a corner)
 template <class real>
-__device__ double cell_or_side_ghost(const real *__restrict__ F, const Dims &d, const double *__restrict__ W,
+__device__ double cell_or_side_ghost(const Src<real> &S, const Dims &d, const double *__restrict__ W,
                                      const int *__restrict__ K, int q, int i, int j) {
-    if (i >= d.iend) return (double)(real)side_ghost(F, d, W, K, q, SIDE_E, i - d.iend, j);
-    if (i < d.i0) return (double)(real)side_ghost(F, d, W, K, q, SIDE_W, d.i0 - 1 - i, j);
-    if (j >= d.iend) return (double)(real)side_ghost(F, d, W, K, q, SIDE_N, j - d.iend, i);
-    if (j < d.i0) return (double)(real)side_ghost(F, d, W, K, q, SIDE_S, d.i0 - 1 - j, i);
-    return (double)F[at(d, q, i, j)];
+    if (i >= d.iend) return (double)(real)side_ghost(S, d, W, K, q, SIDE_E, i - d.iend, j);
+    if (i < d.i0) return (double)(real)side_ghost(S, d, W, K, q, SIDE_W, d.i0 - 1 - i, j);
+    if (j >= d.iend) return (double)(real)side_ghost(S, d, W, K, q, SIDE_N, j - d.iend, i);
+    if (j < d.i0) return (double)(real)side_ghost(S, d, W, K, q, SIDE_S, d.i0 - 1 - j, i);
+    return S.interior(d, q, i, j);
 }
 
+// blockIdx.y = tracer (fields `fstride` elements apart); corr[tracer] optional
 template <class real>
-__global__ void k_halo_dg(real *F, Dims d, const double *__restrict__ W, const int *__restrict__ K) {
+__global__ void k_halo_dg(real *F0, long long fstride, Dims d, const double *__restrict__ W,
+                          const int *__restrict__ K, const double *__restrict__ corr, const real *__restrict__ g) {
     const int n = d.n;
     int tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= NFACE * 4 * NG * n) return;
+    real *F = F0 + blockIdx.y * fstride;
+    Src<real> S{F, g, corr ? (real)corr[blockIdx.y] : real(0), corr != nullptr};
     int k = tid % n;
     int dep = (tid / n) % NG;
     int s = (tid / (n * NG)) % 4;
@@ -64,7 +84,7 @@ __global__ void k_halo_dg(real *F, Dims d, const double *__restrict__ W, const i
     int gi, gj;
     ghost_ij(d, s, dep, k, gi, gj);
     if (is_interior(d, k)) {
-        F[at(d, p, gi, gj)] = (real)side_ghost(F, d, W, K, p, s, dep, k);
+        F[at(d, p, gi, gj)] = (real)side_ghost(S, d, W, K, p, s, dep, k);
         return;
     }
     if (s == SIDE_N || s == SIDE_S) return;  // corner blocks are filled from the E/W sides
@@ -78,7 +98,7 @@ __global__ void k_halo_dg(real *F, Dims d, const double *__restrict__ W, const i
         int along = c.rev ? n - 1 - kk : kk;
         int i, j;
         inside_ij(d, c.qs, dep, along, i, j);
-        prod[m] = cell_or_side_ghost(F, d, W, K, c.q, i, j) * w[m];
+        prod[m] = cell_or_side_ghost(S, d, W, K, c.q, i, j) * w[m];
     }
     F[at(d, p, gi, gj)] = (real)(((prod[0] + prod[1]) + prod[2]) + prod[3]);
 }
@@ -105,7 +125,16 @@ __global__ void k_halo_adjacent(real *Qx, real *Qy, Dims d) {
 template <class real>
 int launch_halo_dg(real *F, const Grid &g, cudaStream_t st) {
     int tot = NFACE * 4 * NG * g.d.n;
-    k_halo_dg<real><<<ceil_div(tot, 128), 128, 0, st>>>(F, g.d, g.lag_w, g.lag_k);
+    k_halo_dg<real><<<ceil_div(tot, 128), 128, 0, st>>>(F, 0, g.d, g.lag_w, g.lag_k, nullptr, nullptr);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+template <class real>
+int launch_halo_dg_tracers(real *F, int T, const Grid &g, const double *corr, const real *greal, cudaStream_t st) {
+    int tot = NFACE * 4 * NG * g.d.n;
+    dim3 grid(ceil_div(tot, 128), T);
+    k_halo_dg<real><<<grid, 128, 0, st>>>(F, g.d.field, g.d, g.lag_w, g.lag_k, corr, greal);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -120,6 +149,9 @@ int launch_halo_adjacent(real *Qx, real *Qy, const Grid &g, cudaStream_t st) {
 
 template int launch_halo_dg<double>(double *, const Grid &, cudaStream_t);
 template int launch_halo_dg<float>(float *, const Grid &, cudaStream_t);
+template int launch_halo_dg_tracers<double>(double *, int, const Grid &, const double *, const double *,
+                                            cudaStream_t);
+template int launch_halo_dg_tracers<float>(float *, int, const Grid &, const double *, const float *, cudaStream_t);
 template int launch_halo_adjacent<double>(double *, double *, const Grid &, cudaStream_t);
 template int launch_halo_adjacent<float>(float *, float *, const Grid &, cudaStream_t);
 

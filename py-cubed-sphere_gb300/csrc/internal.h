@@ -52,7 +52,7 @@ class DeviceArena {
 };
 
 struct Options {
-    int recon, dp, opsplit, et, mt, mf, vf, precision, engine;
+    int recon, dp, opsplit, et, mt, mf, vf, precision, engine, tile;
     double wp[4];
 };
 
@@ -84,6 +84,8 @@ struct Scratch {
 template <class real> int launch_halo_dg(real *F, const Grid &g, cudaStream_t st);
 template <class real> int launch_halo_adjacent(real *Qx, real *Qy, const Grid &g, cudaStream_t st);
 template <class real>
+int launch_halo_dg_tracers(real *F, int T, const Grid &g, const double *corr, const real *greal, cudaStream_t st);
+template <class real>
 int staged_divergence(const Options &o, const Grid &g, const Winds &w, double dt, real *Q, const Scratch &s,
                       double *partials, int npart, cudaStream_t st);
 template <class real>
@@ -91,10 +93,44 @@ int staged_update(const Options &o, const Grid &g, double dt, real *Q, const Scr
                   int npart, double *scal, cudaStream_t st);
 int staged_partial_count(const Grid &g);
 
-int wind_interior(const Options &o, const Grid &g, Winds &w, double t, bool keep_old, cudaStream_t st);
+int wind_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, double dt, cudaStream_t st);
+int wind_initial(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
+int wind_update(const Options &o, const Grid &g, Winds &w, bool tick, long long k, double t, cudaStream_t st);
 int wind_halo(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
 int wind_average(const Options &o, const Grid &g, Winds &w, double dt, cudaStream_t st);
+// departure-point winds in the state's precision + upwind bits (fused engine), one pass
+template <class real>
+int wind_avgprep(const Options &o, const Grid &g, const Winds &w, double dt, real *ua, real *va, uint32_t *ub,
+                 uint32_t *vb, int wpitch, cudaStream_t st);
 int wind_cfl(const Grid &g, const Winds &w, double dt, double *dev_tmp, double &cfl, cudaStream_t st);
+
+// ---------------------------------------------------------------- fused engine state
+struct FusedState {
+    bool on = false;
+    int tile = 1;               // FUSED_TILES index
+    void *Qbuf[2] = {nullptr, nullptr};
+    double *corr[2] = {nullptr, nullptr};  // [T] pending MF-PR correction of Qbuf[b]
+    double *partials = nullptr; // [T][max blocks]
+    unsigned int *counter = nullptr;
+    void *ua = nullptr, *va = nullptr;     // departure-point winds in the state's precision
+    uint32_t *upos = nullptr, *vpos = nullptr;  // upwind flags (1 bit per edge)
+    int wpitch = 0;             // 32-bit words per row of the flag arrays
+    const void *g_pc = nullptr, *g_pu = nullptr, *g_pv = nullptr;  // metric in the state's precision
+};
+
+int fused_supported(const Options &o);
+int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedState &f, cudaStream_t st);
+int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, cudaStream_t st);
+// one step: ghost cells of Qbuf[cur] (+ correction), fused kernel into Qbuf[1-cur]; cur flips
+int fused_step(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
+               cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
+// set the dynamic shared-memory limit of the kernel a plan will launch (outside capture)
+int fused_prepare(const Options &o, int tile);
+// ghost cells of Qbuf[cur] <- those of Qbuf[1-cur] (the halo the last step used)
+int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
+// apply and clear the pending MF-PR correction of Qbuf[cur]
+int fused_materialize(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
+template <class real> int fused_launch(const struct FusedArgs &a, int recon, int tile, cudaStream_t st);
 
 int diag_partials(const Grid &g);
 template <class real>

@@ -1,6 +1,6 @@
 // Winds (FP64, shared by every tracer of a plan).
 //
-//  wind_interior -- analytic winds on the interior edges -> contravariant
+//  wind_initial / wind_update -- analytic winds on the interior edges -> contravariant
 //                   (advection_vars.py:38-53 at t = 0; update_adv, advection_timestep.py:48-75)
 //  wind_halo     -- ET-DG: edge->centre cubic band, contravariant->lat-lon, Lagrange ghost
 //                   fill of the centre winds, centre->ghost-edge cubic, lat-lon->contravariant
@@ -22,27 +22,6 @@ struct WindParams {
     int vf;
     double prm[4];
 };
-
-// old <- current over the whole arrays; for ET-S72/ET-PL07 the non-interior entries of the
-// current wind then become 0 (update_adv converts lat-lon winds that are 0 there).  For
-// ET-DG those entries keep their value: update_adv recomputes them from the lat-lon winds
-// the wind halo stored with them, which gives the same numbers.
-__global__ void k_wind_shift(Dims d, double *u, double *v, double *uo, double *vo, int zero_ghosts) {
-    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (tid >= d.field) return;
-    int p = (int)(tid / d.plane);
-    long long r = tid - p * d.plane;
-    int i = (int)(r / d.pitch), j = (int)(r % d.pitch);
-    (void)p;
-    uo[tid] = u[tid];
-    vo[tid] = v[tid];
-    if (zero_ghosts) {
-        bool iu = (i >= d.i0 && i <= d.iend && j >= d.i0 && j < d.iend);
-        bool iv = (i >= d.i0 && i < d.iend && j >= d.i0 && j <= d.iend);
-        if (!iu) u[tid] = 0.0;
-        if (!iv) v[tid] = 0.0;
-    }
-}
 
 // analytic winds at interior edges at time t, converted to contravariant components
 __global__ void k_wind_interior(Grid g, double *u, double *v, WindParams wp, double t) {
@@ -69,6 +48,127 @@ __global__ void k_wind_interior(Grid g, double *u, double *v, WindParams wp, dou
         v[o] = (-g.cv[1][o] * ulon + g.cv[0][o] * vlat) / g.cv[4][o];
     }
 }
+
+// ---------------------------------------------------------------- time-dependent winds
+// The reference re-evaluates the analytic wind on every interior edge each step
+// (update_adv, advection_timestep.py:55-58), about ten FP64 transcendental calls per
+// edge.  Here the parts that do not depend on t are evaluated once per plan, together
+// with the lat-lon -> contravariant factors, so a step costs ~15 FP64 operations per
+// edge:
+//   vf 2 / deformational:  u_lat-lon = k cos(pi t/T) sin^2(lon - 2 pi t/T) sin(2 lat) + 2 pi cos(lat) / T
+//                          v_lat-lon = k cos(pi t/T) sin(2 (lon - 2 pi t/T)) cos(lat)
+//                          with sin / cos of (lon - w t) from the angle-difference identities
+//   vf 3:                  separable, u = cos(pi t/T) * w0(edge)
+//   vf 4:                  constant in time, u = w0(edge)
+// Results agree with the reference's direct evaluation to a few ulp.
+struct WindTables {
+    int kind;             // 1: deformational (6 coefficients per edge), 2: separable / constant (1)
+    const double *c[6];   // per-edge coefficient planes (x-edges and y-edges interleaved: [set][coef])
+};
+
+// per-edge coefficients (time-independent parts) of the wind at the x-edges (set 0)
+// and y-edges (set 1): deformational -> {sin lon, cos lon, sin 2lat, cos lat, a, b} with
+// contravariant = a * u_ll + b * v_ll; separable/constant -> {contravariant at t = 0}
+__global__ void k_wind_tables(Grid g, WindParams wp, double *tab0, double *tab1, int ncoef) {
+    const Dims d = g.d;
+    const int N = d.N;
+    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long per = (long long)(N + 1) * N;
+    if (tid >= 2 * NFACE * per) return;
+    int which = (int)(tid / (NFACE * per));
+    long long r = tid % (NFACE * per);
+    int p = (int)(r / per);
+    int a = (int)((r % per) / N), b = (int)(r % N);
+    int i = which == 0 ? d.i0 + a : d.i0 + b;
+    int j = which == 0 ? d.i0 + b : d.i0 + a;
+    long long o = at(d, p, i, j);
+    const double *lon = which == 0 ? g.lon_pu : g.lon_pv, *lat = which == 0 ? g.lat_pu : g.lat_pv;
+    const double *const *cf = which == 0 ? g.cu : g.cv;
+    double *tab = which == 0 ? tab0 : tab1;
+    // contravariant = a * ulon + b * vlat  (sphgeo.py:120-125)
+    double ca = which == 0 ? cf[3][o] / cf[4][o] : -cf[1][o] / cf[4][o];
+    double cb = which == 0 ? -cf[2][o] / cf[4][o] : cf[0][o] / cf[4][o];
+    if (ncoef == 6) {
+        double L = lon[o], P = lat[o];
+        tab[0 * d.field + o] = sin(L);
+        tab[1 * d.field + o] = cos(L);
+        tab[2 * d.field + o] = sin(2.0 * P);
+        tab[3 * d.field + o] = cos(P);
+        tab[4 * d.field + o] = ca;
+        tab[5 * d.field + o] = cb;
+    } else {
+        double ulon, vlat;
+        wind_latlon(wp.vf, wp.prm, lon[o], lat[o], 0.0, ulon, vlat);  // vf 3 at t = 0 (cos 0 = 1); vf 4
+        tab[o] = ca * ulon + cb * vlat;
+    }
+}
+
+struct Clock {
+    long long k;  // completed steps
+    double dt;
+    double t;     // time of the wind held in the "current" arrays
+};
+
+__global__ void k_clock_tick(Clock *c) {
+    c->k += 1;
+    c->t = (double)c->k * c->dt;
+}
+__global__ void k_clock_set(Clock *c, long long k, double t) {
+    c->k = k;
+    c->t = t;
+}
+
+// update_adv: old <- current everywhere; current <- wind(t) on interior edges; non-interior
+// entries become 0 for ET-S72/ET-PL07 and keep the wind-halo values for ET-DG (the
+// reference recomputes them from unchanged lat-lon values)
+__global__ void k_wind_update(Dims d, double *u, double *v, double *uo, double *vo, const double *__restrict__ tu,
+                              const double *__restrict__ tv, int kind, WindParams wp, const Clock *clk,
+                              int zero_ghosts) {
+    __shared__ double sc[4];
+    if (threadIdx.x == 0) {
+        const double t = clk->t;
+        if (kind == 1) {
+            const double Tp = wp.vf == 2 ? 5.0 : wp.prm[1], k = wp.vf == 2 ? 2.0 : wp.prm[0];
+            double w = 2 * PI * t / Tp;
+            sc[0] = k * cos(PI * t / Tp);
+            sc[1] = sin(w);
+            sc[2] = cos(w);
+            sc[3] = 2.0 * PI / Tp;
+        } else {
+            sc[0] = wp.vf == 3 ? cos(PI * t / 5.0) : 1.0;
+        }
+    }
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y, p = blockIdx.z;
+    if (j >= d.pitch) return;
+    const long long tid = at(d, p, i, j);
+    uo[tid] = u[tid];
+    vo[tid] = v[tid];
+    const bool iu = (i >= d.i0 && i <= d.iend && j >= d.i0 && j < d.iend);
+    const bool iv = (i >= d.i0 && i < d.iend && j >= d.i0 && j <= d.iend);
+    for (int which = 0; which < 2; ++which) {
+        const bool in = which == 0 ? iu : iv;
+        double *out = which == 0 ? u : v;
+        const double *tab = which == 0 ? tu : tv;
+        if (in) {
+            if (kind == 1) {
+                double sl = tab[tid], cl = tab[d.field + tid], s2p = tab[2 * d.field + tid], cp = tab[3 * d.field + tid];
+                double ca = tab[4 * d.field + tid], cb = tab[5 * d.field + tid];
+                double s = sl * sc[2] - cl * sc[1];  // sin(lon - w t)
+                double c = cl * sc[2] + sl * sc[1];  // cos(lon - w t)
+                double ulon = sc[0] * (s * s) * s2p + sc[3] * cp;
+                double vlat = sc[0] * (2.0 * s * c) * cp;
+                out[tid] = ca * ulon + cb * vlat;
+            } else {
+                out[tid] = sc[0] * tab[tid];
+            }
+        } else if (zero_ghosts) {
+            out[tid] = 0.0;
+        }
+    }
+}
+
+static dim3 plane_grid(const Dims &d, int bx) { return dim3(ceil_div(d.pitch, bx), d.n + 1, NFACE); }
 
 // ET-DG wind halo, part 1: cubic edge->centre interpolation of the contravariant wind in
 // the band of 4 cells along each panel boundary, then contravariant->lat-lon there
@@ -199,36 +299,64 @@ __global__ void k_wind_adjacent(Dims d, double *U, double *V) {
 }
 
 // departure-point winds (averaged_velocity.py:14-62)
+// RK2 average at edge (i, j) along direction dir (0: x, 1: y): the wind extrapolated to
+// n+1/2, interpolated linearly at the departure point on the upwind side
+__device__ __forceinline__ double rk2_average(const double *__restrict__ U, const double *__restrict__ Uo,
+                                              const Dims &d, int p, int i, int j, int dir, double dto2, double dx) {
+    auto ui = [&](int k) {
+        long long o = dir == 0 ? at(d, p, k, j) : at(d, p, i, k);
+        return 1.5 * U[o] - 0.5 * Uo[o];
+    };
+    const int e = dir == 0 ? i : j;
+    const double u = U[at(d, p, i, j)];
+    const double a = u * dto2 / dx;
+    return (u >= 0) ? (1.0 - a) * ui(e) + a * ui(e - 1) : -a * ui(e + 1) + (1.0 + a) * ui(e);
+}
+
 __global__ void k_wind_average(Dims d, const double *__restrict__ U, const double *__restrict__ Uo, double *Ua,
                                const double *__restrict__ V, const double *__restrict__ Vo, double *Va, int rk2,
                                double dto2, double dx) {
-    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (tid >= d.field) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y, p = blockIdx.z;
+    if (j >= d.pitch) return;
+    const long long tid = at(d, p, i, j);
     if (!rk2) {
         Ua[tid] = U[tid];
         Va[tid] = V[tid];
         return;
     }
-    int p = (int)(tid / d.plane);
-    long long r = tid - p * d.plane;
-    int i = (int)(r / d.pitch), j = (int)(r % d.pitch);
-    if (j < d.n && i >= d.i0 && i <= d.iend) {  // x-edges [i0, iend] x all columns
-        double u = U[tid];
-        double a = u * dto2 / dx;
-        auto ui = [&](int ii) {
-            long long o = at(d, p, ii, j);
-            return 1.5 * U[o] - 0.5 * Uo[o];
-        };
-        Ua[tid] = (u >= 0) ? (1.0 - a) * ui(i) + a * ui(i - 1) : -a * ui(i + 1) + (1.0 + a) * ui(i);
+    if (j < d.n && i >= d.i0 && i <= d.iend) Ua[tid] = rk2_average(U, Uo, d, p, i, j, 0, dto2, dx);
+    if (i < d.n && j >= d.i0 && j <= d.iend) Va[tid] = rk2_average(V, Vo, d, p, i, j, 1, dto2, dx);
+}
+
+// departure-point wind and upwind flag of the fused engine in one pass: the wind in the
+// state's precision, and one bit per edge (warp ballot over 32 consecutive columns)
+template <class real>
+__global__ void k_wind_avgprep(Dims d, const double *__restrict__ U, const double *__restrict__ Uo,
+                               const double *__restrict__ V, const double *__restrict__ Vo, real *ua, real *va,
+                               uint32_t *ubits, uint32_t *vbits, int wpitch, int rk2, double dto2, double dx) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y, p = blockIdx.z;
+    const bool ok = j < d.pitch;
+    double u = 0.0, v = 0.0, au = 0.0, av = 0.0;
+    long long tid = 0;
+    if (ok) {
+        tid = at(d, p, i, j);
+        u = U[tid];
+        v = V[tid];
+        au = u;
+        av = v;
+        if (rk2) {
+            au = (j < d.n && i >= d.i0 && i <= d.iend) ? rk2_average(U, Uo, d, p, i, j, 0, dto2, dx) : 0.0;
+            av = (i < d.n && j >= d.i0 && j <= d.iend) ? rk2_average(V, Vo, d, p, i, j, 1, dto2, dx) : 0.0;
+        }
+        ua[tid] = (real)au;
+        va[tid] = (real)av;
     }
-    if (i < d.n && j >= d.i0 && j <= d.iend) {  // y-edges all rows x [j0, jend]
-        double v = V[tid];
-        double a = v * dto2 / dx;
-        auto vi = [&](int jj) {
-            long long o = at(d, p, i, jj);
-            return 1.5 * V[o] - 0.5 * Vo[o];
-        };
-        Va[tid] = (v >= 0) ? (1.0 - a) * vi(j) + a * vi(j - 1) : -a * vi(j + 1) + (1.0 + a) * vi(j);
+    unsigned bu = __ballot_sync(0xffffffffu, ok && u >= 0.0);
+    unsigned bv = __ballot_sync(0xffffffffu, ok && v >= 0.0);
+    if (ok && (threadIdx.x & 31) == 0) {
+        long long w = ((long long)p * (d.n + 1) + i) * wpitch + (j >> 5);
+        ubits[w] = bu;
+        vbits[w] = bv;
     }
 }
 
@@ -267,13 +395,58 @@ static WindParams wparams(const Options &o) {
     return wp;
 }
 
-int wind_interior(const Options &o, const Grid &g, Winds &w, double t, bool shift, cudaStream_t st) {
+// Allocate and fill the time-independent wind coefficients and the device clock.
+int wind_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, double dt, cudaStream_t st) {
     const Dims d = g.d;
-    if (shift) {
-        k_wind_shift<<<ceil_div(d.field, 256), 256, 0, st>>>(d, w.u_pu, w.v_pv, w.u_old, w.v_old, o.et != ET_DG);
+    Clock *clk = mem.alloc<Clock>(1);
+    if (!mem.ok()) return CSADV_ERR_OOM;
+    w.clock = clk;
+    k_clock_set<<<1, 1, 0, st>>>(clk, 0, 0.0);
+    Clock h{0, dt, 0.0};
+    CSADV_CUDA(cudaMemcpyAsync(clk, &h, sizeof(Clock), cudaMemcpyHostToDevice, st));
+    if (!wind_time_dependent(o)) {
+        w.tkind = 0;
+        return CSADV_OK;
+    }
+    const bool deform = (o.vf == 2 || o.vf == CSADV_WIND_DEFORM);
+    const int nc = deform ? 6 : 1;
+    w.tkind = deform ? 1 : 2;
+    for (int s2 = 0; s2 < 2; ++s2) {
+        w.tab[s2] = mem.alloc<double>(nc * d.field);
+        if (!mem.ok()) return CSADV_ERR_OOM;
+        CSADV_CUDA(cudaMemsetAsync(w.tab[s2], 0, nc * d.field * sizeof(double), st));
     }
     long long tot = 2LL * NFACE * (d.N + 1) * d.N;
-    k_wind_interior<<<ceil_div(tot, 128), 128, 0, st>>>(g, w.u_pu, w.v_pv, wparams(o), t);
+    k_wind_tables<<<ceil_div(tot, 128), 128, 0, st>>>(g, wparams(o), w.tab[0], w.tab[1], nc);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+// Winds of the interior edges at the initial time (advection_vars.py:38-53).
+int wind_initial(const Options &o, const Grid &g, Winds &w, cudaStream_t st) {
+    const Dims d = g.d;
+    if (w.tkind == 0) {
+        long long tot = 2LL * NFACE * (d.N + 1) * d.N;
+        k_wind_interior<<<ceil_div(tot, 128), 128, 0, st>>>(g, w.u_pu, w.v_pv, wparams(o), 0.0);
+    } else {
+        k_wind_update<<<plane_grid(d, 128), 128, 0, st>>>(d, w.u_pu, w.v_pv, w.u_old, w.v_old, w.tab[0], w.tab[1],
+                                                         w.tkind, wparams(o), (const Clock *)w.clock, 0);
+    }
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+// update_adv (advection_timestep.py:48-75).  tick: the clock advances by one step (time
+// k*dt computed on the device, so the sequence can be replayed from a CUDA graph);
+// otherwise the clock is set to (k, t).
+int wind_update(const Options &o, const Grid &g, Winds &w, bool tick, long long k, double t, cudaStream_t st) {
+    const Dims d = g.d;
+    Clock *clk = (Clock *)w.clock;
+    if (tick) k_clock_tick<<<1, 1, 0, st>>>(clk);
+    else k_clock_set<<<1, 1, 0, st>>>(clk, k, t);
+    if (w.tkind != 0)
+        k_wind_update<<<plane_grid(d, 128), 128, 0, st>>>(d, w.u_pu, w.v_pv, w.u_old, w.v_old, w.tab[0], w.tab[1],
+                                                         w.tkind, wparams(o), clk, o.et != ET_DG);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -283,9 +456,7 @@ int wind_halo(const Options &o, const Grid &g, Winds &w, cudaStream_t st) {
     if (o.et == ET_DG) {
         long long tot = (long long)NFACE * d.N * d.N;
         k_wind_band<<<ceil_div(tot, 128), 128, 0, st>>>(g, w.u_pu, w.v_pv, w.ulon_pc, w.vlat_pc);
-        int rc = launch_halo_dg<double>(w.ulon_pc, g, st);
-        if (rc) return rc;
-        rc = launch_halo_dg<double>(w.vlat_pc, g, st);
+        int rc = launch_halo_dg_tracers<double>(w.ulon_pc, 2, g, nullptr, nullptr, st);  // ulon_pc, vlat_pc
         if (rc) return rc;
         long long per = (long long)(d.N + 1) * 2 * NG + 2LL * d.n;
         tot = 2 * NFACE * per;
@@ -300,11 +471,25 @@ int wind_halo(const Options &o, const Grid &g, Winds &w, cudaStream_t st) {
 
 int wind_average(const Options &o, const Grid &g, Winds &w, double dt, cudaStream_t st) {
     const Dims d = g.d;
-    k_wind_average<<<ceil_div(d.field, 256), 256, 0, st>>>(d, w.u_pu, w.u_old, w.u_avg, w.v_pv, w.v_old, w.v_avg,
-                                                          o.dp == 2, dt * 0.5, g.dx);
+    k_wind_average<<<plane_grid(d, 128), 128, 0, st>>>(d, w.u_pu, w.u_old, w.u_avg, w.v_pv, w.v_old, w.v_avg,
+                                                       o.dp == 2, dt * 0.5, g.dx);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
+
+template <class real>
+int wind_avgprep(const Options &o, const Grid &g, const Winds &w, double dt, real *ua, real *va, uint32_t *ub,
+                 uint32_t *vb, int wpitch, cudaStream_t st) {
+    const Dims d = g.d;
+    k_wind_avgprep<real><<<plane_grid(d, 128), 128, 0, st>>>(d, w.u_pu, w.u_old, w.v_pv, w.v_old, ua, va, ub, vb,
+                                                              wpitch, o.dp == 2, dt * 0.5, g.dx);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+template int wind_avgprep<double>(const Options &, const Grid &, const Winds &, double, double *, double *, uint32_t *,
+                                  uint32_t *, int, cudaStream_t);
+template int wind_avgprep<float>(const Options &, const Grid &, const Winds &, double, float *, float *, uint32_t *,
+                                 uint32_t *, int, cudaStream_t);
 
 int wind_cfl(const Grid &g, const Winds &w, double dt, double *dev_tmp, double &cfl, cudaStream_t st) {
     k_wind_cfl<<<1, 512, 0, st>>>(g.d, w.u_pu, w.v_pv, dt, g.dx, dev_tmp);

@@ -1,0 +1,141 @@
+"""GPU tests of the fused engine (one tile kernel per step) against the reference goldens,
+the staged engine and the CPU oracle, plus the FP32 form's accuracy and mass budget.
+
+Tolerances: FP64 fused vs reference / oracle / staged: 1e-12 relative to the field
+maximum (the FP64 parity bar).  FP32 vs FP64: 2e-5 relative after tens of steps, and
+mass conserved to 1e-6 relative with MF-PR (the FP32 form's stated bars).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import solver
+from oracle.grid import CubedSphere
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+FUSED = 2
+STAGED = 1
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__
+    __graft_entry__.build()
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def plan(N, dt, c, vf, **kw):
+    from csadv import Plan
+    recon, dp, sp, et, mt, mf = c
+    return Plan(N, dt, recon=recon, dp=dp, opsplit=sp, et=et, mt=mt, mf=mf, vf=vf, **kw)
+
+
+def test_fused_rejects_schemes_it_does_not_cover():
+    from csadv import CsadvError
+    for c in ((3, 1, 1, 1, 1, 3), (3, 1, 1, 2, 1, 3), (3, 1, 1, 3, 1, 2)):
+        with pytest.raises(CsadvError):
+            plan(16, 0.01, c, 1, engine=FUSED)
+
+
+@pytest.mark.parametrize("vf", [2, 1])
+def test_fused_fp64_vs_reference_golden(golden_dir, vf):
+    z = np.load(os.path.join(golden_dir, "combos_N10.npz"))
+    n = 0
+    for c, Qref in zip(z["combos_vf%d" % vf], z["Q_vf%d" % vf]):
+        c = tuple(int(x) for x in c)
+        if c[3] != 3 or c[5] == 2:
+            continue
+        with plan(10, float(z["dt"]), c, vf, engine=FUSED) as pl:
+            pl.init_tracer(int(z["ic"]))
+            pl.advance(int(z["nsteps"]))
+            assert rel(pl.get_tracer(), Qref) <= RTOL, c
+        n += 1
+    assert n > 0
+
+
+@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("N", [40, 50, 64])
+def test_fused_fp64_partial_tiles_vs_oracle(N, tile):
+    c, vf, ic, dt, nsteps = (2, 2, 1, 3, 1, 3), 2, 3, 0.004, 6
+    g = CubedSphere(N)
+    sim = solver.Simulation(g, dt, 5.0, ic, vf, *c)
+    solver.run_steps(sim, nsteps)
+    with plan(N, dt, c, vf, engine=FUSED, tile=tile) as pl:
+        pl.init_tracer(ic)
+        pl.advance(nsteps)
+        assert rel(pl.get_tracer(), sim.Q[g.interior]) <= RTOL
+
+
+@pytest.mark.parametrize("c", [(1, 1, 1, 3, 1, 1), (2, 2, 1, 3, 1, 3), (3, 2, 2, 3, 1, 3), (4, 1, 3, 3, 2, 3),
+                               (4, 2, 3, 3, 2, 1), (3, 1, 1, 3, 1, 3)])
+def test_fused_equals_staged_long_run_fp64(c):
+    N, dt, nsteps = 96, 0.002, 60
+    outs = []
+    for eng in (STAGED, FUSED):
+        with plan(N, dt, c, 2, engine=eng) as pl:
+            pl.init_tracer(3)
+            pl.advance(nsteps)
+            outs.append((pl.get_tracer(), pl.mass()))
+    assert rel(outs[1][0], outs[0][0]) <= RTOL
+    assert abs(outs[1][1] - outs[0][1]) <= 1e-12 * abs(outs[0][1])
+
+
+def test_fused_tracers_equal_single_runs():
+    c, vf, dt = (2, 2, 1, 3, 1, 3), 2, 0.004
+    with plan(48, dt, c, vf, ntracers=3, engine=FUSED) as pl:
+        for t, ic in enumerate((2, 3, 4)):
+            pl.init_tracer(ic, tracer=t)
+        pl.advance(5)
+        multi = [pl.get_tracer(t) for t in range(3)]
+    for t, ic in enumerate((2, 3, 4)):
+        with plan(48, dt, c, vf, engine=FUSED) as pl:
+            pl.init_tracer(ic)
+            pl.advance(5)
+            np.testing.assert_array_equal(pl.get_tracer(), multi[t])
+
+
+def test_fused_set_get_between_steps_keeps_state():
+    # reading/writing the state in the middle of a run applies the pending mass-fixer correction
+    c, vf, dt = (2, 2, 1, 3, 1, 3), 2, 0.004
+    with plan(48, dt, c, vf, engine=FUSED) as a, plan(48, dt, c, vf, engine=FUSED) as b:
+        a.init_tracer(3)
+        b.init_tracer(3)
+        a.advance(4)
+        b.advance(2)
+        q = b.get_tracer(full=True)
+        b.set_tracer(q)
+        b.advance(2)
+        assert rel(b.get_tracer(), a.get_tracer()) <= RTOL
+
+
+@pytest.mark.parametrize("c", [(2, 2, 1, 3, 1, 3), (3, 1, 1, 3, 1, 3)])
+def test_fp32_form_accuracy_and_mass(c):
+    N, dt, nsteps, ic, vf = 96, 0.002, 80, 3, 2
+    res = {}
+    for prec in (64, 32):
+        with plan(N, dt, c, vf, precision=prec, engine=FUSED) as pl:
+            pl.init_tracer(ic)
+            m0 = pl.mass()
+            pl.advance(nsteps)
+            res[prec] = (pl.get_tracer(), abs(pl.mass() - m0) / abs(m0), pl.errors(ic, nsteps * dt))
+    assert rel(res[32][0], res[64][0]) < 2e-5
+    assert res[32][1] < 1e-6
+    # L2 error against the analytic solution within 1% of the FP64 run's
+    assert abs(res[32][2][2] - res[64][2][2]) <= 0.01 * res[64][2][2]
+
+
+def test_fp32_staged_and_fused_agree():
+    c, N, dt = (2, 2, 1, 3, 1, 3), 64, 0.003
+    outs = []
+    for eng in (STAGED, FUSED):
+        with plan(N, dt, c, 2, precision=32, engine=eng) as pl:
+            pl.init_tracer(2)
+            pl.advance(20)
+            outs.append(pl.get_tracer())
+    assert rel(outs[1], outs[0]) < 1e-5
