@@ -72,7 +72,8 @@ typedef struct csadv_options {
     int vf;        /* wind code (see above) */
     int precision; /* 64: state in float64 ("plain form"); 32: state/PPM/fluxes in float32 */
     int engine;    /* CSADV_ENGINE_* */
-    int tile;      /* fused engine tile shape: 0 default, 1..4 = 16x32, 32x32, 32x64, 64x32 cells */
+    int tile;      /* fused engine tile (rows x columns of cells): 1 = 16x58, 2 = 32x58, 3 = 16x26,
+                      4 = 32x26; 0 = default (4 for FP32, 3 for FP64) */
     double wind_param[4];
 } csadv_options;
 

@@ -35,7 +35,7 @@ UNITS = {
     "io.cu": False,
     "fused_host.cu": False,
     "fused_f32.cu": True,
-    "fused_f64.cu": False,
+    "fused_f64.cu": True,
 }
 
 

@@ -76,6 +76,9 @@ struct csadv_plan {
     cudaStream_t cap = nullptr;
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int gkernels[2][2] = {{0, 0}, {0, 0}};
+    // second stream and fork/join events of the fused step
+    cudaStream_t side = nullptr;
+    cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
     // profiling of the main kernel
     bool prof = false;
     cudaEvent_t pev[2] = {nullptr, nullptr};
@@ -91,6 +94,9 @@ struct csadv_plan {
     ~csadv_plan() {
         drop_graphs();
         if (cap) cudaStreamDestroy(cap);
+        if (side) cudaStreamDestroy(side);
+        for (auto &e : sev)
+            if (e) cudaEventDestroy(e);
         for (auto &e : pev)
             if (e) cudaEventDestroy(e);
     }
@@ -135,6 +141,50 @@ int time_step(csadv_plan *pl, cudaStream_t st, bool update, int only_tracer) {
     return CSADV_OK;
 }
 
+int do_update_winds(csadv_plan *pl, bool tick, long long k, double t, cudaStream_t st);
+
+int ensure_side(csadv_plan *pl) {
+    if (!pl->side) {
+        CSADV_CUDA(cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking));
+        for (auto &e : pl->sev) CSADV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    return CSADV_OK;
+}
+
+// One step of the fused engine on two streams:
+//   side: tracer ghost cells ............................ | wind update (kind 1)
+//   main: wind halo + departure-point winds | fused kernel
+// The fused kernel waits for both; the wind update for the next step overlaps it.
+int fused_step_work(csadv_plan *pl, int kind, cudaStream_t st) {
+    int rc = ensure_side(pl);
+    if (rc) return rc;
+    cudaStream_t sd = pl->side;
+    CSADV_CUDA(cudaEventRecord(pl->sev[0], st));
+    CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[0], 0));
+    rc = fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, pl->cur, sd);
+    if (rc) return rc;
+    const bool td = wind_time_dependent(pl->opt);
+    if (td) {
+        rc = wind_halo(pl->opt, pl->grid, pl->w, st);
+        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
+        if (rc) return rc;
+    }
+    CSADV_CUDA(cudaEventRecord(pl->sev[1], sd));
+    CSADV_CUDA(cudaStreamWaitEvent(st, pl->sev[1], 0));
+    if (kind == 1) {
+        CSADV_CUDA(cudaEventRecord(pl->sev[2], st));
+        CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[2], 0));
+        rc = do_update_winds(pl, true, 0, 0.0, sd);
+        if (rc) return rc;
+    }
+    rc = fused_kernel(pl->opt, pl->grid, pl->dt, pl->T, pl->f, pl->cur, st, pl->prof ? pl->pev[0] : nullptr,
+                      pl->prof ? pl->pev[1] : nullptr);
+    if (rc) return rc;
+    CSADV_CUDA(cudaEventRecord(pl->sev[3], sd));
+    CSADV_CUDA(cudaStreamWaitEvent(st, pl->sev[3], 0));
+    return CSADV_OK;
+}
+
 int do_time_step(csadv_plan *pl, cudaStream_t st) {
     if (!pl->f.on) {
         if (pl->prof) CSADV_CUDA(cudaEventRecord(pl->pev[0], st));
@@ -142,13 +192,7 @@ int do_time_step(csadv_plan *pl, cudaStream_t st) {
         if (!rc && pl->prof) CSADV_CUDA(cudaEventRecord(pl->pev[1], st));
         return rc;
     }
-    if (wind_time_dependent(pl->opt)) {
-        int rc = wind_halo(pl->opt, pl->grid, pl->w, st);
-        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
-        if (rc) return rc;
-    }
-    return fused_step(pl->opt, pl->grid, pl->dt, pl->T, pl->f, pl->cur, st, pl->prof ? pl->pev[0] : nullptr,
-                      pl->prof ? pl->pev[1] : nullptr);
+    return fused_step_work(pl, 0, st);
 }
 
 // the stored state equals the true state (no pending MF-PR correction)
@@ -164,6 +208,7 @@ int do_update_winds(csadv_plan *pl, bool tick, long long k, double t, cudaStream
 
 // the work of one step: adv_time_step, and for kind 1 also update_adv(k * dt) via the clock
 int step_work(csadv_plan *pl, int kind, cudaStream_t st) {
+    if (pl->f.on) return fused_step_work(pl, kind, st);
     int rc = do_time_step(pl, st);
     if (!rc && kind == 1) rc = do_update_winds(pl, true, 0, 0.0, st);
     return rc;
@@ -235,6 +280,16 @@ int select_device(csadv_plan *pl) {
     return CSADV_OK;
 }
 
+int zero(void *p, size_t bytes, cudaStream_t st) {
+    CSADV_CUDA(cudaMemsetAsync(p, 0, bytes, st));
+    return CSADV_OK;
+}
+
+int copy_d2d(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+    CSADV_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st));
+    return CSADV_OK;
+}
+
 IcParams ic_params(const csadv_plan *pl, const double *ic_param) {
     IcParams p{};
     if (ic_param)
@@ -303,11 +358,6 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     }
     const Dims d = pl->grid.d;
     const long long F = d.field;
-    double **wa[] = {&pl->w.u_pu, &pl->w.v_pv, &pl->w.u_old, &pl->w.v_old, &pl->w.u_avg, &pl->w.v_avg,
-                     &pl->w.ulon_pc, &pl->w.vlat_pc};
-    for (int c = 0; c < 6; ++c) *wa[c] = pl->mem.alloc<double>(F);
-    pl->w.ulon_pc = pl->mem.alloc<double>(2 * F);  // ulon_pc and vlat_pc in one allocation
-    pl->w.vlat_pc = pl->w.ulon_pc ? pl->w.ulon_pc + F : nullptr;
     const size_t es = pl->esize();
     pl->Q = pl->mem.alloc<char>((long long)ntracers * F * es);
     void **sa[] = {&pl->s.Qx, &pl->s.Qy, &pl->s.qLx, &pl->s.qRx, &pl->s.qLy, &pl->s.qRy, &pl->s.fx, &pl->s.fy, &pl->s.div};
@@ -323,7 +373,7 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     }
     if (fused) {
         pl->f.Qbuf[0] = pl->Q;
-        pl->f.tile = o.tile > 0 ? o.tile - 1 : 1;
+        pl->f.tile = o.tile > 0 ? o.tile - 1 : (o.precision == 64 ? 2 : 3);
         rc = fused_prepare(o, pl->f.tile);
         if (!rc) rc = fused_alloc(o, pl->grid, ntracers, pl->mem, pl->f, st);
         if (rc) {
@@ -331,25 +381,22 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
             return rc;
         }
     }
-    bool ok = true;
-    for (double **p : wa) ok = ok && cudaMemsetAsync(*p, 0, F * sizeof(double), st) == cudaSuccess;
-    ok = ok && cudaMemsetAsync(pl->Q, 0, (size_t)ntracers * F * es, st) == cudaSuccess;
-    for (void **p : sa) ok = ok && cudaMemsetAsync(*p, 0, F * es, st) == cudaSuccess;
-    if (!ok) {
+    rc = zero(pl->Q, (size_t)ntracers * F * es, st);
+    for (void **p : sa)
+        if (!rc) rc = zero(*p, F * es, st);
+    if (rc) {
         delete pl;
-        return CSADV_ERR_CUDA;
+        return rc;
     }
     // init_vars_adv (advection_vars.py:19-107): t = 0 winds, wind halo, old <- current,
     // departure-point winds, CFL
     rc = wind_setup(o, pl->grid, pl->w, pl->mem, dt, st);
     if (!rc) rc = wind_initial(o, pl->grid, pl->w, st);
     if (!rc) rc = wind_halo(o, pl->grid, pl->w, st);
-    if (!rc && cudaMemcpyAsync(pl->w.u_old, pl->w.u_pu, F * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
-        rc = CSADV_ERR_CUDA;
-    if (!rc && cudaMemcpyAsync(pl->w.v_old, pl->w.v_pv, F * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
-        rc = CSADV_ERR_CUDA;
+    if (!rc) rc = copy_d2d(pl->w.u_old, pl->w.u_pu, (size_t)F * pl->w.esize, st);
+    if (!rc) rc = copy_d2d(pl->w.v_old, pl->w.v_pv, (size_t)F * pl->w.esize, st);
     if (!rc) rc = wind_average(o, pl->grid, pl->w, dt, st);
-    if (!rc) rc = wind_cfl(pl->grid, pl->w, dt, pl->tmp, pl->cfl, st);
+    if (!rc) rc = wind_cfl(o, pl->grid, pl->w, dt, pl->tmp, pl->cfl, st);
     if (!rc && fused) rc = fused_prep_winds(o, pl->grid, pl->w, dt, pl->f, st);
     if (rc) {
         delete pl;

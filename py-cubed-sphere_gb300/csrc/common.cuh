@@ -108,13 +108,14 @@ struct Grid {
     double a2;  // sum over the interior of g_pc^2, all panels (MF-PR denominator)
 };
 
-// Wind state (FP64), shared by every tracer of a plan.
+// Wind state, shared by every tracer of a plan, in the state's precision (see wind.cu).
 struct Winds {
-    double *u_pu, *v_pv;          // contravariant wind at x-edges / y-edges
-    double *u_old, *v_old;        // previous step (RK2)
-    double *u_avg, *v_avg;        // departure-point (time-averaged) winds
-    double *ulon_pc, *vlat_pc;    // lat-lon wind at centres (ET-DG wind halo), contiguous fields
-    double *tab[2] = {nullptr, nullptr};  // time-independent wind coefficients (x-, y-edges)
+    int esize = 8;                // bytes per element (8: float64, 4: float32)
+    void *u_pu = nullptr, *v_pv = nullptr;      // contravariant wind at x-edges / y-edges
+    void *u_old = nullptr, *v_old = nullptr;    // previous step (RK2)
+    void *u_avg = nullptr, *v_avg = nullptr;    // departure-point (time-averaged) winds
+    void *ulon_pc = nullptr, *vlat_pc = nullptr;  // lat-lon wind at centres (ET-DG halo), contiguous
+    void *tab[2] = {nullptr, nullptr};  // time-independent wind coefficients (x-, y-edges)
     int tkind = 0;                // 0: static wind, 1: deformational (6 coefs), 2: separable (1 coef)
     void *clock = nullptr;        // device clock (step count, time of the current wind)
 };

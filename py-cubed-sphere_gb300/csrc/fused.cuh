@@ -61,14 +61,25 @@ __device__ __forceinline__ real fsign(real x) {
     return x > real(0) ? real(1) : (x < real(0) ? real(-1) : (x == real(0) ? real(0) : x));
 }
 
+// Division by a constant.  The fused engine multiplies by the rounded reciprocal (one
+// rounding more than the reference's division, far inside both forms' error budgets; an
+// IEEE division costs ~10 FP32 or ~15 FP64 instructions, and GB300's FP64 rate is 1/64 of
+// FP32).  The staged engine keeps the reference's divisions.
+template <class real>
+struct Div {
+    static constexpr bool exact = false;
+    __device__ static __forceinline__ real by(real x, real d, real inv_d) { return exact ? x / d : x * inv_d; }
+};
+
 // q_L, q_R of the cell at position 2 of the 5-point window q[0..4] (reconstruction_1d.py:26-192)
 template <class real, int REC>
-__device__ __forceinline__ void recon5(const real q[5], real &L, real &R) {
+__device__ __forceinline__ void recon5f(const real q[5], real &L, real &R) {
     using O = RealOps<real>;
+    using D = Div<real>;
     if (REC == REC_PPM0) {
         const real a = real(7.0 / 12.0);
-        R = a * (q[3] + q[2]) - (q[4] + q[1]) / real(12.0);
-        L = a * (q[2] + q[1]) - (q[3] + q[0]) / real(12.0);
+        R = a * (q[3] + q[2]) - D::by(q[4] + q[1], real(12.0), real(1.0 / 12.0));
+        L = a * (q[2] + q[1]) - D::by(q[3] + q[0], real(12.0), real(1.0 / 12.0));
     } else if (REC == REC_PL07) {
         const real a1 = real(2.0 / 60.0), a2 = real(-13.0 / 60.0), a3 = real(47.0 / 60.0), a4 = real(27.0 / 60.0),
                    a5 = real(-3.0 / 60.0);
@@ -78,41 +89,44 @@ __device__ __forceinline__ void recon5(const real q[5], real &L, real &R) {
         real dQ[3];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-            real qm = q[m], q0 = q[m + 1], qp = q[m + 2];
-            real d0 = real(0.5) * (qp - qm);
-            real d1 = real(2.0) * (qp - q0);
-            real d2 = real(2.0) * (q0 - qm);
-            real s = O::fmn(O::ab(d0), O::ab(d1));
-            s = O::fmn(s, O::ab(d2)) * fsign(d0);
-            if (!((qp - q0) * (q0 - qm) > real(0))) s = real(0);
-            dQ[m] = s;
+            const real qm = q[m], q0 = q[m + 1], qp = q[m + 2];
+            const real d0 = real(0.5) * (qp - qm);
+            const real d1 = real(2.0) * (qp - q0);
+            const real d2 = real(2.0) * (q0 - qm);
+            real s = O::fmn(O::fmn(O::ab(d0), O::ab(d1)), O::ab(d2)) * fsign(d0);
+            dQ[m] = ((qp - q0) * (q0 - qm) > real(0)) ? s : real(0);
         }
-        R = real(0.5) * (q[3] + q[2]) - (dQ[2] - dQ[1]) / real(6.0);
-        L = real(0.5) * (q[2] + q[1]) - (dQ[1] - dQ[0]) / real(6.0);
+        R = real(0.5) * (q[3] + q[2]) - D::by(dQ[2] - dQ[1], real(6.0), real(1.0 / 6.0));
+        L = real(0.5) * (q[2] + q[1]) - D::by(dQ[1] - dQ[0], real(6.0), real(1.0 / 6.0));
         const real qc = q[2];
         const real dq = R - L;
         const real q6 = real(6) * qc - real(3) * (R + L);
-        if ((R - qc) * (qc - L) <= real(0)) {
-            R = qc;
-            L = qc;
-        }
+        const bool flat = (R - qc) * (qc - L) <= real(0);
+        R = flat ? qc : R;
+        L = flat ? qc : L;
         const bool over = O::ab(dq) < O::ab(q6);
         const real DL = R - L;
         const real mid = qc - real(0.5) * (R + L);
-        if (over && DL * mid > (DL * DL) / real(6.0)) L = real(3.0) * qc - real(2.0) * R;
-        else if (over && (-(DL * DL)) / real(6.0) > DL * mid) R = real(3.0) * qc - real(2.0) * L;
+        const real d2 = D::by(DL * DL, real(6.0), real(1.0 / 6.0));
+        const real prod = DL * mid;
+        const bool ml = over && prod > d2;
+        const bool mr = over && !ml && -d2 > prod;
+        const real Ln = real(3.0) * qc - real(2.0) * R;
+        const real Rn = real(3.0) * qc - real(2.0) * L;
+        L = ml ? Ln : L;
+        R = mr ? Rn : R;
     } else {  // REC_L04
         real mono[3];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-            real qm = q[m], q0 = q[m + 1], qp = q[m + 2];
-            real dq = real(0.25) * (qp - qm);
-            real dmin = O::fmx(O::fmx(qm, q0), qp) - q0;
-            real dmax = q0 - O::fmn(O::fmn(qm, q0), qp);
+            const real qm = q[m], q0 = q[m + 1], qp = q[m + 2];
+            const real dq = real(0.25) * (qp - qm);
+            const real dmin = O::fmx(O::fmx(qm, q0), qp) - q0;
+            const real dmax = q0 - O::fmn(O::fmn(qm, q0), qp);
             mono[m] = O::fmn(O::fmn(O::ab(dq), dmin), dmax) * fsign(dq);
         }
-        R = real(0.5) * (q[3] + q[2]) - (mono[2] - mono[1]) / real(3.0);
-        L = real(0.5) * (q[2] + q[1]) - (mono[1] - mono[0]) / real(3.0);
+        R = real(0.5) * (q[3] + q[2]) - D::by(mono[2] - mono[1], real(3.0), real(1.0 / 3.0));
+        L = real(0.5) * (q[2] + q[1]) - D::by(mono[1] - mono[0], real(3.0), real(1.0 / 3.0));
         const real q0 = q[2], m2 = real(2.0) * mono[1];
         L = q0 - O::fmn(real(2.0) * O::ab(mono[1]), O::ab(L - q0)) * fsign(m2);
         R = q0 + O::fmn(real(2.0) * O::ab(mono[1]), O::ab(R - q0)) * fsign(m2);
@@ -120,12 +134,13 @@ __device__ __forceinline__ void recon5(const real q[5], real &L, real &R) {
 }
 
 // upwind PPM flux through an edge (flux.py:20-128).  w = the 5-point window around the
-// upwind cell; gl, gr = metric at the cell's left/right edges, gc at its centre.
+// upwind cell; gl, gr = metric at the cell's left/right edges, gc at its centre; c = Courant
 template <class real, int REC>
 __device__ __forceinline__ real ppm_flux(const real w[5], bool upos, real ua, real c, real gl, real gr, real gc,
                                          real gedge, int mt) {
+    using D = Div<real>;
     real L, R;
-    recon5<real, REC>(w, L, R);
+    recon5f<real, REC>(w, L, R);
     real q = w[2];
     if (mt == MT_0) {
         L = L * gl;
@@ -134,32 +149,36 @@ __device__ __forceinline__ real ppm_flux(const real w[5], bool upos, real ua, re
     }
     const real dq = R - L;
     const real q6 = real(6) * q - real(3) * (R + L);
-    real f;
-    if (upos) f = R + c * real(0.5) * (q6 - dq) - q6 * c * c / real(3.0);
-    else f = L - c * real(0.5) * (q6 + dq) - q6 * c * c / real(3.0);
+    const real e = upos ? R : L;
+    const real hc = c * real(0.5);
+    const real t1 = upos ? hc * (q6 - dq) : -(hc * (q6 + dq));
+    real f = e + t1 - D::by(q6 * c * c, real(3.0), real(1.0 / 3.0));
     f = f * ua;
     if (mt == MT_PL07) f = f * gedge;
     return f;
 }
 
-template <int TI, int TJ>
-struct TileGeom {
-    static constexpr int QI = TI + 6, QJ = TJ + 6;  // Q tile incl. 3 halo cells
-};
-
+// Tile kernel.  blockDim = (32, NW): lanes run along contiguous columns, warps along rows,
+// so shared-memory accesses are conflict-free and no index needs a division.  TJ + 6 is
+// best a multiple of 32 (the tile columns plus the 3-cell halo on each side).
 template <class real, int REC, int TI, int TJ>
 __global__ void __launch_bounds__(256) k_fused(FusedArgs a) {
     constexpr int QI = TI + 6, QJ = TJ + 6;
-    // shared memory (dynamic): winds and metric (per tile), then per-tracer work arrays
+    using D = Div<real>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    real *sUa = (real *)smem_raw;           // [TI+1][QJ]   x-edge u_avg   rows I0.., cols J0-3..
-    real *sVa = sUa + (TI + 1) * QJ;        // [QI][TJ+1]   y-edge v_avg   rows I0-3.., cols J0..
-    real *sG = sVa + QI * (TJ + 1);         // [QI][QJ]     g at centres
-    real *sQ = sG + QI * QJ;                // [QI][QJ]
-    real *sFx = sQ + QI * QJ;               // [TI+1][QJ]
-    real *sFy = sFx + (TI + 1) * QJ;        // [QI][TJ+1]
-    real *sQx = sFy + QI * (TJ + 1);        // [TI][QJ]
-    real *sQy = sQx + TI * QJ;              // [QI][TJ]
+    // per tile (shared by all tracers)
+    real *sUa = (real *)smem_raw;       // [TI+1][QJ]  x-edge wind, rows I0.., cols J0-3..
+    real *sVa = sUa + (TI + 1) * QJ;    // [QI][TJ+1]  y-edge wind, rows I0-3.., cols J0..
+    real *sG = sVa + QI * (TJ + 1);     // [QI][QJ]    g at centres
+    real *sIG = sG + QI * QJ;           // [QI][QJ]    1/g (FP32 form)
+    real *sGu = sIG + QI * QJ;          // [TI+3][QJ]  g at x-edges, rows I0-1..
+    real *sGv = sGu + (TI + 3) * QJ;    // [QI][TJ+3]  g at y-edges, cols J0-1..
+    // per tracer
+    real *sQ = sGv + QI * (TJ + 3);     // [QI][QJ]
+    real *sFx = sQ + QI * QJ;           // [TI+1][QJ]
+    real *sFy = sFx + (TI + 1) * QJ;    // [QI][TJ+1]
+    real *sQx = sFy + QI * (TJ + 1);    // [TI][QJ]
+    real *sQy = sQx + TI * QJ;          // [QI][TJ]
     unsigned char *sUp = (unsigned char *)(sQy + QI * TJ);  // [TI+1][QJ]
     unsigned char *sVp = sUp + (TI + 1) * QJ;                // [QI][TJ+1]
     __shared__ double red[256];
@@ -169,175 +188,197 @@ __global__ void __launch_bounds__(256) k_fused(FusedArgs a) {
     const int p = blockIdx.x / a.ntiles;
     const int I0 = d.i0 + (tile / a.ntj) * TI, J0 = d.i0 + (tile % a.ntj) * TJ;
     const int ni = min(TI, d.iend - I0), nj = min(TJ, d.iend - J0);
-    const real *ua = (const real *)a.ua, *va = (const real *)a.va;
+    const int tx = threadIdx.x, ty = threadIdx.y, NW = blockDim.y;
+    const int tid = ty * 32 + tx, nth = 32 * NW;
+    const size_t pofs = (size_t)p * d.plane;
+    const int P = d.pitch;
+    const real *ua = (const real *)a.ua + pofs, *va = (const real *)a.va + pofs;
     const real *gpc = (const real *)a.g_pc, *gpu = (const real *)a.g_pu, *gpv = (const real *)a.g_pv;
+    const uint32_t *ub = a.upos + (size_t)p * (d.n + 1) * a.wpitch, *vb = a.vpos + (size_t)p * (d.n + 1) * a.wpitch;
+    const real dtdx = (real)(a.dt / a.dx);  // FP32: one rounding; FP64 path keeps u*dt/dx below
     const real rdt = (real)a.dt, rdx = (real)a.dx;
-    const int tid = threadIdx.x, nth = blockDim.x;
 
-    // ---- per-tile data shared by every tracer
-    for (int t = tid; t < (TI + 1) * QJ; t += nth) {
-        int ei = t / QJ, cj = t % QJ;
-        int i = I0 + ei, j = J0 - 3 + cj;
-        if (ei <= ni && cj < nj + 6) {
-            sUa[t] = ua[at(d, p, i, j)];
-            sUp[t] = (a.upos[(p * (long long)(d.n + 1) + i) * a.wpitch + (j >> 5)] >> (j & 31)) & 1u;
+    // ---- per-tile data
+    for (int r = ty; r <= ni; r += NW)
+        for (int c = tx; c < nj + 6; c += 32) {
+            const int i = I0 + r, j = J0 - 3 + c;
+            sUa[r * QJ + c] = ua[i * P + j];
+            sUp[r * QJ + c] = (ub[i * a.wpitch + (j >> 5)] >> (j & 31)) & 1u;
         }
-    }
-    for (int t = tid; t < QI * (TJ + 1); t += nth) {
-        int ri = t / (TJ + 1), ej = t % (TJ + 1);
-        int i = I0 - 3 + ri, j = J0 + ej;
-        if (ri < ni + 6 && ej <= nj) {
-            sVa[t] = va[at(d, p, i, j)];
-            sVp[t] = (a.vpos[(p * (long long)(d.n + 1) + i) * a.wpitch + (j >> 5)] >> (j & 31)) & 1u;
+    for (int r = ty; r < ni + 6; r += NW)
+        for (int c = tx; c <= nj; c += 32) {
+            const int i = I0 - 3 + r, j = J0 + c;
+            sVa[r * (TJ + 1) + c] = va[i * P + j];
+            sVp[r * (TJ + 1) + c] = (vb[i * a.wpitch + (j >> 5)] >> (j & 31)) & 1u;
         }
-    }
-    for (int t = tid; t < QI * QJ; t += nth) {
-        int ri = t / QJ, cj = t % QJ;
-        if (ri < ni + 6 && cj < nj + 6) sG[t] = gpc[at2(d, I0 - 3 + ri, J0 - 3 + cj)];
-    }
+    for (int r = ty; r < ni + 6; r += NW)
+        for (int c = tx; c < nj + 6; c += 32) {
+            const real g = gpc[(I0 - 3 + r) * P + J0 - 3 + c];
+            sG[r * QJ + c] = g;
+            if (!D::exact) sIG[r * QJ + c] = real(1) / g;
+        }
+    for (int r = ty; r < ni + 3; r += NW)
+        for (int c = tx; c < nj + 6; c += 32) sGu[r * QJ + c] = gpu[(I0 - 1 + r) * P + J0 - 3 + c];
+    for (int r = ty; r < ni + 6; r += NW)
+        for (int c = tx; c < nj + 3; c += 32) sGv[r * (TJ + 3) + c] = gpv[(I0 - 3 + r) * P + J0 - 1 + c];
     __syncthreads();
 
     for (int tr = 0; tr < a.T; ++tr) {
-        const real *Qin = (const real *)a.Qin + (size_t)tr * d.field;
-        real *Qout = (real *)a.Qout + (size_t)tr * d.field;
-        const real corr = a.corr_in ? (real)a.corr_in[tr] : real(0);
-        // A: load Q (+ pending correction on interior cells)
-        for (int t = tid; t < QI * QJ; t += nth) {
-            int ri = t / QJ, cj = t % QJ;
-            if (ri < ni + 6 && cj < nj + 6) {
-                int i = I0 - 3 + ri, j = J0 - 3 + cj;
-                real v = Qin[at(d, p, i, j)];
-                if (a.corr_in && i >= d.i0 && i < d.iend && j >= d.i0 && j < d.iend) v = v + sG[t] * corr;
-                sQ[t] = v;
+        const real *Qin = (const real *)a.Qin + (size_t)tr * d.field + pofs;
+        real *Qout = (real *)a.Qout + (size_t)tr * d.field + pofs;
+        const bool hc = a.corr_in != nullptr;
+        const real corr = hc ? (real)a.corr_in[tr] : real(0);
+        // A: Q on the tile + halo (+ pending mass-fixer correction on interior cells)
+        for (int r = ty; r < ni + 6; r += NW) {
+            const int i = I0 - 3 + r;
+            const bool irow = i >= d.i0 && i < d.iend;
+            for (int c = tx; c < nj + 6; c += 32) {
+                const int j = J0 - 3 + c;
+                real v = Qin[i * P + j];
+                if (hc && irow && j >= d.i0 && j < d.iend) v = v + sG[r * QJ + c] * corr;
+                sQ[r * QJ + c] = v;
             }
         }
         __syncthreads();
-        // B: first-pass fluxes
-        for (int t = tid; t < (TI + 1) * QJ; t += nth) {  // x-edges: rows I0+ei, cols J0-3+cj
-            int ei = t / QJ, cj = t % QJ;
-            if (ei > ni || cj >= nj + 6) continue;
-            const bool up = sUp[t];
-            const int c = ei + (up ? 2 : 3);  // upwind cell's row in sQ
-            real w[5];
+        // B: first-pass fluxes.  x-edges: rows I0+e (e <= ni), cols J0-3+c
+        for (int e = ty; e <= ni; e += NW)
+            for (int c = tx; c < nj + 6; c += 32) {
+                const int wi = e * QJ + c;
+                const bool up = sUp[wi];
+                const int cr = e + (up ? 2 : 3);  // upwind cell's row in sQ
+                real w[5];
 #pragma unroll
-            for (int m = 0; m < 5; ++m) w[m] = sQ[(c - 2 + m) * QJ + cj];
-            const int ci = I0 - 3 + c, j = J0 - 3 + cj;
-            const real u = sUa[t];
-            const real cc = u * rdt / rdx;
-            sFx[t] = ppm_flux<real, REC>(w, up, u, cc, gpu[at2(d, ci, j)], gpu[at2(d, ci + 1, j)], sG[c * QJ + cj],
-                                         gpu[at2(d, I0 + ei, j)], a.mt);
-        }
-        for (int t = tid; t < QI * (TJ + 1); t += nth) {  // y-edges: rows I0-3+ri, cols J0+ej
-            int ri = t / (TJ + 1), ej = t % (TJ + 1);
-            if (ri >= ni + 6 || ej > nj) continue;
-            const bool up = sVp[t];
-            const int c = ej + (up ? 2 : 3);  // upwind cell's column in sQ
-            real w[5];
+                for (int m = 0; m < 5; ++m) w[m] = sQ[(cr - 2 + m) * QJ + c];
+                const real u = sUa[wi];
+                const real cc = D::exact ? u * rdt / rdx : u * dtdx;
+                sFx[wi] = ppm_flux<real, REC>(w, up, u, cc, sGu[(cr - 2) * QJ + c], sGu[(cr - 1) * QJ + c],
+                                              sG[cr * QJ + c], sGu[(e + 1) * QJ + c], a.mt);
+            }
+        // y-edges: rows I0-3+r, cols J0+e (e <= nj)
+        for (int r = ty; r < ni + 6; r += NW)
+            for (int e = tx; e <= nj; e += 32) {
+                const int wi = r * (TJ + 1) + e;
+                const bool up = sVp[wi];
+                const int cc0 = e + (up ? 2 : 3);  // upwind cell's column in sQ
+                real w[5];
 #pragma unroll
-            for (int m = 0; m < 5; ++m) w[m] = sQ[ri * QJ + c - 2 + m];
-            const int i = I0 - 3 + ri, cjg = J0 - 3 + c;
-            const real v = sVa[t];
-            const real cc = v * rdt / rdx;
-            sFy[t] = ppm_flux<real, REC>(w, up, v, cc, gpv[at2(d, i, cjg)], gpv[at2(d, i, cjg + 1)], sG[ri * QJ + c],
-                                         gpv[at2(d, i, J0 + ej)], a.mt);
-        }
+                for (int m = 0; m < 5; ++m) w[m] = sQ[r * QJ + cc0 - 2 + m];
+                const real v = sVa[wi];
+                const real cc = D::exact ? v * rdt / rdx : v * dtdx;
+                sFy[wi] = ppm_flux<real, REC>(w, up, v, cc, sGv[r * (TJ + 3) + cc0 - 2],
+                                              sGv[r * (TJ + 3) + cc0 - 1], sG[r * QJ + cc0],
+                                              sGv[r * (TJ + 3) + e + 1], a.mt);
+            }
         __syncthreads();
-        // C: splitting
-        for (int t = tid; t < TI * QJ; t += nth) {  // Qx: rows I0+ri, cols J0-3+cj
-            int ri = t / QJ, cj = t % QJ;
-            if (ri >= ni || cj >= nj + 6) continue;
-            const int sq = (ri + 3) * QJ + cj;
-            const real q = sQ[sq], g = sG[sq];
-            real dF = -(sFx[(ri + 1) * QJ + cj] - sFx[ri * QJ + cj]);
-            dF = dF * rdt / rdx;
-            real out;
-            if (a.split == SP_AVLT) {
-                out = (q * g + real(0.5) * dF) / g;
-            } else {
-                const int j = J0 - 3 + cj;
-                real c1 = gpu[at2(d, I0 + ri + 1, j)] * (sUa[(ri + 1) * QJ + cj] * rdt / rdx);
-                real c2 = gpu[at2(d, I0 + ri, j)] * (sUa[ri * QJ + cj] * rdt / rdx);
-                if (a.split == SP_L04) out = (q * g + real(0.5) * dF + real(0.5) * (c1 - c2) * q) / g;
-                else out = real(0.5) * (q + (q + dF) / (real(1.0) - (c1 - c2)));
+        // C: splitting (discrete_operators.py:49-73)
+        for (int r = ty; r < ni; r += NW)  // Qx: rows I0+r, cols J0-3+c
+            for (int c = tx; c < nj + 6; c += 32) {
+                const int sq = (r + 3) * QJ + c;
+                const real q = sQ[sq], g = sG[sq];
+                real dF = -(sFx[(r + 1) * QJ + c] - sFx[r * QJ + c]);
+                dF = D::exact ? dF * rdt / rdx : dF * dtdx;
+                real out;
+                if (a.split == SP_AVLT) {
+                    out = D::exact ? (q * g + real(0.5) * dF) / g : q + real(0.5) * dF * sIG[sq];
+                } else {
+                    const real c1 = sGu[(r + 2) * QJ + c] * (D::exact ? sUa[(r + 1) * QJ + c] * rdt / rdx
+                                                                      : sUa[(r + 1) * QJ + c] * dtdx);
+                    const real c2 = sGu[(r + 1) * QJ + c] * (D::exact ? sUa[r * QJ + c] * rdt / rdx
+                                                                      : sUa[r * QJ + c] * dtdx);
+                    if (a.split == SP_L04)
+                        out = D::exact ? (q * g + real(0.5) * dF + real(0.5) * (c1 - c2) * q) / g
+                                       : (q * g + real(0.5) * dF + real(0.5) * (c1 - c2) * q) * sIG[sq];
+                    else
+                        out = real(0.5) * (q + (q + dF) / (real(1.0) - (c1 - c2)));
+                }
+                sQx[r * QJ + c] = out;
             }
-            sQx[t] = out;
-        }
-        for (int t = tid; t < QI * TJ; t += nth) {  // Qy: rows I0-3+ri, cols J0+cj
-            int ri = t / TJ, cj = t % TJ;
-            if (ri >= ni + 6 || cj >= nj) continue;
-            const int sq = ri * QJ + cj + 3;
-            const real q = sQ[sq], g = sG[sq];
-            real dF = -(sFy[ri * (TJ + 1) + cj + 1] - sFy[ri * (TJ + 1) + cj]);
-            dF = dF * rdt / rdx;
-            real out;
-            if (a.split == SP_AVLT) {
-                out = (q * g + real(0.5) * dF) / g;
-            } else {
-                const int i = I0 - 3 + ri;
-                real c1 = gpv[at2(d, i, J0 + cj + 1)] * (sVa[ri * (TJ + 1) + cj + 1] * rdt / rdx);
-                real c2 = gpv[at2(d, i, J0 + cj)] * (sVa[ri * (TJ + 1) + cj] * rdt / rdx);
-                if (a.split == SP_L04) out = (q * g + real(0.5) * dF + real(0.5) * (c1 - c2) * q) / g;
-                else out = real(0.5) * (q + (q + dF) / (real(1.0) - (c1 - c2)));
+        for (int r = ty; r < ni + 6; r += NW)  // Qy: rows I0-3+r, cols J0+c
+            for (int c = tx; c < nj; c += 32) {
+                const int sq = r * QJ + c + 3;
+                const real q = sQ[sq], g = sG[sq];
+                real dF = -(sFy[r * (TJ + 1) + c + 1] - sFy[r * (TJ + 1) + c]);
+                dF = D::exact ? dF * rdt / rdx : dF * dtdx;
+                real out;
+                if (a.split == SP_AVLT) {
+                    out = D::exact ? (q * g + real(0.5) * dF) / g : q + real(0.5) * dF * sIG[sq];
+                } else {
+                    const real c1 = sGv[r * (TJ + 3) + c + 2] * (D::exact ? sVa[r * (TJ + 1) + c + 1] * rdt / rdx
+                                                                         : sVa[r * (TJ + 1) + c + 1] * dtdx);
+                    const real c2 = sGv[r * (TJ + 3) + c + 1] * (D::exact ? sVa[r * (TJ + 1) + c] * rdt / rdx
+                                                                         : sVa[r * (TJ + 1) + c] * dtdx);
+                    if (a.split == SP_L04)
+                        out = D::exact ? (q * g + real(0.5) * dF + real(0.5) * (c1 - c2) * q) / g
+                                       : (q * g + real(0.5) * dF + real(0.5) * (c1 - c2) * q) * sIG[sq];
+                    else
+                        out = real(0.5) * (q + (q + dF) / (real(1.0) - (c1 - c2)));
+                }
+                sQy[r * TJ + c] = out;
             }
-            sQy[t] = out;
-        }
         __syncthreads();
         // D: second-pass fluxes (x of Qy, y of Qx) on the tile's edges
-        for (int t = tid; t < (TI + 1) * TJ; t += nth) {
-            int ei = t / TJ, cj = t % TJ;
-            if (ei > ni || cj >= nj) continue;
-            const int wi = ei * QJ + cj + 3;  // wind index (cols offset by 3)
-            const bool up = sUp[wi];
-            const int c = ei + (up ? 2 : 3);  // upwind cell's row in sQy
-            real w[5];
+        for (int e = ty; e <= ni; e += NW)
+            for (int c = tx; c < nj; c += 32) {
+                const int wi = e * QJ + c + 3;
+                const bool up = sUp[wi];
+                const int cr = e + (up ? 2 : 3);  // upwind cell's row in sQy
+                real w[5];
 #pragma unroll
-            for (int m = 0; m < 5; ++m) w[m] = sQy[(c - 2 + m) * TJ + cj];
-            const int ci = I0 - 3 + c, j = J0 + cj;
-            const real u = sUa[wi];
-            const real cc = u * rdt / rdx;
-            sFx[ei * QJ + cj + 3] = ppm_flux<real, REC>(w, up, u, cc, gpu[at2(d, ci, j)], gpu[at2(d, ci + 1, j)],
-                                                        sG[c * QJ + cj + 3], gpu[at2(d, I0 + ei, j)], a.mt);
-        }
-        for (int t = tid; t < TI * (TJ + 1); t += nth) {
-            int ri = t / (TJ + 1), ej = t % (TJ + 1);
-            if (ri >= ni || ej > nj) continue;
-            const int wi = (ri + 3) * (TJ + 1) + ej;
-            const bool up = sVp[wi];
-            const int c = ej + (up ? 2 : 3);  // upwind cell's column in sQx
-            real w[5];
-#pragma unroll
-            for (int m = 0; m < 5; ++m) w[m] = sQx[ri * QJ + c - 2 + m];
-            const int i = I0 + ri, cjg = J0 - 3 + c;
-            const real v = sVa[wi];
-            const real cc = v * rdt / rdx;
-            sFy[(ri + 3) * (TJ + 1) + ej] = ppm_flux<real, REC>(w, up, v, cc, gpv[at2(d, i, cjg)],
-                                                                gpv[at2(d, i, cjg + 1)], sG[(ri + 3) * QJ + c],
-                                                                gpv[at2(d, i, J0 + ej)], a.mt);
-        }
-        __syncthreads();
-        // E: divergence and update
-        double acc = 0.0;
-        for (int t = tid; t < TI * TJ; t += nth) {
-            int ri = t / TJ, cj = t % TJ;
-            if (ri >= ni || cj >= nj) continue;
-            real dFx = -(sFx[(ri + 1) * QJ + cj + 3] - sFx[ri * QJ + cj + 3]);
-            dFx = dFx * rdt / rdx;
-            real dFy = -(sFy[(ri + 3) * (TJ + 1) + cj + 1] - sFy[(ri + 3) * (TJ + 1) + cj]);
-            dFy = dFy * rdt / rdx;
-            const int sq = (ri + 3) * QJ + cj + 3;
-            const real g = sG[sq];
-            const real dv = -(dFx + dFy) / (rdt * g);
-            Qout[at(d, p, I0 + ri, J0 + cj)] = sQ[sq] - rdt * dv;
-            if (a.mfpr) acc += (double)dv * (double)g;
-        }
-        if (a.mfpr) {
-            red[tid] = acc;
-            __syncthreads();
-            for (int s = nth / 2; s > 0; s >>= 1) {
-                if (tid < s) red[tid] += red[tid + s];
-                __syncthreads();
+                for (int m = 0; m < 5; ++m) w[m] = sQy[(cr - 2 + m) * TJ + c];
+                const real u = sUa[wi];
+                const real cc = D::exact ? u * rdt / rdx : u * dtdx;
+                sFx[wi] = ppm_flux<real, REC>(w, up, u, cc, sGu[(cr - 2) * QJ + c + 3], sGu[(cr - 1) * QJ + c + 3],
+                                              sG[cr * QJ + c + 3], sGu[(e + 1) * QJ + c + 3], a.mt);
             }
-            if (tid == 0) a.partials[(size_t)tr * gridDim.x + blockIdx.x] = red[0];
+        for (int r = ty; r < ni; r += NW)
+            for (int e = tx; e <= nj; e += 32) {
+                const int wi = (r + 3) * (TJ + 1) + e;
+                const bool up = sVp[wi];
+                const int cc0 = e + (up ? 2 : 3);  // upwind cell's column in sQx
+                real w[5];
+#pragma unroll
+                for (int m = 0; m < 5; ++m) w[m] = sQx[r * QJ + cc0 - 2 + m];
+                const real v = sVa[wi];
+                const real cc = D::exact ? v * rdt / rdx : v * dtdx;
+                sFy[wi] = ppm_flux<real, REC>(w, up, v, cc, sGv[(r + 3) * (TJ + 3) + cc0 - 2],
+                                              sGv[(r + 3) * (TJ + 3) + cc0 - 1], sG[(r + 3) * QJ + cc0],
+                                              sGv[(r + 3) * (TJ + 3) + e + 1], a.mt);
+            }
+        __syncthreads();
+        // E: divergence and update; the MF-PR partial sum is kept in the state's precision
+        // per thread (at most a few cells) and in FP64 across threads and CTAs
+        real acc = real(0);
+        for (int r = ty; r < ni; r += NW)
+            for (int c = tx; c < nj; c += 32) {
+                const real s = (sFx[(r + 1) * QJ + c + 3] - sFx[r * QJ + c + 3]) +
+                               (sFy[(r + 3) * (TJ + 1) + c + 1] - sFy[(r + 3) * (TJ + 1) + c]);
+                const int sq = (r + 3) * QJ + c + 3;
+                real dv, qn;
+                if (D::exact) {
+                    real dFx = -(sFx[(r + 1) * QJ + c + 3] - sFx[r * QJ + c + 3]);
+                    dFx = dFx * rdt / rdx;
+                    real dFy = -(sFy[(r + 3) * (TJ + 1) + c + 1] - sFy[(r + 3) * (TJ + 1) + c]);
+                    dFy = dFy * rdt / rdx;
+                    dv = -(dFx + dFy) / (rdt * sG[sq]);
+                    qn = sQ[sq] - rdt * dv;
+                } else {
+                    // div = (fluxes out - in) / (dx g); Q - dt div
+                    dv = s * sIG[sq] * (real(1) / rdx);
+                    qn = sQ[sq] - s * dtdx * sIG[sq];
+                }
+                Qout[(I0 + r) * P + J0 + c] = qn;
+                if (a.mfpr) acc += dv * sG[sq];
+            }
+        if (a.mfpr) {
+            double dacc = (double)acc;
+            for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
+            if (tx == 0) red[ty] = dacc;
+            __syncthreads();
+            if (tid == 0) {
+                double s = 0.0;
+                for (int w = 0; w < NW; ++w) s += red[w];
+                a.partials[(size_t)tr * gridDim.x + blockIdx.x] = s;
+            }
         }
         __syncthreads();
     }
@@ -371,14 +412,14 @@ __global__ void __launch_bounds__(256) k_fused(FusedArgs a) {
 template <class real, int TI, int TJ>
 constexpr size_t fused_smem_bytes() {
     constexpr int QI = TI + 6, QJ = TJ + 6;
-    size_t reals = (size_t)(TI + 1) * QJ + QI * (TJ + 1) + QI * QJ + QI * QJ + (TI + 1) * QJ + QI * (TJ + 1) +
-                   TI * QJ + QI * TJ;
+    size_t reals = (size_t)(TI + 1) * QJ + QI * (TJ + 1) + 2 * QI * QJ + (TI + 3) * QJ + QI * (TJ + 3) + QI * QJ +
+                   (TI + 1) * QJ + QI * (TJ + 1) + TI * QJ + QI * TJ;
     size_t bytes = reals * sizeof(real) + (size_t)(TI + 1) * QJ + QI * (TJ + 1);
     return (bytes + 15) / 16 * 16;
 }
 
 // tile shapes selectable per launch (the autotuner times them): {TI, TJ}
-constexpr int FUSED_TILES[][2] = {{16, 32}, {32, 32}, {32, 64}, {64, 32}};
+constexpr int FUSED_TILES[][2] = {{16, 58}, {32, 58}, {16, 26}, {32, 26}};
 constexpr int FUSED_NTILE_CFG = 4;
 
 template <class real, int REC, int TI, int TJ>
@@ -391,7 +432,7 @@ static int fused_go(FusedArgs a, cudaStream_t st) {
     }
     a.ntj = (a.d.N + TJ - 1) / TJ;
     a.ntiles = ((a.d.N + TI - 1) / TI) * a.ntj;
-    k_fused<real, REC, TI, TJ><<<NFACE * a.ntiles, 256, smem, st>>>(a);
+    k_fused<real, REC, TI, TJ><<<NFACE * a.ntiles, dim3(32, 8), smem, st>>>(a);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -399,10 +440,10 @@ static int fused_go(FusedArgs a, cudaStream_t st) {
 template <class real, int REC>
 static int fused_tile(FusedArgs a, int tile, cudaStream_t st) {
     switch (tile) {
-        case 0: return fused_go<real, REC, 16, 32>(a, st);
-        case 1: return fused_go<real, REC, 32, 32>(a, st);
-        case 2: return fused_go<real, REC, 32, 64>(a, st);
-        default: return fused_go<real, REC, 64, 32>(a, st);
+        case 0: return fused_go<real, REC, 16, 58>(a, st);
+        case 1: return fused_go<real, REC, 32, 58>(a, st);
+        case 2: return fused_go<real, REC, 16, 26>(a, st);
+        default: return fused_go<real, REC, 32, 26>(a, st);
     }
 }
 

@@ -1,4 +1,5 @@
-// float64 instantiations of the fused step kernel.
+// float64 instantiations of the fused step kernel (FMA contraction allowed; parity with the
+// reference is checked at 1e-12 relative in tests/test_gpu_fused.py).
 #include "fused.cuh"
 
 namespace csadv {

@@ -97,17 +97,18 @@ int fused_prepare(const Options &o, int tile) {
                              : fused_launch<float>(a, o.recon, tile, (cudaStream_t)-1);
 }
 
-int fused_step(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
-               cudaEvent_t ev0, cudaEvent_t ev1) {
+int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
     const bool pr = o.mf == MF_PR;
-    int rc;
     if (o.precision == 64)
-        rc = launch_halo_dg_tracers<double>((double *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
-                                            (const double *)f.g_pc, st);
-    else
-        rc = launch_halo_dg_tracers<float>((float *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
-                                           (const float *)f.g_pc, st);
-    if (rc) return rc;
+        return launch_halo_dg_tracers<double>((double *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
+                                              (const double *)f.g_pc, st);
+    return launch_halo_dg_tracers<float>((float *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
+                                         (const float *)f.g_pc, st);
+}
+
+int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
+                 cudaEvent_t ev0, cudaEvent_t ev1) {
+    const bool pr = o.mf == MF_PR;
     FusedArgs a{};
     a.d = g.d;
     a.T = T;
@@ -132,7 +133,8 @@ int fused_step(const Options &o, const Grid &g, double dt, int T, FusedState &f,
     a.mfpr = pr ? 1 : 0;
     a.wpitch = f.wpitch;
     if (ev0) CSADV_CUDA(cudaEventRecord(ev0, st));
-    rc = o.precision == 64 ? fused_launch<double>(a, o.recon, f.tile, st) : fused_launch<float>(a, o.recon, f.tile, st);
+    int rc = o.precision == 64 ? fused_launch<double>(a, o.recon, f.tile, st)
+                               : fused_launch<float>(a, o.recon, f.tile, st);
     if (rc) return rc;
     if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
     cur = 1 - cur;

@@ -102,7 +102,7 @@ int wind_average(const Options &o, const Grid &g, Winds &w, double dt, cudaStrea
 template <class real>
 int wind_avgprep(const Options &o, const Grid &g, const Winds &w, double dt, real *ua, real *va, uint32_t *ub,
                  uint32_t *vb, int wpitch, cudaStream_t st);
-int wind_cfl(const Grid &g, const Winds &w, double dt, double *dev_tmp, double &cfl, cudaStream_t st);
+int wind_cfl(const Options &o, const Grid &g, const Winds &w, double dt, double *dev_tmp, double &cfl, cudaStream_t st);
 
 // ---------------------------------------------------------------- fused engine state
 struct FusedState {
@@ -121,9 +121,11 @@ struct FusedState {
 int fused_supported(const Options &o);
 int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedState &f, cudaStream_t st);
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, cudaStream_t st);
-// one step: ghost cells of Qbuf[cur] (+ correction), fused kernel into Qbuf[1-cur]; cur flips
-int fused_step(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
-               cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
+// ghost cells of every tracer of Qbuf[cur] (with the pending correction applied)
+int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
+// the fused kernel Qbuf[cur] -> Qbuf[1-cur]; cur flips
+int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
+                 cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 // set the dynamic shared-memory limit of the kernel a plan will launch (outside capture)
 int fused_prepare(const Options &o, int tile);
 // ghost cells of Qbuf[cur] <- those of Qbuf[1-cur] (the halo the last step used)

@@ -215,7 +215,7 @@ __global__ void k_edges_extrap(ParabolaRefs<real> r, Dims d, EdgePairs pairs, in
 // numerical_flux_ppm_x / _y (flux.py:20-128): edges [i0, iend] along the direction
 template <class real, int DIR>
 __global__ void k_flux(const real *__restrict__ A, const real *__restrict__ qL, const real *__restrict__ qR, real *f,
-                       const double *__restrict__ uavg, const double *__restrict__ ucur,
+                       const real *__restrict__ uavg, const real *__restrict__ ucur,
                        const double *__restrict__ gE, const double *__restrict__ gC, Dims d, double dt, double dx,
                        int mt) {
     const int n = d.n, nedge = d.N + 1;
@@ -233,7 +233,7 @@ __global__ void k_flux(const real *__restrict__ A, const real *__restrict__ qL, 
     }
     long long oe = lat<DIR>(d, p, l, e);
     auto g2 = [&](const double *g, int k) { return DIR == 0 ? g[at2(d, k, l)] : g[at2(d, l, k)]; };
-    const bool upos = ucur[oe] >= 0.0;
+    const bool upos = ucur[oe] >= real(0);
     const int c = upos ? e - 1 : e;
     long long oc = lat<DIR>(d, p, l, c);
     real L = qL[oc], R = qR[oc], q = A[oc];
@@ -244,12 +244,12 @@ __global__ void k_flux(const real *__restrict__ A, const real *__restrict__ qL, 
     }
     real dq = R - L;
     real q6 = real(6) * q - real(3) * (R + L);
-    const double ua = uavg[oe];
-    const real cc = (real)(ua * dt / dx);
+    const real ua = uavg[oe];
+    const real cc = ua * (real)dt / (real)dx;
     real fl;
     if (upos) fl = R + cc * real(0.5) * (q6 - dq) - q6 * cc * cc / real(3.0);
     else fl = L - cc * real(0.5) * (q6 + dq) - q6 * cc * cc / real(3.0);
-    fl = fl * (real)ua;
+    fl = fl * ua;
     if (mt == MT_PL07) fl = fl * (real)g2(gE, e);
     f[oe] = fl;
 }
@@ -290,8 +290,8 @@ __global__ void k_mfaf(real *fx, real *fy, Dims d, EdgePairs pairs) {
 template <class real>
 __global__ void k_split(const real *__restrict__ Q, const real *__restrict__ fx, const real *__restrict__ fy, real *Qx,
                         real *Qy, const double *__restrict__ g_pc, const double *__restrict__ g_pu,
-                        const double *__restrict__ g_pv, const double *__restrict__ uavg,
-                        const double *__restrict__ vavg, Dims d, double dt, double dx, int split) {
+                        const double *__restrict__ g_pv, const real *__restrict__ uavg,
+                        const real *__restrict__ vavg, Dims d, double dt, double dx, int split) {
     const int n = d.n;
     long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= (long long)NFACE * n * n) return;
@@ -315,10 +315,10 @@ __global__ void k_split(const real *__restrict__ Q, const real *__restrict__ fx,
         Qy[o] = (gQ + real(0.5) * dFy) / g;
         return;
     }
-    real c1x = (real)g_pu[at2(d, i + 1, j)] * (real)(uavg[at(d, p, i + 1, j)] * dt / dx);
-    real c2x = (real)g_pu[at2(d, i, j)] * (real)(uavg[o] * dt / dx);
-    real c1y = (real)g_pv[at2(d, i, j + 1)] * (real)(vavg[at(d, p, i, j + 1)] * dt / dx);
-    real c2y = (real)g_pv[at2(d, i, j)] * (real)(vavg[o] * dt / dx);
+    real c1x = (real)g_pu[at2(d, i + 1, j)] * (uavg[at(d, p, i + 1, j)] * rdt / rdx);
+    real c2x = (real)g_pu[at2(d, i, j)] * (uavg[o] * rdt / rdx);
+    real c1y = (real)g_pv[at2(d, i, j + 1)] * (vavg[at(d, p, i, j + 1)] * rdt / rdx);
+    real c2y = (real)g_pv[at2(d, i, j)] * (vavg[o] * rdt / rdx);
     if (split == SP_L04) {
         real gQ = q * g;
         Qx[o] = (gQ + real(0.5) * dFx + real(0.5) * (c1x - c2x) * q) / g;
@@ -442,10 +442,10 @@ static int compute_fluxes(const Options &o, const Grid &g, const Winds &w, doubl
         k_edges_extrap<real><<<ceil_div(12LL * d.N, 128), 128, 0, st>>>(r, d, edge_pairs(), o.recon);
     }
     long long tot = (long long)NFACE * (d.N + 1) * d.n;
-    k_flux<real, 0><<<ceil_div(tot, 128), 128, 0, st>>>(Qa, qLx, qRx, (real *)s.fx, w.u_avg, w.u_pu, g.g_pu, g.g_pc,
-                                                        d, dt, g.dx, o.mt);
-    k_flux<real, 1><<<ceil_div(tot, 128), 128, 0, st>>>(Qb, qLy, qRy, (real *)s.fy, w.v_avg, w.v_pv, g.g_pv, g.g_pc,
-                                                        d, dt, g.dx, o.mt);
+    k_flux<real, 0><<<ceil_div(tot, 128), 128, 0, st>>>(Qa, qLx, qRx, (real *)s.fx, (const real *)w.u_avg,
+                                                        (const real *)w.u_pu, g.g_pu, g.g_pc, d, dt, g.dx, o.mt);
+    k_flux<real, 1><<<ceil_div(tot, 128), 128, 0, st>>>(Qb, qLy, qRy, (real *)s.fy, (const real *)w.v_avg,
+                                                        (const real *)w.v_pv, g.g_pv, g.g_pc, d, dt, g.dx, o.mt);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -462,7 +462,8 @@ int staged_divergence(const Options &o, const Grid &g, const Winds &w, double dt
     real *Qx = (real *)s.Qx, *Qy = (real *)s.Qy;
     long long tot = (long long)NFACE * d.n * d.n;
     k_split<real><<<ceil_div(tot, 128), 128, 0, st>>>(Q, (real *)s.fx, (real *)s.fy, Qx, Qy, g.g_pc, g.g_pu, g.g_pv,
-                                                      w.u_avg, w.v_avg, d, dt, g.dx, o.opsplit);
+                                                      (const real *)w.u_avg, (const real *)w.v_avg, d, dt, g.dx,
+                                                      o.opsplit);
     if (o.et != ET_DG) {
         rc = launch_halo_adjacent<real>(Qx, Qy, g, st);
         if (rc) return rc;
