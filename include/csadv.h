@@ -149,6 +149,20 @@ typedef struct csadv_stats {
 int csadv_get_stats(csadv_plan *plan, csadv_stats *out);
 int csadv_reset_stats(csadv_plan *plan);
 
+/* ---------------------------------------------------------------- allocation-free mass fixer */
+/* No counterpart in the reference.  The divergence-projection mass fixer (the MF-PR step of
+ * divergence, div -= g * sum(div g) / sum(g g) over the interior) applied to caller-owned
+ * DEVICE arrays in the reference layout (N+8, N+8, 6) float64: div_in (a divergence),
+ * metric (sqrt(g) at the cell centres, cs_grid.metric_tensor_pc), div_out (may equal
+ * div_in; non-interior cells are copied).  For callers that cannot call cudaMalloc (a
+ * service whose device memory is fully committed, or memory owned by another runtime's
+ * pool): it needs no plan and allocates nothing; its reduction scratch is a fixed 98 KB
+ * device array inside the library, held by every GPU that loads it until exit.
+ * Limit: N <= 2048 (CSADV_ERR_TOO_LARGE beyond).  The first call on a device looks up the
+ * scratch's device address; make it before any stream capture.  Calls that overlap on the
+ * GPU share the scratch and race; order them on one stream. */
+int csadv_mass_fixer_noalloc(const double *div_in, const double *metric, double *div_out, int N, void *stream);
+
 /* ---------------------------------------------------------------- pinned host memory */
 int csadv_host_alloc(void **ptr, size_t bytes);
 int csadv_host_free(void *ptr);

@@ -78,6 +78,7 @@ _SIGS = {
     "csadv_set_profiling": ([_vp, _c_int], _c_int),
     "csadv_get_stats": ([_vp, ctypes.POINTER(Stats)], _c_int),
     "csadv_reset_stats": ([_vp], _c_int),
+    "csadv_mass_fixer_noalloc": ([_vp, _vp, _vp, _c_int, _vp], _c_int),
     "csadv_host_alloc": ([ctypes.POINTER(_vp), ctypes.c_size_t], _c_int),
     "csadv_host_free": ([_vp], _c_int),
 }

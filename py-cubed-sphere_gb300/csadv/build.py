@@ -36,6 +36,7 @@ UNITS = {
     "fused_host.cu": False,
     "fused_f32.cu": True,
     "fused_f64.cu": True,
+    "noalloc.cu": False,
 }
 
 
