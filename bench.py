@@ -57,6 +57,19 @@ def dt_for_cfl(make_plan):
     return 1e-3 * CFL / c
 
 
+def profiled_traffic(key):
+    """DRAM bytes (read + write) of one launch of the step kernel on this workload, from the
+    committed ncu summary (a `key = value` line); None when absent."""
+    path = os.path.join(ROOT, "profiles", "k_fused_N384_T2.md")
+    try:
+        for ln in open(path):
+            if ln.strip().startswith(key + " ="):
+                return int(ln.split("=")[1])
+    except OSError:
+        pass
+    return None
+
+
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms while active."""
@@ -274,12 +287,7 @@ def bench_gpu(args):
             "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
             "traffic": None, "kernel_ms": round(kms, 5), "alg_bytes_per_launch": alg,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(prof):
-        try:
-            roof["traffic"] = json.load(open(prof)).get("k_fused_f32_bytes_per_launch")
-        except Exception:
-            pass
+    roof["traffic"] = profiled_traffic("dram_bytes_per_launch")
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "tracer cell-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
