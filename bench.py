@@ -219,6 +219,98 @@ def run_e2e(torch, precision, steps, stream):
     return sec, NTRACERS * nb_in, NTRACERS * nb_out
 
 
+# ----------------------------------------------------------------------------- batched and serving legs
+BATCH_SOLVES = 256
+BATCH_NS = (48, 96, 192, 384, 768)
+
+
+def batched_requests(n=BATCH_SOLVES, seed=0, steps=200):
+    """256 independent FP32 solves: N uniform in {48, 96, 192, 384, 768}, 1-3 tracers of
+    Gaussian hills (centres uniform on the sphere, width parameter uniform in [2, 10]),
+    solid-body rotation at an angle uniform in [0, pi/2], CFL 0.5, 200 steps."""
+    import math
+    import numpy as np
+    from csadv import serve
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        N = int(rng.choice(BATCH_NS))
+        T = int(rng.integers(1, 4))
+        hills = tuple((float(rng.uniform(-math.pi, math.pi)), float(math.asin(rng.uniform(-1.0, 1.0))),
+                       float(rng.uniform(2.0, 10.0))) for _ in range(T))
+        out.append(serve.Request(rid=i, N=N, steps=steps, tracers=T, wind="solid",
+                                 alpha=float(rng.uniform(0.0, math.pi / 2)), hills=hills))
+    return out
+
+
+def run_batched(torch, steps, warmup, stream, hbm):
+    """All 256 solves in one batch: one step-kernel launch per step for all of them, tile
+    shapes from the autotuner (one probe plan per distinct N and tracer count).  The resident
+    state (~10 GB) is far larger than L2, so no flush is needed between steps."""
+    from csadv import Batch, serve, tune
+    reqs = batched_requests()
+    tiles = {}
+    for key in sorted({(r.N, r.tracers) for r in reqs}):
+        probe = next(r for r in reqs if (r.N, r.tracers) == key)
+        with serve.make_plan(probe, 32, 0.5, stream) as pl:
+            tiles["%dx%d" % key] = tune(pl, reps=3, stream=stream)
+    t0 = time.perf_counter()
+    plans = [serve.make_plan(r, 32, 0.5, stream) for r in reqs]
+    torch.cuda.synchronize()
+    create_s = time.perf_counter() - t0
+    b = Batch(len(plans))
+    for pl in plans:
+        b.add(pl)
+    b.advance(warmup, stream)
+    torch.cuda.synchronize()
+    b.reset_stats()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    b.advance(steps, stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    st = b.stats()
+    b.set_profiling(True)
+    b.reset_stats()
+    b.advance(max(3, steps // 4), stream)
+    pst = b.stats()
+    b.set_profiling(False)
+    kms = pst["main_ms"] / max(1, pst["main_launches"])
+    cells = sum(6 * r.N * r.N * r.tracers for r in reqs)
+    alg = sum(6 * r.N * r.N * (r.tracers * 2 * 4 + 3 * 4) for r in reqs)
+    b.close()
+    for pl in plans:
+        pl.close()
+    achieved = alg / (kms * 1e-3) / 1e9
+    return {"value": round(cells / (ms * 1e-3), 1), "unit": "tracer cell-steps/s", "solves": len(reqs),
+            "ms_per_step": round(ms, 4), "kernels_per_step": st["kernels_per_step"],
+            "gpu_launches": st["kernel_launches"], "step_kernel_ms": round(kms, 4),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "alg_bytes_per_launch": alg},
+            "plan_create_s": round(create_s, 2), "tiles": tiles,
+            "config": "256 solves, N in {48,96,192,384,768}, 1-3 tracers, solid-body wind at random angles, "
+                      "Gaussian hills, CFL 0.5, FP32 (timed: %d of the 200 steps)" % steps}
+
+
+def run_serving(torch, nreq, stream, budget_gb=120.0):
+    """The request loop on a seeded Poisson stream (200 req/s; N log-uniform in [32, 1024],
+    steps uniform in [50, 2000], 1-4 tracers, solid-body or deformational wind 50/50, FP32,
+    120 GB budget), truncated to the first `nreq` requests."""
+    from csadv import serve
+    reqs = serve.poisson_requests(nreq, rate=200.0, seed=0)
+    srv = serve.Server(budget_bytes=budget_gb * 1e9, precision=32, stream=stream)
+    _, summ = srv.run(reqs, realtime=True)
+    offered = sum(6 * r.N * r.N * r.tracers * r.steps for r in reqs) / max(reqs[-1].arrival, 1e-9)
+    return {"requests": summ["requests"], "p50_latency_s": round(summ["p50_latency_s"], 3),
+            "p99_latency_s": round(summ["p99_latency_s"], 3), "value": round(summ["throughput"], 1),
+            "unit": "tracer cell-steps/s", "wall_s": round(summ["wall_s"], 2),
+            "offered_load": round(offered, 1), "peak_resident_gb": round(summ["peak_bytes"] / 1e9, 2),
+            "budget_gb": budget_gb, "max_mass_change": float("%.3e" % summ["max_mass_change"]),
+            "config": "Poisson 200 req/s, N log-uniform [32,1024], steps U[50,2000], 1-4 tracers, "
+                      "solid/deformational 50/50, FP32, first %d requests of the seeded stream" % nreq}
+
+
 def cpu_sample(nsteps):
     """The oracle (numpy restatement of the reference) on this host, one core."""
     from oracle import cases, solver
@@ -304,6 +396,11 @@ def bench_gpu(args):
         "clocks": clk.summary(),
         "errors_fp32_linf_l1_l2_vs_exact": [float("%.4e" % e) for e in f32["errors_linf_l1_l2"]],
     }
+    if not args.no_batched:
+        line["batched"] = run_batched(torch, args.batched_steps, args.warmup, stream, hbm)
+        line["batched"]["vs_fp64_single"] = round(line["batched"]["value"] / line["fp64"]["value"], 2)
+    if args.serve_requests > 0:
+        line["serving"] = run_serving(torch, args.serve_requests, stream)
     if world == 1 and not args.no_cpu:
         k = 2
         line["cpu_baseline"] = {"value": round(cpu_sample(k), 1), "unit": "tracer cell-steps/s", "cores": 1,
@@ -355,6 +452,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="csadv", choices=("csadv", "reference"))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-solve batched leg")
+    ap.add_argument("--batched-steps", type=int, default=20, help="timed steps of the batched leg")
+    ap.add_argument("--serve-requests", type=int, default=0,
+                    help="run the serving leg on the first N requests of the seeded stream (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -72,8 +72,10 @@ typedef struct csadv_options {
     int vf;        /* wind code (see above) */
     int precision; /* 64: state in float64 ("plain form"); 32: state/PPM/fluxes in float32 */
     int engine;    /* CSADV_ENGINE_* */
-    int tile;      /* fused engine tile (rows x columns of cells): 1 = 16x58, 2 = 32x58, 3 = 16x26,
-                      4 = 32x26; 0 = default (4 for FP32, 3 for FP64) */
+    int tile;      /* fused engine tile (rows x columns of cells).  Per-edge tile kernel: 1 = 16x58,
+                      2 = 32x58, 3 = 16x26, 4 = 32x26.  Line-marching kernel: 5 = 58x58, 6 = 58x26,
+                      7 = 26x58, 8 = 26x26.  0 = default: the tile csadv_tune chose for this shape,
+                      else 5 for N >= 116 and 8 below */
     double wind_param[4];
 } csadv_options;
 
@@ -91,10 +93,13 @@ int csadv_set_device(int device);
  * builds the FP64 grid and Lagrange tables on the device, allocates the tracer state and
  * scratch, and computes the t = 0 winds, wind halo and departure-point winds.
  * Tracers start at zero; set them with csadv_init_tracer / csadv_set_tracer.
+ * dt > 0 is the time step; dt < 0 asks for the time step whose CFL number (as
+ * advection_vars.py:89-98 defines it, from the t = 0 winds) is -dt (csadv_get_dt reads it).
  * Errors: CSADV_ERR_OPTION, CSADV_ERR_OPTION_PAIR, CSADV_ERR_ARG, CSADV_ERR_OOM. */
 int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, void *stream,
                       csadv_plan **out);
 int csadv_plan_destroy(csadv_plan *plan);
+int csadv_get_dt(const csadv_plan *plan, double *dt);
 
 /* q0_adv (advection_ic.py:208-210) evaluated on the device at the interior cell centres
  * (the reference's Q0 is a point value, advection_vars.py:105). */
@@ -142,12 +147,43 @@ typedef struct csadv_stats {
     double main_ms;             /* their total device time */
     int kernels_per_step;       /* kernel launches of one step (from the captured graph; 0 if none yet) */
     int engine;                 /* CSADV_ENGINE_STAGED or CSADV_ENGINE_FUSED */
-    int tile;                   /* fused tile shape in use (1..4), 0 for staged */
+    int tile;                   /* fused tile configuration in use (1..8, as csadv_options.tile), 0 for staged */
     int reserved;
-    size_t device_bytes;        /* device memory held by the plan */
+    size_t device_bytes;        /* device memory held by the plan (with its grid, which plans of one N share) */
 } csadv_stats;
 int csadv_get_stats(csadv_plan *plan, csadv_stats *out);
 int csadv_reset_stats(csadv_plan *plan);
+
+/* ---------------------------------------------------------------- batches of solves */
+/* Replaces the reference's one-solve-at-a-time loop (advection_sphere.py:45-58) when many
+ * independent solves run together; no single reference function corresponds.  A batch
+ * advances every attached plan by one step per step (adv_time_step + update_adv,
+ * advection_timestep.py:19-75) with ONE launch of the step kernel over the tiles of all of
+ * them; each plan's ghost-cell and wind work is launched per plan on the same stream, and a
+ * step is replayed as a CUDA graph while the membership is unchanged.  Plans must use the
+ * fused engine's line-marching kernel (tile 5..8 or the default), one precision and one
+ * reconstruction; N, tracer count, wind, dt and tile may differ (CSADV_ERR_UNSUPPORTED
+ * otherwise).  A plan keeps its own state, step counter and diagnostics; it gives the same
+ * result in a batch as alone.  Destroying an attached plan detaches it. */
+typedef struct csadv_batch csadv_batch;
+int csadv_batch_create(int capacity, csadv_batch **out);
+int csadv_batch_destroy(csadv_batch *batch);
+int csadv_batch_add(csadv_batch *batch, csadv_plan *plan);       /* CSADV_ERR_TOO_LARGE when full */
+int csadv_batch_remove(csadv_batch *batch, csadv_plan *plan);
+int csadv_batch_size(const csadv_batch *batch, int *n);
+int csadv_batch_advance(csadv_batch *batch, int nsteps, void *stream);
+int csadv_batch_set_graphs(csadv_batch *batch, int enable);
+/* profiling: steps launch directly and the step kernel is timed (csadv_stats.main_ms) */
+int csadv_batch_set_profiling(csadv_batch *batch, int enable);
+int csadv_batch_get_stats(const csadv_batch *batch, csadv_stats *out);
+int csadv_batch_reset_stats(csadv_batch *batch);
+
+/* Tile autotuner (no reference counterpart): times the step kernel of `plan` with each
+ * line-marching tile configuration (`reps` launches each, on `stream`, without changing the
+ * plan's state), selects the fastest and remembers it for plans of the same N, tracer count,
+ * precision and scheme created later in the process with tile = 0.  *tile_out (optional)
+ * receives the chosen csadv_options.tile code. */
+int csadv_tune(csadv_plan *plan, int reps, void *stream, int *tile_out);
 
 /* ---------------------------------------------------------------- allocation-free mass fixer */
 /* No counterpart in the reference.  The divergence-projection mass fixer (the MF-PR step of

@@ -63,6 +63,7 @@ _SIGS = {
     "csadv_set_device": ([_c_int], _c_int),
     "csadv_plan_create": ([_c_int, _c_double, _c_int, ctypes.POINTER(Options), _vp, ctypes.POINTER(_vp)], _c_int),
     "csadv_plan_destroy": ([_vp], _c_int),
+    "csadv_get_dt": ([_vp, _dp], _c_int),
     "csadv_init_tracer": ([_vp, _c_int, _c_int, _dp, _vp], _c_int),
     "csadv_set_tracer": ([_vp, _c_int, _vp, _c_int, _vp], _c_int),
     "csadv_get_tracer": ([_vp, _c_int, _vp, _c_int, _vp], _c_int),
@@ -78,6 +79,17 @@ _SIGS = {
     "csadv_set_profiling": ([_vp, _c_int], _c_int),
     "csadv_get_stats": ([_vp, ctypes.POINTER(Stats)], _c_int),
     "csadv_reset_stats": ([_vp], _c_int),
+    "csadv_batch_create": ([_c_int, ctypes.POINTER(_vp)], _c_int),
+    "csadv_batch_destroy": ([_vp], _c_int),
+    "csadv_batch_add": ([_vp, _vp], _c_int),
+    "csadv_batch_remove": ([_vp, _vp], _c_int),
+    "csadv_batch_size": ([_vp, ctypes.POINTER(_c_int)], _c_int),
+    "csadv_batch_advance": ([_vp, _c_int, _vp], _c_int),
+    "csadv_batch_set_graphs": ([_vp, _c_int], _c_int),
+    "csadv_batch_get_stats": ([_vp, ctypes.POINTER(Stats)], _c_int),
+    "csadv_batch_set_profiling": ([_vp, _c_int], _c_int),
+    "csadv_batch_reset_stats": ([_vp], _c_int),
+    "csadv_tune": ([_vp, _c_int, _vp, ctypes.POINTER(_c_int)], _c_int),
     "csadv_mass_fixer_noalloc": ([_vp, _vp, _vp, _c_int, _vp], _c_int),
     "csadv_host_alloc": ([ctypes.POINTER(_vp), ctypes.c_size_t], _c_int),
     "csadv_host_free": ([_vp], _c_int),

@@ -28,6 +28,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 # translation units and whether FMA contraction is allowed in their device code
 UNITS = {
     "api.cu": False,
+    "batch.cu": False,
     "grid.cu": False,
     "halo.cu": False,
     "wind.cu": False,
@@ -36,6 +37,8 @@ UNITS = {
     "fused_host.cu": False,
     "fused_f32.cu": True,
     "fused_f64.cu": True,
+    "sweep_f32.cu": True,
+    "sweep_f64.cu": True,
     "noalloc.cu": False,
 }
 

@@ -9,6 +9,7 @@ from . import _lib as L
 class Plan:
     """A solve resident on the GPU.
 
+    ``dt`` > 0 is the time step; ``dt`` < 0 asks for the time step of CFL number -dt.
     Parameters mirror the reference's ``adv_simulation_par`` option codes (advection.par):
     recon 1-4, dp 1-2, opsplit 1-3, et 1-3, mt 1-2, mf 1-3, and ``vf`` (reference wind
     codes 1-4 or the benchmark winds 101-103 with ``wind_param``).  ``precision`` is 64
@@ -30,6 +31,10 @@ class Plan:
         L.check(L.lib().csadv_plan_create(self.N, self.dt, self.ntracers, ctypes.byref(o), self.stream,
                                           ctypes.byref(h)), "csadv_plan_create")
         self._h = h
+        if self.dt < 0:  # -dt was a CFL target: read the time step chosen
+            v = ctypes.c_double()
+            L.check(L.lib().csadv_get_dt(self._h, ctypes.byref(v)), "csadv_get_dt")
+            self.dt = v.value
 
     # ------------------------------------------------------------------ lifecycle
     def close(self):

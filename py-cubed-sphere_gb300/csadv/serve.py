@@ -1,0 +1,217 @@
+"""Continuous-batching request loop: many advection solves resident on one GPU.
+
+Requests (N, tracer count, step count, wind, Gaussian-hill initial conditions) arrive over
+time.  The loop admits them in arrival order while their device memory fits a budget,
+attaches each admitted solve to one ``Batch`` (one step-kernel launch per step for all
+resident solves, whatever their sizes), advances the batch, and retires a solve as soon as
+it has taken its steps: its error norms against the exact solution and its mass change are
+read, its memory is released, and the next queued request can take its place.  Requests
+that arrive while others are on the GPU join at the next step boundary, so their work
+overlaps on the device.
+
+Everything a solve computes depends only on that solve (the step kernel's reductions have
+a fixed order per solve), so each result is the same alone and in the mix; the tests check
+this bit for bit.
+
+The reference has no counterpart (it runs one solve per process: advection_sphere.py:13-61).
+"""
+import collections
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .batch import Batch
+from .plan import Plan
+
+# the scheme of the serving and batched workloads: monotone PPM (CW84), RK2 departure points,
+# AVLT splitting, Lagrange ghost cells, MT-0, divergence-projection mass fixer
+SCHEME = dict(recon=2, dp=2, opsplit=1, et=3, mt=1, mf=3)
+U0 = 2.0 * math.pi / 5.0   # solid-body speed: one revolution in T = 5 (unit sphere)
+DEFORM = (0.48, 5.0, 0.0, 0.0)  # deformational wind: k = 2.4 R / T, period T = 5
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    N: int
+    steps: int
+    tracers: int
+    wind: str                  # "solid" or "deform"
+    arrival: float = 0.0       # seconds after the start of the run
+    alpha: float = 0.0         # solid-body rotation angle
+    hills: tuple = ()          # per tracer: (lon, lat, width)
+
+
+@dataclasses.dataclass
+class Result:
+    rid: int
+    N: int
+    tracers: int
+    steps: int
+    arrival: float
+    admitted: float
+    finished: float
+    errors: list               # per tracer (Linf, L1, L2) against the exact solution
+    mass_change: list          # per tracer, relative
+    cell_steps: int
+    state: list = None         # per tracer final interior field (keep_state=True)
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+def poisson_requests(n, rate, seed=0, n_range=(32, 1024), steps_range=(50, 2000), tracers=(1, 4),
+                     width_range=(2.0, 10.0)):
+    """A seeded request stream: Poisson arrivals at `rate` per second, N log-uniform in
+    n_range, steps uniform in steps_range, tracer count uniform in tracers (inclusive),
+    wind solid-body or deformational 50/50, hill centres uniform on the sphere."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    out = []
+    lo, hi = math.log(n_range[0]), math.log(n_range[1])
+    for i in range(n):
+        N = int(round(math.exp(rng.uniform(lo, hi))))
+        T = int(rng.integers(tracers[0], tracers[1] + 1))
+        hills = []
+        for _ in range(T):
+            lon = rng.uniform(-math.pi, math.pi)
+            lat = math.asin(rng.uniform(-1.0, 1.0))
+            hills.append((lon, lat, rng.uniform(*width_range)))
+        out.append(Request(rid=i, N=N, steps=int(rng.integers(steps_range[0], steps_range[1] + 1)), tracers=T,
+                           wind="solid" if rng.random() < 0.5 else "deform", arrival=float(t[i]),
+                           alpha=float(rng.uniform(0.0, math.pi / 2)), hills=tuple(hills)))
+    return out
+
+
+def make_plan(req, precision=32, cfl=0.5, stream=None):
+    """The plan of one request, initial conditions set, dt from the CFL number."""
+    if req.wind == "solid":
+        vf, wp = L.WIND_SOLID, (req.alpha, U0, 0.0, 0.0)
+    else:
+        vf, wp = L.WIND_DEFORM, DEFORM
+    kw = dict(vf=vf, wind_param=wp, ntracers=req.tracers, precision=precision, stream=stream, **SCHEME)
+    pl = Plan(req.N, -cfl, **kw)  # dt from the CFL number of the t = 0 wind
+    for t, (lon, lat, w) in enumerate(req.hills):
+        pl.init_tracer(L.IC_HILL, ic_param=(lon, lat, w, 0.0), tracer=t)
+    return pl
+
+
+def finish(pl, req, mass0):
+    """Error norms (vs the exact solution at the final time) and relative mass change."""
+    errs, dm = [], []
+    t_end = pl.step * pl.dt
+    for t, (lon, lat, w) in enumerate(req.hills):
+        errs.append(pl.errors(L.IC_HILL, t_end, ic_param=(lon, lat, w, 0.0), tracer=t) if req.wind == "solid"
+                    else (float("nan"),) * 3)
+        m = pl.mass(t)
+        dm.append(abs(m - mass0[t]) / abs(mass0[t]) if mass0[t] != 0 else abs(m))
+    return errs, dm
+
+
+def plane_elems(N):
+    n = N + 8
+    return 6 * (n + 1) * ((n + 1 + 31) // 32 * 32)
+
+
+class Server:
+    """The request loop.  budget_bytes bounds the device memory of resident solves."""
+
+    def __init__(self, budget_bytes, precision=32, cfl=0.5, max_active=512, stream=None, clock=time.perf_counter,
+                 keep_state=False, max_steps_per_tick=8):
+        self.budget = int(budget_bytes)
+        self.precision = precision
+        self.cfl = cfl
+        self.max_active = max_active
+        self.stream = stream
+        self.clock = clock
+        self.keep_state = keep_state
+        self.max_steps_per_tick = max_steps_per_tick
+        self._coef = {}
+
+    # device bytes of a plan ~ plane elements x (a + b T), per wind kind; measured once
+    def estimate(self, req):
+        key = req.wind
+        if key not in self._coef:
+            sizes = []
+            for T in (1, 2):
+                probe = Request(rid=-1, N=32, steps=1, tracers=T, wind=req.wind, hills=((0.0, 0.0, 5.0),) * T)
+                with make_plan(probe, self.precision, self.cfl, self.stream) as pl:
+                    sizes.append(pl.stats()["device_bytes"] / plane_elems(32))
+            self._coef[key] = (2 * sizes[0] - sizes[1], sizes[1] - sizes[0])
+        a, b = self._coef[key]
+        return int(plane_elems(req.N) * (a + b * req.tracers) * 1.02) + (1 << 20)
+
+    def run(self, requests, realtime=True, on_step=None):
+        """Serve `requests` (sorted by arrival).  realtime: arrivals follow the wall clock;
+        otherwise every request is available at once.  Returns (results, summary)."""
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        queue = collections.deque()
+        active = {}      # id(plan) -> [plan, req, remaining, admitted, mass0, bytes]
+        used = 0
+        results = []
+        batch = Batch(self.max_active)
+        t0 = self.clock()
+        steps = 0
+        peak = 0
+        try:
+            while pending or queue or active:
+                now = self.clock() - t0
+                while pending and (not realtime or pending[0].arrival <= now):
+                    queue.append(pending.popleft())
+                while queue and len(active) < self.max_active:
+                    req = queue[0]
+                    need = self.estimate(req)
+                    if used + need > self.budget and active:
+                        break
+                    queue.popleft()
+                    pl = make_plan(req, self.precision, self.cfl, self.stream)
+                    nbytes = pl.stats()["device_bytes"]
+                    mass0 = [pl.mass(t) for t in range(req.tracers)]
+                    batch.add(pl)
+                    active[id(pl)] = [pl, req, req.steps, self.clock() - t0, mass0, nbytes]
+                    used += nbytes
+                peak = max(peak, used)
+                if not active:
+                    if pending and realtime:
+                        time.sleep(max(0.0, min(0.01, pending[0].arrival - (self.clock() - t0))))
+                    continue
+                k = min(v[2] for v in active.values())
+                k = max(1, min(k, self.max_steps_per_tick))
+                batch.advance(k, self.stream)
+                steps += k
+                if on_step:
+                    on_step(steps, len(active), used)
+                done = []
+                for key, v in active.items():
+                    v[2] -= k
+                    if v[2] <= 0:
+                        done.append(key)
+                for key in done:
+                    pl, req, _, admitted, mass0, nbytes = active.pop(key)
+                    batch.remove(pl)
+                    errs, dm = finish(pl, req, mass0)  # synchronises the plan's stream
+                    fin = self.clock() - t0
+                    res = Result(req.rid, req.N, req.tracers, req.steps, req.arrival if realtime else 0.0, admitted,
+                                 fin, errs, dm, 6 * req.N * req.N * req.tracers * req.steps)
+                    if self.keep_state:
+                        res.state = [pl.get_tracer(t) for t in range(req.tracers)]
+                    results.append(res)
+                    pl.close()
+                    used -= nbytes
+        finally:
+            for v in active.values():
+                v[0].close()
+            batch.close()
+        wall = self.clock() - t0
+        lat = np.array([r.latency for r in results]) if results else np.zeros(1)
+        cs = sum(r.cell_steps for r in results)
+        summary = {"requests": len(results), "wall_s": wall, "tracer_cell_steps": cs,
+                   "throughput": cs / wall if wall > 0 else 0.0,
+                   "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                   "batch_steps": steps, "peak_bytes": peak, "budget_bytes": self.budget,
+                   "max_mass_change": max((max(r.mass_change) for r in results), default=0.0)}
+        return results, summary

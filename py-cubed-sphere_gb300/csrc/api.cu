@@ -1,6 +1,9 @@
 // C ABI of csadv (declared in include/csadv.h): plan lifecycle and step orchestration.
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -29,7 +32,7 @@ int validate_options(const csadv_options *o, Options &out) {
         return CSADV_ERR_OPTION;
     if (o->precision != 64 && o->precision != 32) return CSADV_ERR_OPTION;
     if (o->engine < CSADV_ENGINE_AUTO || o->engine > CSADV_ENGINE_FUSED) return CSADV_ERR_OPTION;
-    if (o->tile < 0 || o->tile > 4) return CSADV_ERR_OPTION;
+    if (o->tile < 0 || o->tile > 8) return CSADV_ERR_OPTION;
     // discrete_operators.py:49-73: SP-AVLT / SP-L04 need MT-0, SP-PL07 needs MT-PL07
     if ((o->opsplit == SP_PL07) != (o->mt == MT_PL07)) return CSADV_ERR_OPTION_PAIR;
     out.recon = o->recon;
@@ -52,62 +55,52 @@ bool wind_time_dependent(const Options &o) { return wind_is_time_dependent(o.vf)
 
 using namespace csadv;
 
-struct csadv_plan {
-    Options opt;
-    int N = 0, T = 0;
-    double dt = 0.0;
-    DeviceArena mem;
-    Grid grid;
-    Winds w;
-    void *Q = nullptr;  // T fields of `real`
-    Scratch s{};
-    double *partials = nullptr;
-    int npart = 0;
-    double *scal = nullptr;
-    double *stage = nullptr;
-    double *tmp = nullptr;
-    int k = 0;
-    double cfl = 0.0;
-    int device = 0;
-    FusedState f;  // fused engine (f.on) : Q double-buffered in f.Qbuf[cur]
-    int cur = 0;
-    // execution: CUDA graphs of one step, keyed by [kind: 0 time step, 1 time step + wind update][parity]
-    bool graphs = true;
-    cudaStream_t cap = nullptr;
-    cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    int gkernels[2][2] = {{0, 0}, {0, 0}};
-    // second stream and fork/join events of the fused step
-    cudaStream_t side = nullptr;
-    cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
-    // profiling of the main kernel
-    bool prof = false;
-    cudaEvent_t pev[2] = {nullptr, nullptr};
-    csadv_stats stats{};
-    void drop_graphs() {
-        for (auto &row : gexec)
-            for (auto &e : row)
-                if (e) {
-                    cudaGraphExecDestroy(e);
-                    e = nullptr;
-                }
-    }
-    ~csadv_plan() {
-        drop_graphs();
-        if (cap) cudaStreamDestroy(cap);
-        if (side) cudaStreamDestroy(side);
-        for (auto &e : sev)
-            if (e) cudaEventDestroy(e);
-        for (auto &e : pev)
-            if (e) cudaEventDestroy(e);
-    }
-    size_t esize() const { return opt.precision == 64 ? sizeof(double) : sizeof(float); }
-    void *state() const { return f.on ? f.Qbuf[cur] : Q; }
-    void *tracer(int t) const { return (char *)state() + (size_t)t * grid.d.field * esize(); }
-};
+#include "plan.h"
 
 namespace {
 
 cudaStream_t S(void *stream) { return (cudaStream_t)stream; }
+
+// default tile configuration of the fused engine (zero-based csadv_options.tile code):
+// the line-marching kernel, large tiles for large panels
+int default_tile(const Options &o, int N, int T) {
+    const int t = tuned_tile(N, T, o);
+    if (t >= 0) return t;
+    return N >= 116 ? 4 : 7;
+}
+
+// grids shared by the plans of one resolution and device
+std::mutex g_grid_mu;
+std::map<std::pair<int, int>, std::weak_ptr<GridHolder>> g_grids;
+
+int acquire_grid(int N, int device, cudaStream_t st, std::shared_ptr<GridHolder> &out) {
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    const auto key = std::make_pair(device, N);
+    auto it = g_grids.find(key);
+    if (it != g_grids.end()) {
+        out = it->second.lock();
+        if (out) return CSADV_OK;
+    }
+    auto h = std::make_shared<GridHolder>();
+    int rc = build_grid(N, h->mem, h->grid, st);
+    if (rc) return rc;
+    CSADV_CUDA(cudaStreamSynchronize(st));  // plans on other streams may use it next
+    g_grids[key] = h;
+    out = h;
+    return CSADV_OK;
+}
+
+// the staged engine's per-tracer scratch, allocated on first use
+int ensure_scratch(csadv_plan *pl, cudaStream_t st) {
+    if (pl->s.Qx) return CSADV_OK;
+    const long long F = pl->grid.d.field;
+    const size_t es = pl->esize();
+    void **sa[] = {&pl->s.Qx, &pl->s.Qy, &pl->s.qLx, &pl->s.qRx, &pl->s.qLy, &pl->s.qRy, &pl->s.fx, &pl->s.fy, &pl->s.div};
+    for (void **p : sa) *p = pl->mem.alloc<char>(F * es);
+    if (!pl->mem.ok()) return CSADV_ERR_OOM;
+    for (void **p : sa) CSADV_CUDA(cudaMemsetAsync(*p, 0, F * es, st));
+    return CSADV_OK;
+}
 
 template <class real>
 int scalar_halo(csadv_plan *pl, real *Q, cudaStream_t st) {
@@ -117,7 +110,8 @@ int scalar_halo(csadv_plan *pl, real *Q, cudaStream_t st) {
 
 template <class real>
 int time_step(csadv_plan *pl, cudaStream_t st, bool update, int only_tracer) {
-    int rc;
+    int rc = ensure_scratch(pl, st);
+    if (rc) return rc;
     for (int t = 0; t < pl->T; ++t) {
         if (only_tracer >= 0 && t != only_tracer) continue;
         rc = scalar_halo<real>(pl, (real *)pl->tracer(t), st);
@@ -300,6 +294,27 @@ IcParams ic_params(const csadv_plan *pl, const double *ic_param) {
 
 }  // namespace
 
+namespace csadv {
+
+int plan_pre_step(csadv_plan *pl, cudaStream_t st) {
+    int rc = fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
+    if (!rc && wind_time_dependent(pl->opt)) {
+        rc = wind_halo(pl->opt, pl->grid, pl->w, st);
+        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
+    }
+    return rc;
+}
+
+int plan_post_step(csadv_plan *pl, int kind, cudaStream_t st) {
+    return kind == 1 ? do_update_winds(pl, true, 0, 0.0, st) : CSADV_OK;
+}
+
+int plan_select_device(csadv_plan *pl) { return select_device(pl); }
+
+int graph_kernel_nodes(cudaGraph_t g) { return count_kernel_nodes(g); }
+
+}  // namespace csadv
+
 extern "C" {
 
 const char *csadv_version(void) { return "csadv 0.1 (sm_103a)"; }
@@ -335,7 +350,11 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     Options o;
     int rc = validate_options(opt, o);
     if (rc) return rc;
-    if (N < 8 || N > 16384 || ntracers < 1 || ntracers > 64 || !(dt > 0.0)) return CSADV_ERR_ARG;
+    if (N < 8 || N > 16384 || ntracers < 1 || ntracers > 64 || !(dt != 0.0) || dt != dt || dt < -4.0)
+        return CSADV_ERR_ARG;
+    // dt < 0: -dt is the target CFL number; dt follows from the t = 0 winds below
+    const double cfl_target = dt < 0.0 ? -dt : 0.0;
+    if (cfl_target > 0.0) dt = 1.0;
     if (o.engine == CSADV_ENGINE_FUSED && !fused_supported(o)) return CSADV_ERR_UNSUPPORTED;
     const bool fused = o.engine == CSADV_ENGINE_FUSED || (o.engine == CSADV_ENGINE_AUTO && fused_supported(o));
     csadv_plan *pl = new (std::nothrow) csadv_plan();
@@ -351,7 +370,8 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     }
     pl->device = dev;
     cudaStream_t st = S(stream);
-    rc = build_grid(N, pl->mem, pl->grid, st);
+    rc = acquire_grid(N, dev, st, pl->gref);
+    if (!rc) pl->grid = pl->gref->grid;
     if (rc) {
         delete pl;
         return rc;
@@ -360,8 +380,6 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     const long long F = d.field;
     const size_t es = pl->esize();
     pl->Q = pl->mem.alloc<char>((long long)ntracers * F * es);
-    void **sa[] = {&pl->s.Qx, &pl->s.Qy, &pl->s.qLx, &pl->s.qRx, &pl->s.qLy, &pl->s.qRy, &pl->s.fx, &pl->s.fy, &pl->s.div};
-    for (void **p : sa) *p = pl->mem.alloc<char>(F * es);
     pl->npart = staged_partial_count(pl->grid);
     pl->partials = pl->mem.alloc<double>(pl->npart);
     pl->scal = pl->mem.alloc<double>(8);
@@ -371,19 +389,13 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
         delete pl;
         return CSADV_ERR_OOM;
     }
-    if (fused) {
+    // the staged engine's scratch (fused plans allocate it on first use: csadv_divergence)
+    if (!fused) rc = ensure_scratch(pl, st);
+    if (!rc && fused) {
         pl->f.Qbuf[0] = pl->Q;
-        pl->f.tile = o.tile > 0 ? o.tile - 1 : (o.precision == 64 ? 2 : 3);
-        rc = fused_prepare(o, pl->f.tile);
-        if (!rc) rc = fused_alloc(o, pl->grid, ntracers, pl->mem, pl->f, st);
-        if (rc) {
-            delete pl;
-            return rc;
-        }
+        rc = fused_alloc(o, pl->grid, ntracers, pl->mem, pl->f, st);
     }
-    rc = zero(pl->Q, (size_t)ntracers * F * es, st);
-    for (void **p : sa)
-        if (!rc) rc = zero(*p, F * es, st);
+    if (!rc) rc = zero(pl->Q, (size_t)ntracers * F * es, st);
     if (rc) {
         delete pl;
         return rc;
@@ -395,6 +407,18 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     if (!rc) rc = wind_halo(o, pl->grid, pl->w, st);
     if (!rc) rc = copy_d2d(pl->w.u_old, pl->w.u_pu, (size_t)F * pl->w.esize, st);
     if (!rc) rc = copy_d2d(pl->w.v_old, pl->w.v_pv, (size_t)F * pl->w.esize, st);
+    if (!rc && cfl_target > 0.0) {
+        double c1 = 0.0;  // CFL number of dt = 1
+        rc = wind_cfl(o, pl->grid, pl->w, 1.0, pl->tmp, c1, st);
+        if (!rc && !(c1 > 0.0)) rc = CSADV_ERR_ARG;  // no wind: dt undefined
+        if (!rc) {
+            dt = cfl_target / c1;
+            pl->dt = dt;
+            rc = wind_set_dt(pl->w, dt, st);
+        }
+    }
+    if (!rc && fused)
+        rc = fused_set_tile(o, pl->grid, ntracers, dt, pl->f, o.tile > 0 ? o.tile - 1 : default_tile(o, N, ntracers), st);
     if (!rc) rc = wind_average(o, pl->grid, pl->w, dt, st);
     if (!rc) rc = wind_cfl(o, pl->grid, pl->w, dt, pl->tmp, pl->cfl, st);
     if (!rc && fused) rc = fused_prep_winds(o, pl->grid, pl->w, dt, pl->f, st);
@@ -406,8 +430,15 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     return CSADV_OK;
 }
 
+int csadv_get_dt(const csadv_plan *pl, double *dt) {
+    if (!pl || !dt) return CSADV_ERR_ARG;
+    *dt = pl->dt;
+    return CSADV_OK;
+}
+
 int csadv_plan_destroy(csadv_plan *plan) {
     if (!plan) return CSADV_ERR_ARG;
+    batch_forget(plan);
     select_device(plan);
     cudaDeviceSynchronize();
     delete plan;
@@ -557,7 +588,7 @@ int csadv_get_stats(csadv_plan *pl, csadv_stats *out) {
     *out = pl->stats;
     out->engine = pl->f.on ? CSADV_ENGINE_FUSED : CSADV_ENGINE_STAGED;
     out->tile = pl->f.on ? pl->f.tile + 1 : 0;
-    out->device_bytes = pl->mem.bytes();
+    out->device_bytes = pl->mem.bytes() + (pl->gref ? pl->gref->mem.bytes() : 0);
     return CSADV_OK;
 }
 

@@ -22,26 +22,10 @@
 #pragma once
 #include "common.cuh"
 #include "internal.h"
+#include "tiles.h"
 
 namespace csadv {
 
-struct FusedArgs {
-    Dims d;
-    int T;                 // tracers
-    int ntj, ntiles;       // tiles along j, tiles per panel
-    double dt, dx, a2;
-    const void *Qin;       // T fields (real), ghost cells filled
-    void *Qout;            // T fields (real), interior written
-    const double *corr_in; // [T] pending MF-PR correction of Qin (nullptr: none)
-    double *corr_out;      // [T] correction of Qout (MF-PR only)
-    double *partials;      // [T][gridDim.x]
-    unsigned int *counter; // arrival counter (MF-PR)
-    const void *ua, *va;   // departure-point winds (real) at x-/y-edges, 6 planes
-    const uint32_t *upos, *vpos;  // upwind flags: bit j&31 of word [p][i][j>>5] (1: wind >= 0)
-    const void *g_pc, *g_pu, *g_pv;  // metric (real), one plane each
-    int split, mt, mfpr;
-    int wpitch;            // words per row of the flag arrays
-};
 
 template <class real>
 struct RealOps {
@@ -418,9 +402,6 @@ constexpr size_t fused_smem_bytes() {
     return (bytes + 15) / 16 * 16;
 }
 
-// tile shapes selectable per launch (the autotuner times them): {TI, TJ}
-constexpr int FUSED_TILES[][2] = {{16, 58}, {32, 58}, {16, 26}, {32, 26}};
-constexpr int FUSED_NTILE_CFG = 4;
 
 template <class real, int REC, int TI, int TJ>
 static int fused_go(FusedArgs a, cudaStream_t st) {
@@ -457,10 +438,5 @@ int fused_launch(const FusedArgs &a, int recon, int tile, cudaStream_t st) {
     }
 }
 
-// number of CTAs of a launch with tile shape `tile`
-inline int fused_blocks(const Dims &d, int tile) {
-    int TI = FUSED_TILES[tile][0], TJ = FUSED_TILES[tile][1];
-    return NFACE * ((d.N + TI - 1) / TI) * ((d.N + TJ - 1) / TJ);
-}
 
 }  // namespace csadv

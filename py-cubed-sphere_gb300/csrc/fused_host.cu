@@ -1,7 +1,7 @@
 // Host side of the fused engine: buffers, wind preparation, step sequencing, and the
 // lazy MF-PR correction.
-#include "fused.cuh"
 #include "internal.h"
+#include "tiles.h"
 
 namespace csadv {
 
@@ -10,6 +10,23 @@ int fused_supported(const Options &o) { return o.et == ET_DG && o.mf != MF_AF; }
 __global__ void k_plane_to_float(const double *__restrict__ src, float *dst, long long n) {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t < n) dst[t] = (float)src[t];
+}
+
+// dst(j, i) = src(i, j) (transpose) or dst(i, j) = 1 / src(i, j) (recip), or both, for i < rows,
+// j < cols of one plane; entries outside are set to zero
+template <class real>
+__global__ void k_plane_xform(const real *__restrict__ src, real *dst, Dims d, int rows, int cols, int transpose,
+                              int recip) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= d.plane) return;
+    const int a = (int)(t / d.pitch), b = (int)(t % d.pitch);  // destination row, column
+    const int i = transpose ? b : a, j = transpose ? a : b;      // source row, column
+    real v = real(0);
+    if (i < rows && j < cols) {
+        v = src[(long long)i * d.pitch + j];
+        if (recip) v = real(1) / v;
+    }
+    dst[t] = v;
 }
 
 // Q* + g corr on interior cells of every tracer (the true state); blockIdx.y = tracer
@@ -55,6 +72,12 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     for (int b = 0; b < 2; ++b) f.corr[b] = mem.alloc<double>(T);
     int maxb = 0;
     for (int c = 0; c < FUSED_NTILE_CFG; ++c) maxb = maxb > fused_blocks(d, c) ? maxb : fused_blocks(d, c);
+    for (int c = 0; c < SWEEP_NTILE_CFG; ++c) {
+        SweepSolve tmp{};
+        tmp.d = d;
+        sweep_config(tmp, c);
+        maxb = maxb > NFACE * tmp.ntiles ? maxb : NFACE * tmp.ntiles;
+    }
     f.partials = mem.alloc<double>((long long)T * maxb);
     f.counter = mem.alloc<unsigned int>(1);
     f.ua = mem.alloc<char>(d.field * es);
@@ -78,6 +101,37 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
         f.g_pv = gs[2];
     }
     if (!mem.ok()) return CSADV_ERR_OOM;
+    // line-marching kernel data: transposed y-edge winds, flags and metric; 1/g
+    f.vaT = mem.alloc<char>(d.field * es);
+    f.vbT = mem.alloc<uint32_t>(words);
+    void *planes[4];
+    for (int c = 0; c < 4; ++c) planes[c] = mem.alloc<char>(d.plane * es);
+    f.dsolve = mem.alloc<SweepSolve>(2);
+    if (!mem.ok()) return CSADV_ERR_OOM;
+    {
+        const int nb = ceil_div(d.plane, 256);
+        const int n = d.n;
+        if (o.precision == 64) {
+            const double *gpc = (const double *)f.g_pc, *gpv = (const double *)f.g_pv;
+            k_plane_xform<double><<<nb, 256, 0, st>>>(gpc, (double *)planes[0], d, n, n, 1, 0);
+            k_plane_xform<double><<<nb, 256, 0, st>>>(gpv, (double *)planes[1], d, n, n + 1, 1, 0);
+            k_plane_xform<double><<<nb, 256, 0, st>>>(gpc, (double *)planes[2], d, n, n, 0, 1);
+            k_plane_xform<double><<<nb, 256, 0, st>>>(gpc, (double *)planes[3], d, n, n, 1, 1);
+        } else {
+            const float *gpc = (const float *)f.g_pc, *gpv = (const float *)f.g_pv;
+            k_plane_xform<float><<<nb, 256, 0, st>>>(gpc, (float *)planes[0], d, n, n, 1, 0);
+            k_plane_xform<float><<<nb, 256, 0, st>>>(gpv, (float *)planes[1], d, n, n + 1, 1, 0);
+            k_plane_xform<float><<<nb, 256, 0, st>>>(gpc, (float *)planes[2], d, n, n, 0, 1);
+            k_plane_xform<float><<<nb, 256, 0, st>>>(gpc, (float *)planes[3], d, n, n, 1, 1);
+        }
+        CSADV_CUDA(cudaGetLastError());
+    }
+    f.gpcT = planes[0];
+    f.gpvT = planes[1];
+    f.igpc = planes[2];
+    f.igpcT = planes[3];
+    CSADV_CUDA(cudaMemsetAsync(f.vaT, 0, (size_t)d.field * es, st));
+    CSADV_CUDA(cudaMemsetAsync(f.vbT, 0, (size_t)words * sizeof(uint32_t), st));
     CSADV_CUDA(cudaMemsetAsync(f.Qbuf[1], 0, (size_t)T * d.field * es, st));
     for (int b = 0; b < 2; ++b) CSADV_CUDA(cudaMemsetAsync(f.corr[b], 0, T * sizeof(double), st));
     CSADV_CUDA(cudaMemsetAsync(f.counter, 0, sizeof(unsigned int), st));
@@ -86,15 +140,71 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
 }
 
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, cudaStream_t st) {
+    if (f.sweep) {
+        if (o.precision == 64)
+            return wind_avgprep_t<double>(o, g, w, dt, (double *)f.ua, (double *)f.vaT, f.upos, f.vbT, f.wpitch, st);
+        return wind_avgprep_t<float>(o, g, w, dt, (float *)f.ua, (float *)f.vaT, f.upos, f.vbT, f.wpitch, st);
+    }
     if (o.precision == 64)
         return wind_avgprep<double>(o, g, w, dt, (double *)f.ua, (double *)f.va, f.upos, f.vpos, f.wpitch, st);
     return wind_avgprep<float>(o, g, w, dt, (float *)f.ua, (float *)f.va, f.upos, f.vpos, f.wpitch, st);
 }
 
 int fused_prepare(const Options &o, int tile) {
+    if (tile >= FUSED_NTILE_CFG)
+        return o.precision == 64 ? sweep_launch<double>(o.recon, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1)
+                                 : sweep_launch<float>(o.recon, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1);
     FusedArgs a{};
     return o.precision == 64 ? fused_launch<double>(a, o.recon, tile, (cudaStream_t)-1)
                              : fused_launch<float>(a, o.recon, tile, (cudaStream_t)-1);
+}
+
+int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState &f, int tile, cudaStream_t st) {
+    int rc = fused_prepare(o, tile);
+    if (rc) return rc;
+    const bool was = f.sweep;
+    f.tile = tile;
+    f.sweep = tile >= FUSED_NTILE_CFG;
+    if (!f.sweep) return CSADV_OK;
+    f.scfg = tile - FUSED_NTILE_CFG;
+    const bool pr = o.mf == MF_PR;
+    SweepSolve h[2];
+    for (int b = 0; b < 2; ++b) {
+        SweepSolve &s = h[b];
+        s = SweepSolve{};
+        s.d = g.d;
+        s.T = T;
+        sweep_config(s, f.scfg);
+        s.dt = dt;
+        s.dx = g.dx;
+        s.a2 = g.a2;
+        s.Qin = f.Qbuf[b];
+        s.Qout = f.Qbuf[1 - b];
+        s.corr_in = pr ? f.corr[b] : nullptr;
+        s.corr_out = pr ? f.corr[1 - b] : nullptr;
+        s.partials = f.partials;
+        s.counter = f.counter;
+        s.ua = f.ua;
+        s.vaT = f.vaT;
+        s.ub = f.upos;
+        s.vbT = f.vbT;
+        s.gpc = f.g_pc;
+        s.gpcT = f.gpcT;
+        s.igpc = f.igpc;
+        s.igpcT = f.igpcT;
+        s.gpu = f.g_pu;
+        s.gpvT = f.gpvT;
+        s.wpitch = f.wpitch;
+        s.split = o.opsplit;
+        s.mt = o.mt;
+        s.mfpr = pr ? 1 : 0;
+    }
+    f.nitems = NFACE * h[0].ntiles;
+    f.smem = o.precision == 64 ? sweep_smem_bytes<double>(f.scfg) : sweep_smem_bytes<float>(f.scfg);
+    CSADV_CUDA(cudaMemcpyAsync(f.dsolve, h, sizeof(h), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaStreamSynchronize(st));
+    (void)was;
+    return CSADV_OK;
 }
 
 int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
@@ -109,6 +219,15 @@ int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur,
 int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
                  cudaEvent_t ev0, cudaEvent_t ev1) {
     const bool pr = o.mf == MF_PR;
+    if (f.sweep) {
+        if (ev0) CSADV_CUDA(cudaEventRecord(ev0, st));
+        int rc = o.precision == 64 ? sweep_launch<double>(o.recon, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st)
+                                   : sweep_launch<float>(o.recon, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st);
+        if (rc) return rc;
+        if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
+        cur = 1 - cur;
+        return CSADV_OK;
+    }
     FusedArgs a{};
     a.d = g.d;
     a.T = T;

@@ -94,6 +94,8 @@ int staged_update(const Options &o, const Grid &g, double dt, real *Q, const Scr
 int staged_partial_count(const Grid &g);
 
 int wind_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, double dt, cudaStream_t st);
+// the time step of the device clock (set before the first step)
+int wind_set_dt(Winds &w, double dt, cudaStream_t st);
 int wind_initial(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
 int wind_update(const Options &o, const Grid &g, Winds &w, bool tick, long long k, double t, cudaStream_t st);
 int wind_halo(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
@@ -105,9 +107,10 @@ int wind_avgprep(const Options &o, const Grid &g, const Winds &w, double dt, rea
 int wind_cfl(const Options &o, const Grid &g, const Winds &w, double dt, double *dev_tmp, double &cfl, cudaStream_t st);
 
 // ---------------------------------------------------------------- fused engine state
+struct SweepSolve;
 struct FusedState {
     bool on = false;
-    int tile = 1;               // FUSED_TILES index
+    int tile = 1;               // 0-3: k_fused (FUSED_TILES), 4-7: k_sweep (SWEEP_TILES[tile - 4])
     void *Qbuf[2] = {nullptr, nullptr};
     double *corr[2] = {nullptr, nullptr};  // [T] pending MF-PR correction of Qbuf[b]
     double *partials = nullptr; // [T][max blocks]
@@ -116,6 +119,16 @@ struct FusedState {
     uint32_t *upos = nullptr, *vpos = nullptr;  // upwind flags (1 bit per edge)
     int wpitch = 0;             // 32-bit words per row of the flag arrays
     const void *g_pc = nullptr, *g_pu = nullptr, *g_pv = nullptr;  // metric in the state's precision
+    // line-marching kernel (k_sweep): y-edge winds/flags and metric planes transposed,
+    // 1/g, and one launch descriptor per buffer parity (device memory)
+    bool sweep = false;
+    int scfg = 0;               // SWEEP_TILES index
+    void *vaT = nullptr;
+    uint32_t *vbT = nullptr;
+    const void *gpcT = nullptr, *gpvT = nullptr, *igpc = nullptr, *igpcT = nullptr;
+    SweepSolve *dsolve = nullptr;  // [2]
+    int nitems = 0;             // work items of one sweep launch (6 x tiles)
+    size_t smem = 0;
 };
 
 int fused_supported(const Options &o);
@@ -128,6 +141,15 @@ int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &
                  cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 // set the dynamic shared-memory limit of the kernel a plan will launch (outside capture)
 int fused_prepare(const Options &o, int tile);
+// select the tile configuration of the fused engine (tile code as in csadv_options.tile,
+// zero-based); rewrites the sweep descriptors.  Outside stream capture.
+int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState &f, int tile, cudaStream_t st);
+template <class real>
+int sweep_launch(int recon, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
+                 cudaStream_t st);
+template <class real>
+int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, real *ua, real *vaT, uint32_t *ub,
+                   uint32_t *vbT, int wpitch, cudaStream_t st);
 // ghost cells of Qbuf[cur] <- those of Qbuf[1-cur] (the halo the last step used)
 int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
 // apply and clear the pending MF-PR correction of Qbuf[cur]

@@ -1,0 +1,460 @@
+// Line-marching step kernel of the fused engine (k_sweep).
+//
+// Same arithmetic as k_fused (the whole dimension-split divergence and the Q update of one
+// step, all tracers), organised so that each quantity of the PPM sweeps is computed once
+// per cell instead of once per edge:
+//
+//   * a thread owns a segment of one grid line through the tile and marches along it,
+//     keeping the 5-cell window, the slope of the current cell and the edge value at its
+//     left edge in registers.  A cell's slope and each edge value are computed once and
+//     shared by the two cells (reconstruction_1d.py:64-192 computes them the same way,
+//     as edge arrays); the limiter runs once per cell, and the upwind flux through an
+//     edge selects the parabola of the cell on the upwind side (flux.py:46-66).
+//   * x-lines (fixed column, marching rows) read consecutive columns across a warp; y-lines
+//     (fixed row, marching columns) read consecutive rows across a warp, so their global
+//     data (y-edge winds and flags, metric) is stored transposed (row j, column i).  Shared
+//     memory rows have an odd pitch, so both directions are free of bank conflicts.
+//
+// Phases per tracer (one CTA = one tile of one panel of one solve):
+//   P0  Q on the tile + 3 halo cells -> shared (pending MF-PR correction added on load)
+//   P1  x-lines over the tile columns +-3: first-pass x fluxes -> split field Qx;
+//       y-lines over the tile rows +-3:    first-pass y fluxes -> split field Qy
+//       (discrete_operators.py:49-73)
+//   P2  y-lines of Qx over the tile rows: second-pass y-flux differences -> shared
+//   P3  x-lines of Qy over the tile columns: second-pass x fluxes; div and Q update,
+//       written to global memory (coalesced), MF-PR block partial (discrete_operators.py:80-101)
+//
+// Work comes from a table of (solve, item) pairs; item = panel * tiles + tile.  One launch
+// can therefore advance many solves of different sizes (each with its own descriptor), and
+// a persistent grid may loop over the table.  The MF-PR sums use a fixed order that depends
+// only on the solve and its tile shape, so a solve gives the same bits alone or in a batch.
+#pragma once
+#include "fused.cuh"
+
+namespace csadv {
+
+
+
+template <class real>
+__device__ __forceinline__ real csign(real a, real b) { return copysign(a, b); }
+template <>
+__device__ __forceinline__ float csign<float>(float a, float b) { return copysignf(a, b); }
+
+// --------------------------------------------------------------------------- reconstructions
+// CW84 limited slope of the cell q0 between qm and qp (reconstruction_1d.py:64-100);
+// min(...) * sign(d0) written as copysign: equal for every finite input
+template <class real>
+__device__ __forceinline__ real cw84_slope(real qm, real q0, real qp) {
+    using O = RealOps<real>;
+    const real d0 = real(0.5) * (qp - qm);
+    const real d1 = real(2.0) * (qp - q0);
+    const real d2 = real(2.0) * (q0 - qm);
+    const real s = csign(O::fmn(O::fmn(O::ab(d0), O::ab(d1)), O::ab(d2)), d0);
+    return ((qp - q0) * (q0 - qm) > real(0)) ? s : real(0);
+}
+// value at the edge between cells a and b from their values and slopes
+template <class real>
+__device__ __forceinline__ real cw84_edge(real qa, real qb, real sa, real sb) {
+    return real(0.5) * (qb + qa) - Div<real>::by(sb - sa, real(6.0), real(1.0 / 6.0));
+}
+// CW84 monotonicity limiter of the parabola (L, R) of a cell with mean qc (reconstruction_1d.py:102-153)
+template <class real>
+__device__ __forceinline__ void cw84_limit(real qc, real &L, real &R) {
+    using O = RealOps<real>;
+    const real dq = R - L;
+    const real q6 = real(6) * qc - real(3) * (R + L);
+    const bool flat = (R - qc) * (qc - L) <= real(0);
+    R = flat ? qc : R;
+    L = flat ? qc : L;
+    const bool over = O::ab(dq) < O::ab(q6);
+    const real DL = R - L;
+    const real mid = qc - real(0.5) * (R + L);
+    const real d2 = Div<real>::by(DL * DL, real(6.0), real(1.0 / 6.0));
+    const real prod = DL * mid;
+    const bool ml = over && prod > d2;
+    const bool mr = over && !ml && -d2 > prod;
+    const real Ln = real(3.0) * qc - real(2.0) * R;
+    const real Rn = real(3.0) * qc - real(2.0) * L;
+    L = ml ? Ln : L;
+    R = mr ? Rn : R;
+}
+// L04 monotone slope (reconstruction_1d.py:155-172)
+template <class real>
+__device__ __forceinline__ real l04_mono(real qm, real q0, real qp) {
+    using O = RealOps<real>;
+    const real dq = real(0.25) * (qp - qm);
+    const real dmin = O::fmx(O::fmx(qm, q0), qp) - q0;
+    const real dmax = q0 - O::fmn(O::fmn(qm, q0), qp);
+    return csign(O::fmn(O::fmn(O::ab(dq), dmin), dmax), dq);
+}
+template <class real>
+__device__ __forceinline__ real l04_edge(real qa, real qb, real ma, real mb) {
+    return real(0.5) * (qb + qa) - Div<real>::by(mb - ma, real(3.0), real(1.0 / 3.0));
+}
+// L04 limiter (reconstruction_1d.py:174-192)
+template <class real>
+__device__ __forceinline__ void l04_limit(real q0, real mono, real &L, real &R) {
+    using O = RealOps<real>;
+    const real m2 = real(2.0) * mono;
+    L = q0 - csign(O::fmn(real(2.0) * O::ab(mono), O::ab(L - q0)), m2);
+    R = q0 + csign(O::fmn(real(2.0) * O::ab(mono), O::ab(R - q0)), m2);
+}
+// PPM-0 4-point edge value between cells a and b (reconstruction_1d.py:33-44)
+template <class real>
+__device__ __forceinline__ real ppm0_edge(real qam, real qa, real qb, real qbp) {
+    return real(7.0 / 12.0) * (qb + qa) - Div<real>::by(qbp + qam, real(12.0), real(1.0 / 12.0));
+}
+
+// Marching reconstruction: init() with the window of the first cell, then cell() once per
+// cell (window w[0..4] = q[m-2..m+2]) gives the cell's (L, R) and advances.
+template <class real, int REC>
+struct March {
+    real s, E;  // slope of the current cell; edge value at its left edge
+    __device__ __forceinline__ void init(const real w[5]) {
+        if (REC == REC_CW84) {
+            const real sp = cw84_slope(w[0], w[1], w[2]);
+            s = cw84_slope(w[1], w[2], w[3]);
+            E = cw84_edge(w[1], w[2], sp, s);
+        } else if (REC == REC_L04) {
+            const real sp = l04_mono(w[0], w[1], w[2]);
+            s = l04_mono(w[1], w[2], w[3]);
+            E = l04_edge(w[1], w[2], sp, s);
+        } else if (REC == REC_PPM0) {
+            E = ppm0_edge(w[0], w[1], w[2], w[3]);
+        }
+    }
+    __device__ __forceinline__ void cell(const real w[5], real &L, real &R) {
+        if (REC == REC_CW84) {
+            const real sn = cw84_slope(w[2], w[3], w[4]);
+            const real En = cw84_edge(w[2], w[3], s, sn);
+            L = E;
+            R = En;
+            cw84_limit(w[2], L, R);
+            s = sn;
+            E = En;
+        } else if (REC == REC_L04) {
+            const real sn = l04_mono(w[2], w[3], w[4]);
+            const real En = l04_edge(w[2], w[3], s, sn);
+            L = E;
+            R = En;
+            l04_limit(w[2], s, L, R);
+            s = sn;
+            E = En;
+        } else if (REC == REC_PPM0) {
+            const real En = ppm0_edge(w[1], w[2], w[3], w[4]);
+            L = E;
+            R = En;
+            E = En;
+        } else {  // PL07 hybrid 5-point values (reconstruction_1d.py:46-62)
+            const real a1 = real(2.0 / 60.0), a2 = real(-13.0 / 60.0), a3 = real(47.0 / 60.0),
+                       a4 = real(27.0 / 60.0), a5 = real(-3.0 / 60.0);
+            R = a1 * w[0] + a2 * w[1] + a3 * w[2] + a4 * w[3] + a5 * w[4];
+            L = a5 * w[0] + a4 * w[1] + a3 * w[2] + a2 * w[3] + a1 * w[4];
+        }
+    }
+};
+
+// One grid line through a tile.  Cell m (tile-local, 0 = first interior cell of the tile
+// along the line) is at s[m * ss] in shared memory; the edge m (left edge of cell m) and the
+// cell m data in global memory are at [m * P]; the flag of edge m is bit `bit` of b[m * wp].
+template <class real>
+struct Line {
+    const real *s;
+    int ss;
+    const real *u, *gE, *gC, *igC;
+    const uint32_t *b;
+    int bit;
+};
+
+enum { MARCH_SPLIT = 0, MARCH_DIFF = 1, MARCH_UPDATE = 2 };
+
+#ifndef CSADV_SWEEP_UNROLL
+#define CSADV_SWEEP_UNROLL 1
+#endif
+constexpr int SWEEP_UNROLL = CSADV_SWEEP_UNROLL;  // march loop unrolling
+
+// March over cells [ma - 1, mb]: fluxes through edges [ma, mb], outputs for cells [ma, mb).
+//   MARCH_SPLIT : split field of the first pass -> out[k * os]
+//   MARCH_DIFF  : flux difference F(k+1) - F(k) -> out[k * os]
+//   MARCH_UPDATE: Q(k) - dt div(k) -> qout[k * P], with the y-flux differences dY[k * os]
+//                 and Q(k) at Qc[k * qs]; returns the line's sum of div * g (MF-PR)
+// Every load of iteration m + 1 is issued during iteration m, so the global (L1/L2)
+// latency of the line's winds, flags and metric overlaps the arithmetic.
+template <class real, int REC, int MODE>
+__device__ __forceinline__ real march(const Line<real> &ln, int P, int wp, int ma, int mb, real dtdx, real irdx,
+                                      int mt, int split, bool mfpr, real *out, int os, const real *dY,
+                                      const real *Qc, int qs, real *qout) {
+    real w[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) w[k] = ln.s[(ma - 3 + k) * ln.ss];
+    March<real, REC> rc;
+    rc.init(w);
+    real gl = ln.gE[(ma - 1) * P];  // metric at the left edge of the current cell
+    // values of the next iteration, loaded one iteration ahead
+    real ngr = ln.gE[ma * P], ngc = ln.gC[(ma - 1) * P], nu = real(0), nig = real(0), nw4 = real(0);
+    uint32_t nb = 0u;
+    real pL = real(0), pR = real(0), pQ = real(0);  // previous cell's parabola (metric-weighted for MT-0)
+    real Fp = real(0), cp = real(0), gcp = real(0), acc = real(0);
+#pragma unroll SWEEP_UNROLL
+    for (int m = ma - 1; m <= mb; ++m) {
+        const real gr = ngr, gcm = ngc, u = nu, ig = nig;
+        const uint32_t bw = nb;
+        if (m < mb) {
+            nw4 = ln.s[(m + 3) * ln.ss];
+            ngr = ln.gE[(m + 2) * P];
+            ngc = ln.gC[(m + 1) * P];
+            nu = ln.u[(m + 1) * P];
+            nb = ln.b[(m + 1) * wp];
+            if (MODE != MARCH_DIFF) nig = ln.igC[m * P];
+        }
+        real L, R;
+        rc.cell(w, L, R);
+        real cL = L, cR = R, cQ = w[2];
+        if (mt == MT_0) {  // flux.py:28-31
+            cL = L * gl;
+            cR = R * gr;
+            cQ = w[2] * gcm;
+        }
+        if (m >= ma) {
+            // upwind PPM flux through edge m (flux.py:20-128): cell m-1 when the wind is >= 0
+            const bool up = (bw >> ln.bit) & 1u;
+            const real c = u * dtdx;
+            const real eL = up ? pL : cL, eR = up ? pR : cR, eQ = up ? pQ : cQ;
+            const real dq = eR - eL;
+            const real q6 = real(6) * eQ - real(3) * (eR + eL);
+            const real e = up ? eR : eL;
+            const real hc = c * real(0.5);
+            const real t1 = up ? hc * (q6 - dq) : -(hc * (q6 + dq));
+            real F = e + t1 - Div<real>::by(q6 * c * c, real(3.0), real(1.0 / 3.0));
+            F = F * u;
+            if (mt == MT_PL07) F = F * gl;
+            const real cm = gl * c;  // g u dt/dx at edge m (SP-L04, SP-PL07)
+            if (m > ma) {
+                const int k = m - 1;
+                if (MODE == MARCH_SPLIT) {
+                    const real q = w[1];
+                    const real dF = -(F - Fp) * dtdx;
+                    real o;
+                    if (split == SP_AVLT)
+                        o = q + real(0.5) * dF * ig;
+                    else if (split == SP_L04)
+                        o = (q * gcp + real(0.5) * dF + real(0.5) * (cm - cp) * q) * ig;
+                    else
+                        o = real(0.5) * (q + (q + dF) / (real(1.0) - (cm - cp)));
+                    out[k * os] = o;
+                } else if (MODE == MARCH_DIFF) {
+                    out[k * os] = F - Fp;
+                } else {
+                    const real sdiv = (F - Fp) + dY[k * os];
+                    qout[(long long)k * P] = Qc[k * qs] - sdiv * dtdx * ig;
+                    if (mfpr) acc += sdiv * ig * irdx * gcp;
+                }
+            }
+            Fp = F;
+            cp = cm;
+        }
+        pL = cL;
+        pR = cR;
+        pQ = cQ;
+        gl = gr;
+        gcp = gcm;
+        w[0] = w[1];
+        w[1] = w[2];
+        w[2] = w[3];
+        w[3] = w[4];
+        w[4] = nw4;
+    }
+    return acc;
+}
+
+// CTAs per SM the register allocation is sized for: FP32 is latency-bound and gains from a
+// second resident CTA; FP64 is bound by the FP64 pipe and keeps the registers
+#ifndef CSADV_SWEEP_MINB
+template <class real> struct SweepMinBlocks { static constexpr int value = 2; };
+template <> struct SweepMinBlocks<double> { static constexpr int value = 1; };
+#else
+template <class real> struct SweepMinBlocks { static constexpr int value = CSADV_SWEEP_MINB; };
+#endif
+
+template <class real, int REC>
+__global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_sweep(const SweepSolve *__restrict__ solves,
+                                                         const int2 *__restrict__ work, int nwork) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    real *sm = (real *)smem_raw;
+    __shared__ double red[SWEEP_THREADS];
+    __shared__ int last;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NWARP = SWEEP_THREADS / 32;
+
+    for (int wk = blockIdx.x; wk < nwork; wk += gridDim.x) {
+        const int2 it = work ? work[wk] : make_int2(0, wk);
+        const SweepSolve &S = solves[it.x];
+        const Dims d = S.d;
+        const int ti = S.ti, tj = S.tj, ntiles = S.ntiles, nitems = NFACE * ntiles;
+        const int tile = it.y % ntiles, p = it.y / ntiles;
+        const int I0 = d.i0 + (tile / S.ntj) * ti, J0 = d.i0 + (tile % S.ntj) * tj;
+        const int ni = min(ti, d.iend - I0), nj = min(tj, d.iend - J0);
+        const SweepSmem L = sweep_smem(ti, tj);
+        real *sQ = sm, *sQx = sm + L.oQx, *sQy = sm + L.oQy, *sDy = sm + L.oDy;
+        const int P = d.pitch, wp = S.wpitch;
+        const long long pofs = (long long)p * d.plane;
+        const long long bofs = (long long)p * (d.n + 1) * wp;
+        const real dtdx = (real)(S.dt / S.dx);
+        const real irdx = real(1) / (real)S.dx;
+        const int mt = S.mt, split = S.split;
+        const bool mfpr = S.mfpr != 0;
+        const real *ua = (const real *)S.ua + pofs, *vaT = (const real *)S.vaT + pofs;
+        const real *gpc = (const real *)S.gpc, *gpcT = (const real *)S.gpcT;
+        const real *igpc = (const real *)S.igpc, *igpcT = (const real *)S.igpcT;
+        const real *gpu = (const real *)S.gpu, *gpvT = (const real *)S.gpvT;
+        const uint32_t *ub = S.ub + bofs, *vbT = S.vbT + bofs;
+
+        for (int tr = 0; tr < S.T; ++tr) {
+            const real *Qin = (const real *)S.Qin + (long long)tr * d.field + pofs;
+            real *Qout = (real *)S.Qout + (long long)tr * d.field + pofs;
+            const bool hc = S.corr_in != nullptr;
+            const real corr = hc ? (real)S.corr_in[tr] : real(0);
+            // P0: Q on the tile + halo (+ pending mass-fixer correction on interior cells)
+            for (int r = warp; r < ni + 6; r += NWARP) {
+                const int i = I0 - 3 + r;
+                const bool irow = i >= d.i0 && i < d.iend;
+                for (int c = lane; c < nj + 6; c += 32) {
+                    const int j = J0 - 3 + c;
+                    real v = Qin[(long long)i * P + j];
+                    if (hc && irow && j >= d.i0 && j < d.iend) v = v + gpc[(long long)i * P + j] * corr;
+                    sQ[r * L.QJp + c] = v;
+                }
+            }
+            __syncthreads();
+            // P1: first pass.  x-lines: columns c in [-3, nj+3), cells [0, ni) -> Qx;
+            //                  y-lines: rows r in [-3, ni+3), cells [0, nj) -> Qy
+            {
+                const int LX = round32(nj + 6), LY = round32(ni + 6);
+                const int jx = S.s1x * LX, jy = S.s1y * LY;
+                for (int job = tid; job < jx + jy; job += SWEEP_THREADS) {
+                    if (job < jx) {
+                        const int seg = job / LX, c = job - seg * LX - 3;
+                        const int ma = ni * seg / S.s1x, mb = ni * (seg + 1) / S.s1x;
+                        if (c >= nj + 3 || ma >= mb) continue;
+                        const long long g0 = (long long)I0 * P + J0 + c;
+                        Line<real> ln{sQ + 3 * L.QJp + c + 3, L.QJp, ua + g0, gpu + g0, gpc + g0, igpc + g0,
+                                      ub + (long long)I0 * wp + ((J0 + c) >> 5), (J0 + c) & 31};
+                        march<real, REC, MARCH_SPLIT>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, false,
+                                                      sQx + c + 3, L.QJp, nullptr, nullptr, 0, nullptr);
+                    } else {
+                        const int jj = job - jx;
+                        const int seg = jj / LY, r = jj - seg * LY - 3;
+                        const int ma = nj * seg / S.s1y, mb = nj * (seg + 1) / S.s1y;
+                        if (r >= ni + 3 || ma >= mb) continue;
+                        const long long g0 = (long long)J0 * P + I0 + r;
+                        Line<real> ln{sQ + (r + 3) * L.QJp + 3, 1, vaT + g0, gpvT + g0, gpcT + g0, igpcT + g0,
+                                      vbT + (long long)J0 * wp + ((I0 + r) >> 5), (I0 + r) & 31};
+                        march<real, REC, MARCH_SPLIT>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, false,
+                                                      sQy + (r + 3) * L.TJp, 1, nullptr, nullptr, 0, nullptr);
+                    }
+                }
+            }
+            __syncthreads();
+            // P2: y-lines of Qx over rows [0, ni): y-flux differences -> sDy
+            {
+                const int LY = round32(ni);
+                const int jy = S.s2y * LY;
+                for (int job = tid; job < jy; job += SWEEP_THREADS) {
+                    const int seg = job / LY, r = job - seg * LY;
+                    const int ma = nj * seg / S.s2y, mb = nj * (seg + 1) / S.s2y;
+                    if (r >= ni || ma >= mb) continue;
+                    const long long g0 = (long long)J0 * P + I0 + r;
+                    Line<real> ln{sQx + r * L.QJp + 3, 1, vaT + g0, gpvT + g0, gpcT + g0, igpcT + g0,
+                                  vbT + (long long)J0 * wp + ((I0 + r) >> 5), (I0 + r) & 31};
+                    march<real, REC, MARCH_DIFF>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, false, sDy + r * L.TJp, 1,
+                                                 nullptr, nullptr, 0, nullptr);
+                }
+            }
+            __syncthreads();
+            // P3: x-lines of Qy over columns [0, nj): x fluxes, div, update, MF-PR partial
+            real acc = real(0);
+            {
+                const int LX = round32(nj);
+                const int jx = S.s2x * LX;
+                for (int job = tid; job < jx; job += SWEEP_THREADS) {
+                    const int seg = job / LX, c = job - seg * LX;
+                    const int ma = ni * seg / S.s2x, mb = ni * (seg + 1) / S.s2x;
+                    if (c >= nj || ma >= mb) continue;
+                    const long long g0 = (long long)I0 * P + J0 + c;
+                    Line<real> ln{sQy + 3 * L.TJp + c, L.TJp, ua + g0, gpu + g0, gpc + g0, igpc + g0,
+                                  ub + (long long)I0 * wp + ((J0 + c) >> 5), (J0 + c) & 31};
+                    acc += march<real, REC, MARCH_UPDATE>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, mfpr, nullptr,
+                                                          L.TJp, sDy + c, sQ + 3 * L.QJp + c + 3, L.QJp,
+                                                          Qout + g0);
+                }
+            }
+            if (mfpr) {  // FP64 across threads, in a fixed order
+                double dacc = (double)acc;
+                for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
+                if (lane == 0) red[warp] = dacc;
+                __syncthreads();
+                if (tid == 0) {
+                    double s = 0.0;
+                    for (int w = 0; w < NWARP; ++w) s += red[w];
+                    S.partials[(long long)tr * nitems + it.y] = s;
+                }
+            }
+            __syncthreads();
+        }
+        if (mfpr) {
+            // the last item of the solve to finish sums its partials: corr = dt m0 / a2
+            if (tid == 0) {
+                __threadfence();
+                const unsigned int prev = atomicAdd(S.counter, 1u);
+                last = prev == (unsigned int)nitems - 1u;
+            }
+            __syncthreads();
+            if (last) {
+                __threadfence();
+                for (int tr = 0; tr < S.T; ++tr) {
+                    double a = 0.0;
+                    const volatile double *pp = S.partials + (long long)tr * nitems;
+                    for (int b = tid; b < nitems; b += SWEEP_THREADS) a += pp[b];
+                    red[tid] = a;
+                    __syncthreads();
+                    for (int s = SWEEP_THREADS / 2; s > 0; s >>= 1) {
+                        if (tid < s) red[tid] += red[tid + s];
+                        __syncthreads();
+                    }
+                    if (tid == 0) S.corr_out[tr] = S.dt * red[0] / S.a2;
+                    __syncthreads();
+                }
+                if (tid == 0) *S.counter = 0u;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+
+
+template <class real, int REC>
+int sweep_go(const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem, cudaStream_t st) {
+    if (st == (cudaStream_t)-1) {  // prepare only: allow the largest layout
+        size_t mx = 0;
+        for (int c = 0; c < SWEEP_NTILE_CFG; ++c) mx = mx > sweep_smem_bytes<real>(c) ? mx : sweep_smem_bytes<real>(c);
+        CSADV_CUDA(cudaFuncSetAttribute(k_sweep<real, REC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+        return CSADV_OK;
+    }
+    k_sweep<real, REC><<<grid, SWEEP_THREADS, smem, st>>>(dsolves, work, nwork);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+template <class real>
+int sweep_launch(int recon, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
+                 cudaStream_t st) {
+    switch (recon) {
+        case REC_PPM0: return sweep_go<real, REC_PPM0>(dsolves, work, nwork, grid, smem, st);
+        case REC_CW84: return sweep_go<real, REC_CW84>(dsolves, work, nwork, grid, smem, st);
+        case REC_PL07: return sweep_go<real, REC_PL07>(dsolves, work, nwork, grid, smem, st);
+        default: return sweep_go<real, REC_L04>(dsolves, work, nwork, grid, smem, st);
+    }
+}
+
+}  // namespace csadv

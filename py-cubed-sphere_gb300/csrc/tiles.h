@@ -1,0 +1,114 @@
+// Launch descriptors and tile geometry of the fused engine's step kernels, shared by the
+// host code and the kernels.  No kernels here: the kernel templates live in fused.cuh and
+// sweep.cuh and are instantiated only in fused_f32/f64.cu and sweep_f32/f64.cu (one device
+// copy of each kernel in the library).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace csadv {
+
+// ---------------------------------------------------------------- per-edge tile kernel (k_fused)
+struct FusedArgs {
+    Dims d;
+    int T;                 // tracers
+    int ntj, ntiles;       // tiles along j, tiles per panel
+    double dt, dx, a2;
+    const void *Qin;       // T fields (real), ghost cells filled
+    void *Qout;            // T fields (real), interior written
+    const double *corr_in; // [T] pending MF-PR correction of Qin (nullptr: none)
+    double *corr_out;      // [T] correction of Qout (MF-PR only)
+    double *partials;      // [T][gridDim.x]
+    unsigned int *counter; // arrival counter (MF-PR)
+    const void *ua, *va;   // departure-point winds (real) at x-/y-edges, 6 planes
+    const uint32_t *upos, *vpos;  // upwind flags: bit j&31 of word [p][i][j>>5] (1: wind >= 0)
+    const void *g_pc, *g_pu, *g_pv;  // metric (real), one plane each
+    int split, mt, mfpr;
+    int wpitch;            // words per row of the flag arrays
+};
+
+// tile shapes selectable per launch (the autotuner times them): {TI, TJ}
+constexpr int FUSED_TILES[][2] = {{16, 58}, {32, 58}, {16, 26}, {32, 26}};
+constexpr int FUSED_NTILE_CFG = 4;
+
+// number of CTAs of a launch with tile shape `tile`
+inline int fused_blocks(const Dims &d, int tile) {
+    int TI = FUSED_TILES[tile][0], TJ = FUSED_TILES[tile][1];
+    return NFACE * ((d.N + TI - 1) / TI) * ((d.N + TJ - 1) / TJ);
+}
+
+// ---------------------------------------------------------------- line-marching kernel (k_sweep)
+// One solve's part of a sweep launch (device memory; one per solve and buffer parity).
+struct SweepSolve {
+    Dims d;
+    int T;                  // tracers
+    int ti, tj;             // tile shape (interior cells); ti + 6 <= 64, tj + 6 <= 64
+    int ntj, ntiles;        // tiles along j; tiles per panel (items = 6 ntiles)
+    int s1x, s1y, s2y, s2x; // segments per line in P1 (x, y), P2, P3
+    double dt, dx, a2;
+    const void *Qin;        // T fields, ghost cells filled
+    void *Qout;             // T fields, interior written
+    const double *corr_in;  // [T] pending MF-PR correction of Qin, or null
+    double *corr_out;       // [T] correction of Qout (MF-PR)
+    double *partials;       // [T][6 ntiles]
+    unsigned int *counter;  // arrival counter (MF-PR)
+    const void *ua, *vaT;   // departure-point winds: x-edges natural, y-edges transposed
+    const uint32_t *ub, *vbT;  // upwind flags (1: wind >= 0), the same two layouts, 32 per word
+    const void *gpc, *gpcT, *igpc, *igpcT, *gpu, *gpvT;  // metric planes in the state's precision
+    int wpitch;             // words per row of the flag arrays
+    int split, mt, mfpr;
+};
+
+constexpr int SWEEP_THREADS = 256;
+// tile shapes of the sweep kernel: {ti, tj} (ti + 6 and tj + 6 fill whole warps)
+constexpr int SWEEP_TILES[][2] = {{58, 58}, {58, 26}, {26, 58}, {26, 26}};
+constexpr int SWEEP_NTILE_CFG = 4;
+
+__host__ __device__ __forceinline__ int odd_up(int x) { return x | 1; }
+__host__ __device__ __forceinline__ int round32(int x) { return (x + 31) & ~31; }
+
+// shared-memory layout for tile shape (ti, tj), in elements
+struct SweepSmem {
+    int QJp, TJp;           // row pitches (odd): Q/Qx rows hold tj+6 cells, Qy/dY rows tj cells
+    int oQx, oQy, oDy, total;
+};
+__host__ __device__ __forceinline__ SweepSmem sweep_smem(int ti, int tj) {
+    SweepSmem s;
+    s.QJp = odd_up(tj + 6);
+    s.TJp = odd_up(tj);
+    s.oQx = (ti + 6) * s.QJp;
+    s.oQy = s.oQx + ti * s.QJp;
+    s.oDy = s.oQy + (ti + 6) * s.TJp;
+    s.total = s.oDy + ti * s.TJp;
+    return s;
+}
+
+// tile configuration of a solve: shape and segments per line (about 256 threads per phase,
+// segments of at least ~10 cells)
+inline void sweep_config(SweepSolve &s, int cfg) {
+    s.ti = SWEEP_TILES[cfg][0];
+    s.tj = SWEEP_TILES[cfg][1];
+    const int N = s.d.N;
+    const int ti = s.ti < N ? s.ti : N, tj = s.tj < N ? s.tj : N;
+    auto segs = [](int threads_per_seg, int len) {
+        int k = SWEEP_THREADS / (threads_per_seg > 0 ? threads_per_seg : 1);
+        int kmax = len / 10 > 1 ? len / 10 : 1;
+        if (k > kmax) k = kmax;
+        return k > 0 ? k : 1;
+    };
+    s.s1x = segs(round32(tj + 6) + round32(ti + 6), ti);
+    s.s1y = segs(round32(tj + 6) + round32(ti + 6), tj);
+    s.s2y = segs(round32(ti), tj);
+    s.s2x = segs(round32(tj), ti);
+    s.ntj = (N + s.tj - 1) / s.tj;
+    s.ntiles = ((N + s.ti - 1) / s.ti) * s.ntj;
+}
+
+template <class real>
+inline size_t sweep_smem_bytes(int cfg) {
+    return (size_t)sweep_smem(SWEEP_TILES[cfg][0], SWEEP_TILES[cfg][1]).total * sizeof(real);
+}
+
+}  // namespace csadv

@@ -14,8 +14,10 @@
 //
 // Compiled without FMA contraction so the arithmetic order of the reference is kept.
 #include <cmath>
+#include <cstddef>
 
 #include "cases.cuh"
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -367,18 +369,87 @@ __global__ void k_wind_avgprep(Dims d, const W *__restrict__ U, const W *__restr
     }
 }
 
-// max over x-edges [i0, iend] x all columns of u*dt/dx (signed), same for y; one block
+// As k_wind_avgprep, for the line-marching kernel: x-edge winds and flags in the natural
+// layout, y-edge winds and flags transposed (row j, column i) through a shared 32 x 32 tile,
+// so that both stores stay coalesced.  Block (32, 8) covers rows i in [32 by, 32 by + 32) and
+// columns j in [32 bx, 32 bx + 32) of one panel plane.
+template <class W>
+__global__ void k_wind_avgprep_t(Dims d, const W *__restrict__ U, const W *__restrict__ Uo, const W *__restrict__ V,
+                                 const W *__restrict__ Vo, W *ua, W *vaT, uint32_t *ubits, uint32_t *vbitsT,
+                                 int wpitch, int rk2, W dto2, W dx) {
+    __shared__ W tv[32][33];
+    __shared__ unsigned char tf[32][33];
+    const int p = blockIdx.z, jb = blockIdx.x * 32, ib = blockIdx.y * 32;
+    const int lane = threadIdx.x, wy = threadIdx.y;
+    for (int k = 0; k < 4; ++k) {
+        const int r = wy + 8 * k, i = ib + r, j = jb + lane;
+        const bool ok = i <= d.n && j < d.pitch;
+        W u = W(0), v = W(0), av = W(0);
+        if (ok) {
+            const long long t = at(d, p, i, j);
+            u = U[t];
+            v = V[t];
+            W au = u;
+            av = v;
+            if (rk2) {
+                au = (j < d.n && i >= d.i0 && i <= d.iend) ? rk2_average(U, Uo, d, p, i, j, 0, dto2, dx) : W(0);
+                av = (i < d.n && j >= d.i0 && j <= d.iend) ? rk2_average(V, Vo, d, p, i, j, 1, dto2, dx) : W(0);
+            }
+            ua[t] = au;
+        }
+        const unsigned bu = __ballot_sync(0xffffffffu, ok && u >= W(0));
+        if (ok && lane == 0) ubits[((long long)p * (d.n + 1) + i) * wpitch + (j >> 5)] = bu;
+        tv[r][lane] = av;
+        tf[r][lane] = (ok && v >= W(0)) ? 1 : 0;
+    }
+    __syncthreads();
+    for (int k = 0; k < 4; ++k) {
+        const int c = wy + 8 * k, j = jb + c, i = ib + lane;
+        const bool ok = j <= d.n && i < d.pitch;
+        if (ok) vaT[at(d, p, j, i)] = tv[lane][c];
+        const unsigned bv = __ballot_sync(0xffffffffu, ok && tf[lane][c]);
+        if (ok && lane == 0) vbitsT[((long long)p * (d.n + 1) + j) * wpitch + (i >> 5)] = bv;
+    }
+}
+
+// max over x-edges [i0, iend] x all columns of u*dt/dx (signed), same for y
+// (advection_vars.py:89-98): per-block maxima, then one block combines them (max is exact,
+// so the result does not depend on the split)
 template <class W>
 __global__ void k_wind_cfl(Dims d, const W *__restrict__ U, const W *__restrict__ V, double dt, double dx,
                            double *out) {
-    __shared__ double rx[512], ry[512];
+    __shared__ double rx[256], ry[256];
     double mx = -INFINITY, my = -INFINITY;
-    long long cnt = (long long)NFACE * (d.N + 1) * d.n;
-    for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const long long cnt = (long long)NFACE * (d.N + 1) * d.n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < cnt; t += (long long)gridDim.x * blockDim.x) {
         int p = (int)(t / ((long long)(d.N + 1) * d.n));
         int a = (int)((t / d.n) % (d.N + 1)), b = (int)(t % d.n);
         mx = fmax(mx, (double)U[at(d, p, d.i0 + a, b)] * dt / dx);
         my = fmax(my, (double)V[at(d, p, b, d.i0 + a)] * dt / dx);
+    }
+    rx[threadIdx.x] = mx;
+    ry[threadIdx.x] = my;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            rx[threadIdx.x] = fmax(rx[threadIdx.x], rx[threadIdx.x + s]);
+            ry[threadIdx.x] = fmax(ry[threadIdx.x], ry[threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[2 * blockIdx.x] = rx[0];
+        out[2 * blockIdx.x + 1] = ry[0];
+    }
+}
+
+// (max of in[2b], max of in[2b+1]) over b < nb -> out[0], out[1]; one block of 256
+__global__ void k_max_pairs(const double *__restrict__ in, int nb, double *out) {
+    __shared__ double rx[256], ry[256];
+    double mx = -INFINITY, my = -INFINITY;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        mx = fmax(mx, in[2 * b]);
+        my = fmax(my, in[2 * b + 1]);
     }
     rx[threadIdx.x] = mx;
     ry[threadIdx.x] = my;
@@ -503,12 +574,22 @@ static int average_t(const Options &o, const Grid &g, Winds &w, double dt, cudaS
 
 template <class W>
 static int cfl_t(const Grid &g, const Winds &w, double dt, double *tmp, double &cfl, cudaStream_t st) {
-    k_wind_cfl<W><<<1, 512, 0, st>>>(g.d, (const W *)w.u_pu, (const W *)w.v_pv, dt, g.dx, tmp);
+    // tmp holds at least 3 diag_partials(g) + 8 doubles: room for 2 nb + 2
+    int nb = diag_partials(g);
+    nb = nb < 1024 ? nb : 1024;
+    k_wind_cfl<W><<<nb, 256, 0, st>>>(g.d, (const W *)w.u_pu, (const W *)w.v_pv, dt, g.dx, tmp + 2);
+    k_max_pairs<<<1, 256, 0, st>>>(tmp + 2, nb, tmp);
     CSADV_CUDA(cudaGetLastError());
     double h[2];
     CSADV_CUDA(cudaMemcpyAsync(h, tmp, sizeof(h), cudaMemcpyDeviceToHost, st));
     CSADV_CUDA(cudaStreamSynchronize(st));
     cfl = fmax(fabs(h[0]), fabs(h[1]));
+    return CSADV_OK;
+}
+
+int wind_set_dt(Winds &w, double dt, cudaStream_t st) {
+    CSADV_CUDA(cudaMemcpyAsync((char *)w.clock + offsetof(Clock, dt), &dt, sizeof(double), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaStreamSynchronize(st));
     return CSADV_OK;
 }
 
@@ -544,6 +625,21 @@ int wind_avgprep(const Options &o, const Grid &g, const Winds &w, double dt, rea
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
+template <class real>
+int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, real *ua, real *vaT, uint32_t *ub,
+                   uint32_t *vbT, int wpitch, cudaStream_t st) {
+    const Dims d = g.d;
+    dim3 grid(d.pitch / 32, ceil_div(d.n + 1, 32), NFACE);
+    k_wind_avgprep_t<real><<<grid, dim3(32, 8), 0, st>>>(d, (const real *)w.u_pu, (const real *)w.u_old,
+                                                          (const real *)w.v_pv, (const real *)w.v_old, ua, vaT, ub,
+                                                          vbT, wpitch, o.dp == 2, (real)(dt * 0.5), (real)g.dx);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+template int wind_avgprep_t<double>(const Options &, const Grid &, const Winds &, double, double *, double *,
+                                    uint32_t *, uint32_t *, int, cudaStream_t);
+template int wind_avgprep_t<float>(const Options &, const Grid &, const Winds &, double, float *, float *, uint32_t *,
+                                   uint32_t *, int, cudaStream_t);
 template int wind_avgprep<double>(const Options &, const Grid &, const Winds &, double, double *, double *, uint32_t *,
                                   uint32_t *, int, cudaStream_t);
 template int wind_avgprep<float>(const Options &, const Grid &, const Winds &, double, float *, float *, uint32_t *,

@@ -59,7 +59,8 @@ def test_plan_create_rejects_bad_arguments_before_touching_the_gpu(lib):
     bad.opsplit = 3  # SP-PL07 with MT-0
     assert lib.csadv_plan_create(16, 0.01, 1, ctypes.byref(bad), None, ctypes.byref(h)) == _lib.ERR_OPTION_PAIR
     assert lib.csadv_plan_create(4, 0.01, 1, ctypes.byref(o), None, ctypes.byref(h)) == _lib.ERR_ARG
-    assert lib.csadv_plan_create(16, -1.0, 1, ctypes.byref(o), None, ctypes.byref(h)) == _lib.ERR_ARG
+    for dt in (0.0, float("nan"), -5.0):  # dt < 0 is a CFL target (at most 4)
+        assert lib.csadv_plan_create(16, dt, 1, ctypes.byref(o), None, ctypes.byref(h)) == _lib.ERR_ARG
     assert lib.csadv_plan_create(16, 0.01, 0, ctypes.byref(o), None, ctypes.byref(h)) == _lib.ERR_ARG
     assert lib.csadv_plan_create(16, 0.01, 1, None, None, ctypes.byref(h)) == _lib.ERR_ARG
     assert not h.value

@@ -59,7 +59,7 @@ def test_fused_fp64_vs_reference_golden(golden_dir, vf):
     assert n > 0
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5, 6, 7, 8])
 @pytest.mark.parametrize("N", [40, 50, 64])
 def test_fused_fp64_partial_tiles_vs_oracle(N, tile):
     c, vf, ic, dt, nsteps = (2, 2, 1, 3, 1, 3), 2, 3, 0.004, 6
@@ -70,6 +70,32 @@ def test_fused_fp64_partial_tiles_vs_oracle(N, tile):
         pl.init_tracer(ic)
         pl.advance(nsteps)
         assert rel(pl.get_tracer(), sim.Q[g.interior]) <= RTOL
+
+
+def _et_dg_schemes():
+    out = []
+    for recon in (1, 2, 3, 4):
+        for dp in (1, 2):
+            for sp, mt in ((1, 1), (2, 1), (3, 2)):
+                for mf in (1, 3):
+                    out.append((recon, dp, sp, 3, mt, mf))
+    return out
+
+
+@pytest.mark.parametrize("N", [8, 61, 130])
+def test_sweep_kernel_equals_tile_kernel_every_scheme(N):
+    # the line-marching kernel (tiles 5-8) against the per-edge tile kernel (tiles 1-4):
+    # same arithmetic, so FP64 agrees at the parity bar and FP32 to rounding
+    dt = 0.25 / N
+    for c in _et_dg_schemes():
+        for prec, tol in ((64, RTOL), (32, 1e-5)):
+            outs = []
+            for tile in (1, 5 if N >= 100 else 8):
+                with plan(N, dt, c, 2, engine=FUSED, precision=prec, tile=tile) as pl:
+                    pl.init_tracer(3)
+                    pl.advance(4)
+                    outs.append(pl.get_tracer())
+            assert rel(outs[1], outs[0]) <= tol, (c, prec)
 
 
 @pytest.mark.parametrize("c", [(1, 1, 1, 3, 1, 1), (2, 2, 1, 3, 1, 3), (3, 2, 2, 3, 1, 3), (4, 1, 3, 3, 2, 3),
