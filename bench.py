@@ -293,6 +293,50 @@ def run_batched(torch, steps, warmup, stream, hbm):
                       "Gaussian hills, CFL 0.5, FP32 (timed: %d of the 200 steps)" % steps}
 
 
+def run_large(torch, steps, warmup, stream, hbm):
+    """N = 1536 (6 x 1536^2 = 14.2 M cells per tracer), 8 FP32 tracers sharing one divergent
+    wind (solid body at alpha = pi/4 plus the 0.3 u0 divergent perturbation), CFL 0.7; the
+    timed steps are a sample of the 500-step run.  State ~3.6 GB, far above L2."""
+    import math
+    from csadv import Plan, tune
+    N, T = 1536, 8
+    kw = dict(vf=103, wind_param=(math.pi / 4, 2 * math.pi / 5, 0.3, 0.0), ntracers=T, precision=32,
+              stream=stream, **SCHEME)
+    pl = Plan(N, -0.7, **kw)
+    for t in range(T):
+        lon = -math.pi + 2 * math.pi * t / T
+        pl.init_tracer(101, ic_param=(lon, 0.3 * math.sin(3 * t), 5.0, 0.0), tracer=t)
+    tile = tune(pl, reps=2, stream=stream)
+    m0 = [pl.mass(t) for t in range(T)]
+    pl.advance(warmup)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    pl.advance(steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    pl.set_profiling(True)
+    pl.reset_stats()
+    pl.advance(3)
+    pst = pl.stats()
+    pl.set_profiling(False)
+    kms = pst["main_ms"] / max(1, pst["main_launches"])
+    cells = T * 6 * N * N
+    alg = 6 * N * N * (T * 2 * 4 + 3 * 4)
+    achieved = alg / (kms * 1e-3) / 1e9
+    dm = max(abs(pl.mass(t) - m0[t]) / abs(m0[t]) for t in range(T))
+    res = {"value": round(cells / (ms * 1e-3), 1), "unit": "tracer cell-steps/s", "ms_per_step": round(ms, 4),
+           "step_kernel_ms": round(kms, 4), "tile": tile, "cfl": round(pl.cfl, 4),
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                        "frac": round(achieved / hbm, 4), "alg_bytes_per_launch": alg},
+           "max_mass_change": float("%.3e" % dm),
+           "config": "N=1536, 8 FP32 tracers, solid body + 0.3 u0 divergent wind, CFL 0.7 (timed: %d of the "
+                     "500 steps)" % steps}
+    pl.close()
+    return res
+
+
 def run_serving(torch, nreq, stream, budget_gb=120.0):
     """The request loop on a seeded Poisson stream (200 req/s; N log-uniform in [32, 1024],
     steps uniform in [50, 2000], 1-4 tracers, solid-body or deformational wind 50/50, FP32,
@@ -399,6 +443,8 @@ def bench_gpu(args):
     if not args.no_batched:
         line["batched"] = run_batched(torch, args.batched_steps, args.warmup, stream, hbm)
         line["batched"]["vs_fp64_single"] = round(line["batched"]["value"] / line["fp64"]["value"], 2)
+    if not args.no_large:
+        line["large"] = run_large(torch, args.large_steps, args.warmup, stream, hbm)
     if args.serve_requests > 0:
         line["serving"] = run_serving(torch, args.serve_requests, stream)
     if world == 1 and not args.no_cpu:
@@ -454,7 +500,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-solve batched leg")
     ap.add_argument("--batched-steps", type=int, default=20, help="timed steps of the batched leg")
-    ap.add_argument("--serve-requests", type=int, default=0,
+    ap.add_argument("--no-large", action="store_true", help="skip the N=1536, 8-tracer leg")
+    ap.add_argument("--large-steps", type=int, default=20, help="timed steps of the N=1536 leg")
+    ap.add_argument("--serve-requests", type=int, default=100,
                     help="run the serving leg on the first N requests of the seeded stream (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:

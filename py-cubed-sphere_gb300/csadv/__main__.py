@@ -1,0 +1,31 @@
+"""``python -m csadv [pardir]``: the advection test case of the reference's main.py:78-95.
+
+Reads par/configuration.par and par/advection.par (or those in `pardir`); test case 5 runs
+one advection simulation (advection test case 1: adv_sphere) or the convergence study
+(advection test case 2: error_analysis_adv) on the GPU.  Other test cases (grid generation,
+grid quality, interpolation, divergence) are outside this library.
+"""
+import sys
+
+from .advection import adv_simulation_par, adv_sphere, cubed_sphere, error_analysis_adv
+from .configuration import PARDIR, get_advection_parameters, get_parameters
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    pardir = argv[0] if argv else PARDIR
+    N, transformation, showonscreen, gridload, test_case, map_projection = get_parameters(pardir)
+    if test_case != 5:
+        print("ERROR: this library runs the advection test case (5); configuration.par asks for", test_case)
+        raise SystemExit(1)
+    print("Test case 5: Advection test case.\n")
+    cs_grid = cubed_sphere(N, transformation, showonscreen, gridload)
+    dt, Tf, tc, ic, vf, recon, dp, opsplit, et, mt, mf = get_advection_parameters(pardir)
+    simulation = adv_simulation_par(cs_grid, dt, Tf, ic, vf, tc, recon, dp, opsplit, et, mt, mf)
+    if simulation.tc == 1:
+        return adv_sphere(cs_grid, None, simulation, map_projection, False, False)
+    return error_analysis_adv(simulation, map_projection, False, transformation, showonscreen, gridload, pardir=pardir)
+
+
+if __name__ == "__main__":
+    main()

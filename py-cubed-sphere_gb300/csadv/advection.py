@@ -227,9 +227,71 @@ def adv_sphere(cs_grid, ll_grid, simulation, map_projection, plot, divtest_flag)
         adv_time_step(cs_grid, s, 1, dt)
         return s.error_linf[1], s.error_l1[1], s.error_l2[1]
     output_adv(cs_grid, ll_grid, s, plot, 0, 0.0, Nsteps, plotstep, map_projection, divtest_flag)
+    if not plot and Nsteps > 0:
+        # nothing is output before the last step: the same steps (time step, then wind update
+        # at k dt), replayed on the device without a host round trip per step
+        s.plan.advance(Nsteps - 1)
+        adv_time_step(cs_grid, s, Nsteps, Nsteps * dt)
+        output_adv(cs_grid, ll_grid, s, plot, Nsteps, Nsteps * dt, Nsteps, plotstep, map_projection, divtest_flag)
+        update_adv(cs_grid, s, Nsteps * dt)
+        return s.error_linf[Nsteps], s.error_l1[Nsteps], s.error_l2[Nsteps]
     for k in range(1, Nsteps + 1):
         t = k * dt
         adv_time_step(cs_grid, s, k, t)
         output_adv(cs_grid, ll_grid, s, plot, k, t, Nsteps, plotstep, map_projection, divtest_flag)
         update_adv(cs_grid, s, t)
     return s.error_linf[Nsteps], s.error_l1[Nsteps], s.error_l2[Nsteps]
+
+
+def print_errors_simul(error_linf, error_l1, error_l2, i):
+    """errors.py:87-94."""
+    if i > 0:
+        print("Norms          (Linf,    L1,       L2) ")
+        print("Error E_" + str(i) + "    :", "{:.2e}".format(error_linf[i]), "{:.2e}".format(error_l1[i]),
+              "{:.2e}".format(error_l2[i]))
+        print("Ratio E_" + str(i) + "/E_" + str(i - 1) + ":", "{:.2e}".format(error_linf[i - 1] / error_linf[i]),
+              "{:.2e}".format(error_l1[i - 1] / error_l1[i]), "{:.2e}".format(error_l2[i - 1] / error_l2[i]))
+    else:
+        print("Error(Linf, L1, L2) :", "{:.2e}".format(error_linf[i]), "{:.2e}".format(error_l1[i]),
+              "{:.2e}".format(error_l2[i]))
+
+
+# the four schemes of the reference's convergence study (advection_error.py:66-71):
+# (recon, split, et, mt, dp, mf) -> PL07-RK1, PL07-RK1-DG-PR, AVLT-RK2-DG-AF, AVLT-RK2-DG-PR
+CONVERGENCE_SCHEMES = ((3, 3, 2, 2, 1, 1), (3, 3, 3, 2, 1, 3), (3, 1, 3, 1, 2, 2), (3, 1, 3, 1, 2, 3))
+CONVERGENCE_NAMES = ("PL07-RK1", "PL07-RK1-DG-PR", "AVLT-RK2-DG-AF", "ALVT-RK2-DG-PR")
+
+
+def error_analysis_adv(simulation, map_projection, plot, transformation, showonscreen, gridload, Ntest=6,
+                       pardir=None):
+    """advection_error.py:21-188: N = 16, 32, ... (Ntest resolutions), dt halved with N, one
+    period (Tf = 5) of each of the four schemes, errors against the exact solution at Tf.
+    Returns (Nc, error_linf, error_l1, error_l2, rates) with errors of shape (Ntest, 4) and
+    rates[norm] = log2(E_i-1 / E_i).  Figures are not drawn (plot is ignored)."""
+    from .configuration import PARDIR, get_advection_parameters
+    vf = simulation.vf
+    tc = simulation.tc
+    dt0 = {1: 0.025, 2: 0.0125, 3: 0.00625, 4: 0.0125}.get(vf)
+    if dt0 is None:
+        print("ERROR: invalid vector field, ", vf)
+        raise SystemExit(1)
+    Nc = np.array([16 * 2 ** i for i in range(Ntest)], dtype=float)
+    dts = np.array([dt0 * 0.5 ** i for i in range(Ntest)])
+    errs = [np.zeros((Ntest, len(CONVERGENCE_SCHEMES))) for _ in range(3)]
+    dt, Tf, tc_par, ic, vf_par, recon, dp, opsplit, et, mt, mf = get_advection_parameters(pardir or PARDIR, verbose=False)
+    Tf = 5
+    for d, (rec, sp, ET, MT, DP, MF) in enumerate(CONVERGENCE_SCHEMES):
+        for i in range(Ntest):
+            N = int(Nc[i])
+            cs_grid = cubed_sphere(N, transformation, False, gridload)
+            sim = adv_simulation_par(cs_grid, dts[i], Tf, ic, vf, tc, rec, DP, sp, ET, MT, MF)
+            print("\nParameters: N=" + str(N) + ", dt=" + str(dts[i]), ", recon=", sim.recon_name, ", split=",
+                  sim.opsplit_name, ", dp=", sim.dp_name, ", et=", sim.et_name)
+            errs[0][i, d], errs[1][i, d], errs[2][i, d] = adv_sphere(cs_grid, None, sim, map_projection, False, False)
+            print_errors_simul(errs[0][:, d], errs[1][:, d], errs[2][:, d], i)
+            sim.plan.close()
+    rates = {name: np.abs(np.log(e[1:]) - np.log(e[:-1])) / np.log(2.0) for name, e in zip(("linf", "l1", "l2"), errs)}
+    for name, r in rates.items():
+        print("Convergence rate (" + name + "):", " ".join("%s %s" % (CONVERGENCE_NAMES[d], np.array2string(r[:, d], precision=2))
+                                                       for d in range(len(CONVERGENCE_SCHEMES))))
+    return Nc, errs[0], errs[1], errs[2], rates

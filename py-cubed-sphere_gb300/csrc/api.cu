@@ -159,7 +159,7 @@ int fused_step_work(csadv_plan *pl, int kind, cudaStream_t st) {
     if (rc) return rc;
     const bool td = wind_time_dependent(pl->opt);
     if (td) {
-        rc = wind_halo(pl->opt, pl->grid, pl->w, st);
+        if (!pl->w.nbasis) rc = wind_halo(pl->opt, pl->grid, pl->w, st);  // the basis includes the halo
         if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
         if (rc) return rc;
     }
@@ -299,7 +299,7 @@ namespace csadv {
 int plan_pre_step(csadv_plan *pl, cudaStream_t st) {
     int rc = fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
     if (!rc && wind_time_dependent(pl->opt)) {
-        rc = wind_halo(pl->opt, pl->grid, pl->w, st);
+        if (!pl->w.nbasis) rc = wind_halo(pl->opt, pl->grid, pl->w, st);
         if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
     }
     return rc;
@@ -403,6 +403,7 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     // init_vars_adv (advection_vars.py:19-107): t = 0 winds, wind halo, old <- current,
     // departure-point winds, CFL
     rc = wind_setup(o, pl->grid, pl->w, pl->mem, dt, st);
+    if (!rc && fused) rc = wind_basis_setup(o, pl->grid, pl->w, pl->mem, st);
     if (!rc) rc = wind_initial(o, pl->grid, pl->w, st);
     if (!rc) rc = wind_halo(o, pl->grid, pl->w, st);
     if (!rc) rc = copy_d2d(pl->w.u_old, pl->w.u_pu, (size_t)F * pl->w.esize, st);
@@ -450,8 +451,13 @@ int csadv_init_tracer(csadv_plan *pl, int tracer, int ic, const double *ic_param
     if (!((ic >= 1 && ic <= 4) || (ic >= CSADV_IC_HILL && ic <= CSADV_IC_SMOOTH_BELLS))) return CSADV_ERR_OPTION;
     if (ic == CSADV_IC_HILL && !ic_param) return CSADV_ERR_ARG;
     IcParams p = ic_params(pl, ic_param);
-    if (pl->opt.precision == 64) return init_tracer<double>(pl->grid, ic, pl->opt.vf, p, (double *)pl->tracer(tracer), S(stream));
-    return init_tracer<float>(pl->grid, ic, pl->opt.vf, p, (float *)pl->tracer(tracer), S(stream));
+    cudaStream_t st = S(stream);
+    int rc = settle(pl, st);  // a pending correction belongs to the old field
+    if (rc) return rc;
+    rc = pl->opt.precision == 64 ? init_tracer<double>(pl->grid, ic, pl->opt.vf, p, (double *)pl->tracer(tracer), st)
+                                 : init_tracer<float>(pl->grid, ic, pl->opt.vf, p, (float *)pl->tracer(tracer), st);
+    if (!rc && pl->f.on) rc = fused_anchor_mass(pl->opt, pl->grid, pl->f, pl->cur, tracer, st);
+    return rc;
 }
 
 int csadv_set_tracer(csadv_plan *pl, int tracer, const double *host, int layout, void *stream) {
@@ -463,8 +469,10 @@ int csadv_set_tracer(csadv_plan *pl, int tracer, const double *host, int layout,
     int rc = settle(pl, st);
     if (rc) return rc;
     CSADV_CUDA(cudaMemcpyAsync(pl->stage, host, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyHostToDevice, st));
-    if (pl->opt.precision == 64) return tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, true, st);
-    return tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, true, st);
+    rc = pl->opt.precision == 64 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, true, st)
+                                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, true, st);
+    if (!rc && pl->f.on) rc = fused_anchor_mass(pl->opt, pl->grid, pl->f, pl->cur, tracer, st);
+    return rc;
 }
 
 int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void *stream) {
@@ -554,6 +562,7 @@ int csadv_divergence(csadv_plan *pl, int tracer, double *host_div, void *stream)
     if (!pl || !host_div || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
     cudaStream_t st = S(stream);
     int rc = settle(pl, st);
+    if (!rc) rc = wind_sync(pl->opt, pl->grid, pl->w, st);  // the staged operators read u_pu, u_old
     if (rc) return rc;
     rc = pl->opt.precision == 64 ? time_step<double>(pl, st, false, tracer) : time_step<float>(pl, st, false, tracer);
     if (rc) return rc;

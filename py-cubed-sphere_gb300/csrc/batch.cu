@@ -33,7 +33,7 @@ struct csadv_batch {
     int work_cap = 0;                // entries per table
     int nwork = 0;
     size_t smem = 0;
-    int precision = 0, recon = 0;
+    int precision = 0, recon = 0, split = 0;
     int phase = 0;                   // steps since the tables were built, mod 2
     bool dirty = true;
     bool graphs = true;
@@ -67,7 +67,8 @@ bool batch_compatible(const csadv_batch *b, const csadv_plan *pl) {
     if (!pl->f.on || !pl->f.sweep) return false;
     if (b->plans.empty()) return true;
     const csadv_plan *r = b->plans.front();
-    return pl->opt.precision == r->opt.precision && pl->opt.recon == r->opt.recon && pl->device == b->device;
+    return pl->opt.precision == r->opt.precision && pl->opt.recon == r->opt.recon &&
+           pl->opt.opsplit == r->opt.opsplit && pl->device == b->device;
 }
 
 // descriptors and work tables from the current membership and buffer parities
@@ -122,6 +123,7 @@ int batch_rebuild(csadv_batch *b, cudaStream_t st) {
     b->nwork = total;
     b->precision = b->plans.front()->opt.precision;
     b->recon = b->plans.front()->opt.recon;
+    b->split = b->plans.front()->opt.opsplit;
     b->dirty = false;
     return CSADV_OK;
 }
@@ -141,8 +143,8 @@ int batch_step_work(csadv_batch *b, int kind, cudaStream_t st) {
     }
     if (b->prof) CSADV_CUDA(cudaEventRecord(b->pev[0], st));
     int rc = b->precision == 64
-                 ? sweep_launch<double>(b->recon, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st)
-                 : sweep_launch<float>(b->recon, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st);
+                 ? sweep_launch<double>(b->recon, b->split, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st)
+                 : sweep_launch<float>(b->recon, b->split, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st);
     if (rc) return rc;
     if (b->prof) CSADV_CUDA(cudaEventRecord(b->pev[1], st));
     for (csadv_plan *pl : b->plans) {

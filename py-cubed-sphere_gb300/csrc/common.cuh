@@ -118,6 +118,10 @@ struct Winds {
     void *tab[2] = {nullptr, nullptr};  // time-independent wind coefficients (x-, y-edges)
     int tkind = 0;                // 0: static wind, 1: deformational (6 coefs), 2: separable (1 coef)
     void *clock = nullptr;        // device clock (step count, time of the current wind)
+    // fused engine: the time-dependent wind as coefficient fields of a time basis on every
+    // edge (ghost edges included), nbasis fields per direction; 0 = not used
+    void *btab[2] = {nullptr, nullptr};
+    int nbasis = 0;
 };
 
 __host__ __device__ __forceinline__ int ceil_div(long long a, int b) { return (int)((a + b - 1) / b); }

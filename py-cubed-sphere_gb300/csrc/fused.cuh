@@ -21,6 +21,7 @@
 // shared by all tracers.
 #pragma once
 #include "common.cuh"
+#include "halo.cuh"
 #include "internal.h"
 #include "tiles.h"
 
@@ -219,7 +220,7 @@ __global__ void __launch_bounds__(256) k_fused(FusedArgs a) {
             for (int c = tx; c < nj + 6; c += 32) {
                 const int j = J0 - 3 + c;
                 real v = Qin[i * P + j];
-                if (hc && irow && j >= d.i0 && j < d.iend) v = v + sG[r * QJ + c] * corr;
+                if (hc && irow && j >= d.i0 && j < d.iend) v = corrected(v, sG[r * QJ + c], corr);
                 sQ[r * QJ + c] = v;
             }
         }

@@ -1,5 +1,6 @@
 // Host side of the fused engine: buffers, wind preparation, step sequencing, and the
 // lazy MF-PR correction.
+#include "halo.cuh"
 #include "internal.h"
 #include "tiles.h"
 
@@ -29,6 +30,25 @@ __global__ void k_plane_xform(const real *__restrict__ src, real *dst, Dims d, i
     dst[t] = v;
 }
 
+// cell records {g, 1/g} of the n x n centres, natural (dst(i, j)) or transposed (dst(j, i));
+// zero outside
+template <class real>
+__global__ void k_cell_records(const real *__restrict__ g, typename Vec2<real>::type *dst, Dims d, int n,
+                               int transpose) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= d.plane) return;
+    const int a = (int)(t / d.pitch), b = (int)(t % d.pitch);
+    const int i = transpose ? b : a, j = transpose ? a : b;
+    typename Vec2<real>::type v;
+    v.x = real(0);
+    v.y = real(0);
+    if (i < n && j < n) {
+        v.x = g[(long long)i * d.pitch + j];
+        v.y = real(1) / v.x;
+    }
+    dst[t] = v;
+}
+
 // Q* + g corr on interior cells of every tracer (the true state); blockIdx.y = tracer
 template <class real>
 __global__ void k_materialize(real *Q0, Dims d, const real *__restrict__ g, const double *__restrict__ corr) {
@@ -38,7 +58,7 @@ __global__ void k_materialize(real *Q0, Dims d, const real *__restrict__ g, cons
     int j = d.i0 + (int)(t % N), i = d.i0 + (int)((t / N) % N), p = (int)(t / ((long long)N * N));
     real *Q = Q0 + blockIdx.y * d.field;
     long long o = at(d, p, i, j);
-    Q[o] = Q[o] + g[at2(d, i, j)] * (real)corr[blockIdx.y];
+    Q[o] = corrected(Q[o], g[at2(d, i, j)], (real)corr[blockIdx.y]);
 }
 
 // copy every non-interior cell of the n x n cell planes from `src` to `dst` (all tracers)
@@ -55,6 +75,15 @@ __global__ void k_copy_ghosts(const real *__restrict__ src, real *dst, Dims d) {
 
 int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
     const Dims d = g.d;
+    if (f.sweep && f.inline_ghosts) {  // the step kernel kept its ghost cells on chip: fill the input's
+        const bool pr = o.mf == MF_PR;
+        int rc = o.precision == 64
+                     ? launch_halo_dg_tracers<double>((double *)f.Qbuf[1 - cur], T, g, pr ? f.corr[1 - cur] : nullptr,
+                                                      (const double *)f.g_pc, st)
+                     : launch_halo_dg_tracers<float>((float *)f.Qbuf[1 - cur], T, g, pr ? f.corr[1 - cur] : nullptr,
+                                                     (const float *)f.g_pc, st);
+        if (rc) return rc;
+    }
     dim3 grid(ceil_div((long long)NFACE * d.n * d.n, 256), T);
     if (o.precision == 64)
         k_copy_ghosts<double><<<grid, 256, 0, st>>>((const double *)f.Qbuf[1 - cur], (double *)f.Qbuf[cur], d);
@@ -101,37 +130,39 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
         f.g_pv = gs[2];
     }
     if (!mem.ok()) return CSADV_ERR_OOM;
-    // line-marching kernel data: transposed y-edge winds, flags and metric; 1/g
-    f.vaT = mem.alloc<char>(d.field * es);
-    f.vbT = mem.alloc<uint32_t>(words);
-    void *planes[4];
-    for (int c = 0; c < 4; ++c) planes[c] = mem.alloc<char>(d.plane * es);
+    // line-marching kernel data: edge records (filled by the wind preparation), cell records
+    // {g, 1/g} natural and transposed, the y-edge metric transposed (for the y-edge records)
+    f.erx = mem.alloc<char>(2 * d.field * es);
+    f.ery = mem.alloc<char>(2 * d.field * es);
+    f.crx = mem.alloc<char>(2 * d.plane * es);
+    f.cry = mem.alloc<char>(2 * d.plane * es);
+    void *gpvT = mem.alloc<char>(d.plane * es);
     f.dsolve = mem.alloc<SweepSolve>(2);
+    if (o.precision == 32 && o.mf == MF_PR) {
+        f.mass_target = mem.alloc<double>(T);
+        f.anchor_part = mem.alloc<double>(512);
+    }
     if (!mem.ok()) return CSADV_ERR_OOM;
     {
         const int nb = ceil_div(d.plane, 256);
         const int n = d.n;
         if (o.precision == 64) {
             const double *gpc = (const double *)f.g_pc, *gpv = (const double *)f.g_pv;
-            k_plane_xform<double><<<nb, 256, 0, st>>>(gpc, (double *)planes[0], d, n, n, 1, 0);
-            k_plane_xform<double><<<nb, 256, 0, st>>>(gpv, (double *)planes[1], d, n, n + 1, 1, 0);
-            k_plane_xform<double><<<nb, 256, 0, st>>>(gpc, (double *)planes[2], d, n, n, 0, 1);
-            k_plane_xform<double><<<nb, 256, 0, st>>>(gpc, (double *)planes[3], d, n, n, 1, 1);
+            k_cell_records<double><<<nb, 256, 0, st>>>(gpc, (double2 *)f.crx, d, n, 0);
+            k_cell_records<double><<<nb, 256, 0, st>>>(gpc, (double2 *)f.cry, d, n, 1);
+            k_plane_xform<double><<<nb, 256, 0, st>>>(gpv, (double *)gpvT, d, n, n + 1, 1, 0);
         } else {
             const float *gpc = (const float *)f.g_pc, *gpv = (const float *)f.g_pv;
-            k_plane_xform<float><<<nb, 256, 0, st>>>(gpc, (float *)planes[0], d, n, n, 1, 0);
-            k_plane_xform<float><<<nb, 256, 0, st>>>(gpv, (float *)planes[1], d, n, n + 1, 1, 0);
-            k_plane_xform<float><<<nb, 256, 0, st>>>(gpc, (float *)planes[2], d, n, n, 0, 1);
-            k_plane_xform<float><<<nb, 256, 0, st>>>(gpc, (float *)planes[3], d, n, n, 1, 1);
+            k_cell_records<float><<<nb, 256, 0, st>>>(gpc, (float2 *)f.crx, d, n, 0);
+            k_cell_records<float><<<nb, 256, 0, st>>>(gpc, (float2 *)f.cry, d, n, 1);
+            k_plane_xform<float><<<nb, 256, 0, st>>>(gpv, (float *)gpvT, d, n, n + 1, 1, 0);
         }
         CSADV_CUDA(cudaGetLastError());
     }
-    f.gpcT = planes[0];
-    f.gpvT = planes[1];
-    f.igpc = planes[2];
-    f.igpcT = planes[3];
-    CSADV_CUDA(cudaMemsetAsync(f.vaT, 0, (size_t)d.field * es, st));
-    CSADV_CUDA(cudaMemsetAsync(f.vbT, 0, (size_t)words * sizeof(uint32_t), st));
+    f.gpvT = gpvT;
+    CSADV_CUDA(cudaMemsetAsync(f.erx, 0, 2 * (size_t)d.field * es, st));
+    CSADV_CUDA(cudaMemsetAsync(f.ery, 0, 2 * (size_t)d.field * es, st));
+    if (f.mass_target) CSADV_CUDA(cudaMemsetAsync(f.mass_target, 0, T * sizeof(double), st));
     CSADV_CUDA(cudaMemsetAsync(f.Qbuf[1], 0, (size_t)T * d.field * es, st));
     for (int b = 0; b < 2; ++b) CSADV_CUDA(cudaMemsetAsync(f.corr[b], 0, T * sizeof(double), st));
     CSADV_CUDA(cudaMemsetAsync(f.counter, 0, sizeof(unsigned int), st));
@@ -140,10 +171,23 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
 }
 
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, cudaStream_t st) {
+    if (f.sweep && w.nbasis) {
+        if (o.precision == 64)
+            return wind_step<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT, (double2 *)f.erx,
+                                     (double2 *)f.ery, st);
+        return wind_step<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.erx,
+                                (float2 *)f.ery, st);
+    }
+    if (w.nbasis) {  // per-edge tile kernel on a basis wind: current and previous winds first
+        int rc = wind_sync(o, g, w, st);
+        if (rc) return rc;
+    }
     if (f.sweep) {
         if (o.precision == 64)
-            return wind_avgprep_t<double>(o, g, w, dt, (double *)f.ua, (double *)f.vaT, f.upos, f.vbT, f.wpitch, st);
-        return wind_avgprep_t<float>(o, g, w, dt, (float *)f.ua, (float *)f.vaT, f.upos, f.vbT, f.wpitch, st);
+            return wind_avgprep_t<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT,
+                                          (double2 *)f.erx, (double2 *)f.ery, st);
+        return wind_avgprep_t<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.erx,
+                                     (float2 *)f.ery, st);
     }
     if (o.precision == 64)
         return wind_avgprep<double>(o, g, w, dt, (double *)f.ua, (double *)f.va, f.upos, f.vpos, f.wpitch, st);
@@ -152,8 +196,8 @@ int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt,
 
 int fused_prepare(const Options &o, int tile) {
     if (tile >= FUSED_NTILE_CFG)
-        return o.precision == 64 ? sweep_launch<double>(o.recon, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1)
-                                 : sweep_launch<float>(o.recon, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1);
+        return o.precision == 64 ? sweep_launch<double>(o.recon, o.opsplit, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1)
+                                 : sweep_launch<float>(o.recon, o.opsplit, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1);
     FusedArgs a{};
     return o.precision == 64 ? fused_launch<double>(a, o.recon, tile, (cudaStream_t)-1)
                              : fused_launch<float>(a, o.recon, tile, (cudaStream_t)-1);
@@ -184,20 +228,17 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.corr_out = pr ? f.corr[1 - b] : nullptr;
         s.partials = f.partials;
         s.counter = f.counter;
-        s.ua = f.ua;
-        s.vaT = f.vaT;
-        s.ub = f.upos;
-        s.vbT = f.vbT;
+        s.erx = f.erx;
+        s.ery = f.ery;
+        s.crx = f.crx;
+        s.cry = f.cry;
         s.gpc = f.g_pc;
-        s.gpcT = f.gpcT;
-        s.igpc = f.igpc;
-        s.igpcT = f.igpcT;
-        s.gpu = f.g_pu;
-        s.gpvT = f.gpvT;
-        s.wpitch = f.wpitch;
         s.split = o.opsplit;
         s.mt = o.mt;
         s.mfpr = pr ? 1 : 0;
+        s.mass_target = f.mass_target;
+        s.lag_w = f.inline_ghosts ? g.lag_w : nullptr;
+        s.lag_k = f.inline_ghosts ? g.lag_k : nullptr;
     }
     f.nitems = NFACE * h[0].ntiles;
     f.smem = o.precision == 64 ? sweep_smem_bytes<double>(f.scfg) : sweep_smem_bytes<float>(f.scfg);
@@ -208,6 +249,7 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
 }
 
 int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
+    if (f.sweep && f.inline_ghosts) return CSADV_OK;  // the step kernel evaluates them itself
     const bool pr = o.mf == MF_PR;
     if (o.precision == 64)
         return launch_halo_dg_tracers<double>((double *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
@@ -221,8 +263,9 @@ int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &
     const bool pr = o.mf == MF_PR;
     if (f.sweep) {
         if (ev0) CSADV_CUDA(cudaEventRecord(ev0, st));
-        int rc = o.precision == 64 ? sweep_launch<double>(o.recon, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st)
-                                   : sweep_launch<float>(o.recon, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st);
+        int rc = o.precision == 64
+                     ? sweep_launch<double>(o.recon, o.opsplit, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st)
+                     : sweep_launch<float>(o.recon, o.opsplit, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st);
         if (rc) return rc;
         if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
         cur = 1 - cur;
@@ -257,6 +300,52 @@ int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &
     if (rc) return rc;
     if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
     cur = 1 - cur;
+    return CSADV_OK;
+}
+
+// sum over the interior of Q g (metric in the state's precision): per-block partials over a
+// grid-stride range, then one block sums them in a fixed order -> *out
+constexpr int ANCHOR_BLOCKS = 512;
+template <class real>
+__global__ void k_anchor_mass(const real *__restrict__ Q, const real *__restrict__ g, Dims d, double *part) {
+    __shared__ double red[256];
+    const int N = d.N;
+    double acc = 0.0;
+    for (long long t = blockIdx.x * 256LL + threadIdx.x; t < (long long)NFACE * N * N; t += (long long)gridDim.x * 256) {
+        const int j = d.i0 + (int)(t % N), i = d.i0 + (int)((t / N) % N), p = (int)(t / ((long long)N * N));
+        acc += (double)Q[at(d, p, i, j)] * (double)g[at2(d, i, j)];
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_anchor_sum(const double *__restrict__ part, int np, double *out) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < np; b += 256) acc += part[b];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+int fused_anchor_mass(const Options &o, const Grid &g, FusedState &f, int cur, int t, cudaStream_t st) {
+    if (!f.mass_target || o.precision != 32) return CSADV_OK;
+    const float *Q = (const float *)f.Qbuf[cur] + (size_t)t * g.d.field;
+    const int nb = ceil_div((long long)NFACE * g.d.N * g.d.N, 256) < ANCHOR_BLOCKS
+                       ? ceil_div((long long)NFACE * g.d.N * g.d.N, 256)
+                       : ANCHOR_BLOCKS;
+    k_anchor_mass<float><<<nb, 256, 0, st>>>(Q, (const float *)f.g_pc, g.d, f.anchor_part);
+    k_anchor_sum<<<1, 256, 0, st>>>(f.anchor_part, nb, f.mass_target + t);
+    CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
 

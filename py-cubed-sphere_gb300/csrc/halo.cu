@@ -16,57 +16,10 @@
 // Both are compiled without FMA contraction: each product and sum is rounded as in numpy,
 // so the FP64 form reproduces the reference's halo values bit for bit.
 #include "common.cuh"
+#include "halo.cuh"
 #include "internal.h"
 
 namespace csadv {
-
-// Source values of the ghost-cell interpolation.  With a pending MF-PR correction
-// (fused engine) the stored interior value is Q* and the true value is Q* + g corr,
-// formed in the state's precision exactly as the fused kernel forms it on load.
-template <class real>
-struct Src {
-    const real *F;
-    const real *g;  // metric plane (real), used only with corr
-    real corr;
-    bool has_corr;
-    __device__ __forceinline__ double interior(const Dims &d, int q, int i, int j) const {
-        real v = F[at(d, q, i, j)];
-        if (has_corr) v = v + g[at2(d, i, j)] * corr;
-        return (double)v;
-    }
-};
-
-// value of the ghost cell at depth `dep` outside side s of panel p, along index k
-// (k inside the edge's interior range); computed in FP64 from interior cells only
-template <class real>
-__device__ double side_ghost(const Src<real> &S, const Dims &d, const double *__restrict__ W,
-                             const int *__restrict__ K, int p, int s, int dep, int k) {
-    const Conn c = c_conn[p][s];
-    const int n = d.n;
-    const int k0 = K[dep * n + k];
-    const double *w = W + ((long long)dep * n + k) * 4;
-    double prod[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        int kk = k0 + m;
-        int along = c.rev ? n - 1 - kk : kk;
-        int i, j;
-        inside_ij(d, c.qs, dep, along, i, j);
-        prod[m] = S.interior(d, c.q, i, j) * w[m];
-    }
-    return ((prod[0] + prod[1]) + prod[2]) + prod[3];
-}
-
-// value of cell (i, j) of panel q where (i, j) is interior or in a side strip (not a corner)
-template <class real>
-__device__ double cell_or_side_ghost(const Src<real> &S, const Dims &d, const double *__restrict__ W,
-                                     const int *__restrict__ K, int q, int i, int j) {
-    if (i >= d.iend) return (double)(real)side_ghost(S, d, W, K, q, SIDE_E, i - d.iend, j);
-    if (i < d.i0) return (double)(real)side_ghost(S, d, W, K, q, SIDE_W, d.i0 - 1 - i, j);
-    if (j >= d.iend) return (double)(real)side_ghost(S, d, W, K, q, SIDE_N, j - d.iend, i);
-    if (j < d.i0) return (double)(real)side_ghost(S, d, W, K, q, SIDE_S, d.i0 - 1 - j, i);
-    return S.interior(d, q, i, j);
-}
 
 // blockIdx.y = tracer (fields `fstride` elements apart); corr[tracer] optional
 template <class real>
@@ -88,19 +41,7 @@ __global__ void k_halo_dg(real *F0, long long fstride, Dims d, const double *__r
         return;
     }
     if (s == SIDE_N || s == SIDE_S) return;  // corner blocks are filled from the E/W sides
-    const Conn c = c_conn[p][s];
-    const int k0 = K[dep * n + k];
-    const double *w = W + ((long long)dep * n + k) * 4;
-    double prod[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        int kk = k0 + m;
-        int along = c.rev ? n - 1 - kk : kk;
-        int i, j;
-        inside_ij(d, c.qs, dep, along, i, j);
-        prod[m] = cell_or_side_ghost(S, d, W, K, c.q, i, j) * w[m];
-    }
-    F[at(d, p, gi, gj)] = (real)(((prod[0] + prod[1]) + prod[2]) + prod[3]);
+    F[at(d, p, gi, gj)] = (real)ghost_value(S, d, W, K, p, gi, gj);
 }
 
 template <class real>

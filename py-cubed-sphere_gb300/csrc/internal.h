@@ -96,6 +96,15 @@ int staged_partial_count(const Grid &g);
 int wind_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, double dt, cudaStream_t st);
 // the time step of the device clock (set before the first step)
 int wind_set_dt(Winds &w, double dt, cudaStream_t st);
+// time-dependent wind of a fused plan as coefficient fields of a time basis, ghost edges
+// included (uses u_pu / v_pv as scratch: call before wind_initial)
+int wind_basis_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, cudaStream_t st);
+// departure-point winds + upwind flags of the step from the basis (line-marching layouts)
+template <class real, class V>
+int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
+              V *ery, cudaStream_t st);
+// u_pu, v_pv, u_old, v_old <- the basis at the clock's times (before staged operators run)
+int wind_sync(const Options &o, const Grid &g, const Winds &w, cudaStream_t st);
 int wind_initial(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
 int wind_update(const Options &o, const Grid &g, Winds &w, bool tick, long long k, double t, cudaStream_t st);
 int wind_halo(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
@@ -123,11 +132,14 @@ struct FusedState {
     // 1/g, and one launch descriptor per buffer parity (device memory)
     bool sweep = false;
     int scfg = 0;               // SWEEP_TILES index
-    void *vaT = nullptr;
-    uint32_t *vbT = nullptr;
-    const void *gpcT = nullptr, *gpvT = nullptr, *igpc = nullptr, *igpcT = nullptr;
+    void *erx = nullptr, *ery = nullptr;  // edge records {wind, +-g} (x natural, y transposed)
+    void *crx = nullptr, *cry = nullptr;  // cell records {g, 1/g} (natural, transposed)
+    const void *gpvT = nullptr;           // y-edge metric transposed
     SweepSolve *dsolve = nullptr;  // [2]
     int nitems = 0;             // work items of one sweep launch (6 x tiles)
+    bool inline_ghosts = false; // k_sweep evaluates the ET-DG ghost cells of its tiles (no ghost kernel)
+    double *mass_target = nullptr;  // [T] FP32 + MF-PR: sum(Q g) of each tracer when it was set
+    double *anchor_part = nullptr;  // [512] block partials of that sum
     size_t smem = 0;
 };
 
@@ -145,13 +157,17 @@ int fused_prepare(const Options &o, int tile);
 // zero-based); rewrites the sweep descriptors.  Outside stream capture.
 int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState &f, int tile, cudaStream_t st);
 template <class real>
-int sweep_launch(int recon, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
+int sweep_launch(int recon, int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
                  cudaStream_t st);
-template <class real>
-int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, real *ua, real *vaT, uint32_t *ub,
-                   uint32_t *vbT, int wpitch, cudaStream_t st);
+// edge records of the line-marching kernel from the reference-layout winds (static winds: once)
+template <class real, class V>
+int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT,
+                   V *erx, V *ery, cudaStream_t st);
 // ghost cells of Qbuf[cur] <- those of Qbuf[1-cur] (the halo the last step used)
 int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
+// FP32 form with MF-PR: record sum(Q g) of tracer t of Qbuf[cur] (no pending correction) as the
+// mass the step's correction restores
+int fused_anchor_mass(const Options &o, const Grid &g, FusedState &f, int cur, int t, cudaStream_t st);
 // apply and clear the pending MF-PR correction of Qbuf[cur]
 int fused_materialize(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
 template <class real> int fused_launch(const struct FusedArgs &a, int recon, int tile, cudaStream_t st);

@@ -30,6 +30,7 @@
 // only on the solve and its tile shape, so a solve gives the same bits alone or in a batch.
 #pragma once
 #include "fused.cuh"
+#include "halo.cuh"
 
 namespace csadv {
 
@@ -155,18 +156,23 @@ struct March {
 };
 
 // One grid line through a tile.  Cell m (tile-local, 0 = first interior cell of the tile
-// along the line) is at s[m * ss] in shared memory; the edge m (left edge of cell m) and the
-// cell m data in global memory are at [m * P]; the flag of edge m is bit `bit` of b[m * wp].
+// along the line) is at s[m * ss] in shared memory; the record of edge m (left edge of cell
+// m) is e[m * P] and that of cell m is c[m * P] in global memory.
 template <class real>
 struct Line {
+    using V = typename Vec2<real>::type;
     const real *s;
     int ss;
-    const real *u, *gE, *gC, *igC;
-    const uint32_t *b;
-    int bit;
+    const V *e, *c;
 };
 
 enum { MARCH_SPLIT = 0, MARCH_DIFF = 1, MARCH_UPDATE = 2 };
+
+// per-line sums of the update (MF-PR): div * g and the new Q * g
+template <class real>
+struct LineSums {
+    real div, mass;
+};
 
 #ifndef CSADV_SWEEP_UNROLL
 #define CSADV_SWEEP_UNROLL 1
@@ -177,36 +183,34 @@ constexpr int SWEEP_UNROLL = CSADV_SWEEP_UNROLL;  // march loop unrolling
 //   MARCH_SPLIT : split field of the first pass -> out[k * os]
 //   MARCH_DIFF  : flux difference F(k+1) - F(k) -> out[k * os]
 //   MARCH_UPDATE: Q(k) - dt div(k) -> qout[k * P], with the y-flux differences dY[k * os]
-//                 and Q(k) at Qc[k * qs]; returns the line's sum of div * g (MF-PR)
-// Every load of iteration m + 1 is issued during iteration m, so the global (L1/L2)
-// latency of the line's winds, flags and metric overlaps the arithmetic.
+//                 and Q(k) at Qc[k * qs]; returns the line's sums of div * g and of the new
+//                 Q * g (MF-PR)
+// Loads run ahead of the arithmetic: edge records two iterations, cell records and the
+// shared-memory window one iteration, so the global (L1/L2) latency overlaps the work.
 template <class real, int REC, int MODE>
-__device__ __forceinline__ real march(const Line<real> &ln, int P, int wp, int ma, int mb, real dtdx, real irdx,
-                                      int mt, int split, bool mfpr, real *out, int os, const real *dY,
-                                      const real *Qc, int qs, real *qout) {
+__device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int ma, int mb, real dtdx, real irdx,
+                                                int mt, int split, bool mfpr, real *out, int os, const real *dY,
+                                                const real *Qc, int qs, real *qout) {
+    using O = RealOps<real>;
+    using V = typename Vec2<real>::type;
     real w[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) w[k] = ln.s[(ma - 3 + k) * ln.ss];
     March<real, REC> rc;
     rc.init(w);
-    real gl = ln.gE[(ma - 1) * P];  // metric at the left edge of the current cell
-    // values of the next iteration, loaded one iteration ahead
-    real ngr = ln.gE[ma * P], ngc = ln.gC[(ma - 1) * P], nu = real(0), nig = real(0), nw4 = real(0);
-    uint32_t nb = 0u;
+    V eA = ln.e[(ma - 1) * P], eB = ln.e[ma * P], eN = eA;  // edges m, m+1 (m+2 loaded in the loop)
+    V cC = ln.c[(ma - 1) * P], cN = cC;                     // cell m
+    real nw4 = real(0);
     real pL = real(0), pR = real(0), pQ = real(0);  // previous cell's parabola (metric-weighted for MT-0)
-    real Fp = real(0), cp = real(0), gcp = real(0), acc = real(0);
+    real Fp = real(0), cp = real(0), gcp = real(0), igp = real(0), acc = real(0), accm = real(0);
 #pragma unroll SWEEP_UNROLL
     for (int m = ma - 1; m <= mb; ++m) {
-        const real gr = ngr, gcm = ngc, u = nu, ig = nig;
-        const uint32_t bw = nb;
         if (m < mb) {
             nw4 = ln.s[(m + 3) * ln.ss];
-            ngr = ln.gE[(m + 2) * P];
-            ngc = ln.gC[(m + 1) * P];
-            nu = ln.u[(m + 1) * P];
-            nb = ln.b[(m + 1) * wp];
-            if (MODE != MARCH_DIFF) nig = ln.igC[m * P];
+            eN = ln.e[(m + 2) * P];
+            cN = ln.c[(m + 1) * P];
         }
+        const real gl = O::ab(eA.y), gr = O::ab(eB.y), gcm = cC.x;
         real L, R;
         rc.cell(w, L, R);
         real cL = L, cR = R, cQ = w[2];
@@ -217,7 +221,9 @@ __device__ __forceinline__ real march(const Line<real> &ln, int P, int wp, int m
         }
         if (m >= ma) {
             // upwind PPM flux through edge m (flux.py:20-128): cell m-1 when the wind is >= 0
-            const bool up = (bw >> ln.bit) & 1u;
+            const real u = eA.x;
+            const bool up = !signbit(eA.y);
+            const real ig = igp;
             const real c = u * dtdx;
             const real eL = up ? pL : cL, eR = up ? pR : cR, eQ = up ? pQ : cQ;
             const real dq = eR - eL;
@@ -246,8 +252,12 @@ __device__ __forceinline__ real march(const Line<real> &ln, int P, int wp, int m
                     out[k * os] = F - Fp;
                 } else {
                     const real sdiv = (F - Fp) + dY[k * os];
-                    qout[(long long)k * P] = Qc[k * qs] - sdiv * dtdx * ig;
-                    if (mfpr) acc += sdiv * ig * irdx * gcp;
+                    const real qn = Qc[k * qs] - sdiv * dtdx * ig;
+                    qout[(long long)k * P] = qn;
+                    if (mfpr) {
+                        acc += sdiv * ig * irdx * gcp;
+                        accm += qn * gcp;
+                    }
                 }
             }
             Fp = F;
@@ -256,15 +266,18 @@ __device__ __forceinline__ real march(const Line<real> &ln, int P, int wp, int m
         pL = cL;
         pR = cR;
         pQ = cQ;
-        gl = gr;
         gcp = gcm;
+        igp = cC.y;
+        eA = eB;
+        eB = eN;
+        cC = cN;
         w[0] = w[1];
         w[1] = w[2];
         w[2] = w[3];
         w[3] = w[4];
         w[4] = nw4;
     }
-    return acc;
+    return LineSums<real>{acc, accm};
 }
 
 // CTAs per SM the register allocation is sized for: FP32 is latency-bound and gains from a
@@ -276,7 +289,9 @@ template <> struct SweepMinBlocks<double> { static constexpr int value = 1; };
 template <class real> struct SweepMinBlocks { static constexpr int value = CSADV_SWEEP_MINB; };
 #endif
 
-template <class real, int REC>
+// SPL: the splitting (SP_AVLT, SP_L04 with MT-0; SP_PL07 with MT-PL07), fixed per kernel so
+// the march loop carries no scheme branches
+template <class real, int REC, int SPL>
 __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_sweep(const SweepSolve *__restrict__ solves,
                                                          const int2 *__restrict__ work, int nwork) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -296,32 +311,41 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
         const int ni = min(ti, d.iend - I0), nj = min(tj, d.iend - J0);
         const SweepSmem L = sweep_smem(ti, tj);
         real *sQ = sm, *sQx = sm + L.oQx, *sQy = sm + L.oQy, *sDy = sm + L.oDy;
-        const int P = d.pitch, wp = S.wpitch;
+        const int P = d.pitch;
         const long long pofs = (long long)p * d.plane;
-        const long long bofs = (long long)p * (d.n + 1) * wp;
         const real dtdx = (real)(S.dt / S.dx);
         const real irdx = real(1) / (real)S.dx;
-        const int mt = S.mt, split = S.split;
+        constexpr int split = SPL, mt = SPL == SP_PL07 ? MT_PL07 : MT_0;
         const bool mfpr = S.mfpr != 0;
-        const real *ua = (const real *)S.ua + pofs, *vaT = (const real *)S.vaT + pofs;
-        const real *gpc = (const real *)S.gpc, *gpcT = (const real *)S.gpcT;
-        const real *igpc = (const real *)S.igpc, *igpcT = (const real *)S.igpcT;
-        const real *gpu = (const real *)S.gpu, *gpvT = (const real *)S.gpvT;
-        const uint32_t *ub = S.ub + bofs, *vbT = S.vbT + bofs;
+        using V = typename Vec2<real>::type;
+        const V *erx = (const V *)S.erx + pofs, *ery = (const V *)S.ery + pofs;
+        const V *crx = (const V *)S.crx, *cry = (const V *)S.cry;
+        const real *gpc = (const real *)S.gpc;
 
         for (int tr = 0; tr < S.T; ++tr) {
             const real *Qin = (const real *)S.Qin + (long long)tr * d.field + pofs;
             real *Qout = (real *)S.Qout + (long long)tr * d.field + pofs;
             const bool hc = S.corr_in != nullptr;
             const real corr = hc ? (real)S.corr_in[tr] : real(0);
-            // P0: Q on the tile + halo (+ pending mass-fixer correction on interior cells)
+            // P0: Q on the tile + halo: interior cells with the pending mass-fixer correction;
+            // ghost cells as filled by the ghost-cell kernel, or (lag_w set) interpolated here
+            // from the neighbouring panels (ET-DG, from the corrected interior values)
+            const Src<real> src{(const real *)S.Qin + (long long)tr * d.field, gpc, corr, hc};
+            const bool inline_ghosts = S.lag_w != nullptr;
             for (int r = warp; r < ni + 6; r += NWARP) {
                 const int i = I0 - 3 + r;
                 const bool irow = i >= d.i0 && i < d.iend;
                 for (int c = lane; c < nj + 6; c += 32) {
                     const int j = J0 - 3 + c;
-                    real v = Qin[(long long)i * P + j];
-                    if (hc && irow && j >= d.i0 && j < d.iend) v = v + gpc[(long long)i * P + j] * corr;
+                    real v;
+                    if (irow && j >= d.i0 && j < d.iend) {
+                        v = Qin[(long long)i * P + j];
+                        if (hc) v = corrected(v, gpc[(long long)i * P + j], corr);
+                    } else if (!inline_ghosts) {
+                        v = Qin[(long long)i * P + j];
+                    } else {
+                        v = (real)ghost_value(src, d, S.lag_w, S.lag_k, p, i, j);
+                    }
                     sQ[r * L.QJp + c] = v;
                 }
             }
@@ -337,19 +361,17 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
                         const int ma = ni * seg / S.s1x, mb = ni * (seg + 1) / S.s1x;
                         if (c >= nj + 3 || ma >= mb) continue;
                         const long long g0 = (long long)I0 * P + J0 + c;
-                        Line<real> ln{sQ + 3 * L.QJp + c + 3, L.QJp, ua + g0, gpu + g0, gpc + g0, igpc + g0,
-                                      ub + (long long)I0 * wp + ((J0 + c) >> 5), (J0 + c) & 31};
-                        march<real, REC, MARCH_SPLIT>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, false,
-                                                      sQx + c + 3, L.QJp, nullptr, nullptr, 0, nullptr);
+                        Line<real> ln{sQ + 3 * L.QJp + c + 3, L.QJp, erx + g0, crx + g0};
+                        march<real, REC, MARCH_SPLIT>(ln, P, ma, mb, dtdx, irdx, mt, split, false, sQx + c + 3,
+                                                      L.QJp, nullptr, nullptr, 0, nullptr);
                     } else {
                         const int jj = job - jx;
                         const int seg = jj / LY, r = jj - seg * LY - 3;
                         const int ma = nj * seg / S.s1y, mb = nj * (seg + 1) / S.s1y;
                         if (r >= ni + 3 || ma >= mb) continue;
                         const long long g0 = (long long)J0 * P + I0 + r;
-                        Line<real> ln{sQ + (r + 3) * L.QJp + 3, 1, vaT + g0, gpvT + g0, gpcT + g0, igpcT + g0,
-                                      vbT + (long long)J0 * wp + ((I0 + r) >> 5), (I0 + r) & 31};
-                        march<real, REC, MARCH_SPLIT>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, false,
+                        Line<real> ln{sQ + (r + 3) * L.QJp + 3, 1, ery + g0, cry + g0};
+                        march<real, REC, MARCH_SPLIT>(ln, P, ma, mb, dtdx, irdx, mt, split, false,
                                                       sQy + (r + 3) * L.TJp, 1, nullptr, nullptr, 0, nullptr);
                     }
                 }
@@ -364,15 +386,14 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
                     const int ma = nj * seg / S.s2y, mb = nj * (seg + 1) / S.s2y;
                     if (r >= ni || ma >= mb) continue;
                     const long long g0 = (long long)J0 * P + I0 + r;
-                    Line<real> ln{sQx + r * L.QJp + 3, 1, vaT + g0, gpvT + g0, gpcT + g0, igpcT + g0,
-                                  vbT + (long long)J0 * wp + ((I0 + r) >> 5), (I0 + r) & 31};
-                    march<real, REC, MARCH_DIFF>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, false, sDy + r * L.TJp, 1,
+                    Line<real> ln{sQx + r * L.QJp + 3, 1, ery + g0, cry + g0};
+                    march<real, REC, MARCH_DIFF>(ln, P, ma, mb, dtdx, irdx, mt, split, false, sDy + r * L.TJp, 1,
                                                  nullptr, nullptr, 0, nullptr);
                 }
             }
             __syncthreads();
-            // P3: x-lines of Qy over columns [0, nj): x fluxes, div, update, MF-PR partial
-            real acc = real(0);
+            // P3: x-lines of Qy over columns [0, nj): x fluxes, div, update, MF-PR partials
+            real acc = real(0), accm = real(0);
             {
                 const int LX = round32(nj);
                 const int jx = S.s2x * LX;
@@ -381,15 +402,17 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
                     const int ma = ni * seg / S.s2x, mb = ni * (seg + 1) / S.s2x;
                     if (c >= nj || ma >= mb) continue;
                     const long long g0 = (long long)I0 * P + J0 + c;
-                    Line<real> ln{sQy + 3 * L.TJp + c, L.TJp, ua + g0, gpu + g0, gpc + g0, igpc + g0,
-                                  ub + (long long)I0 * wp + ((J0 + c) >> 5), (J0 + c) & 31};
-                    acc += march<real, REC, MARCH_UPDATE>(ln, P, wp, ma, mb, dtdx, irdx, mt, split, mfpr, nullptr,
-                                                          L.TJp, sDy + c, sQ + 3 * L.QJp + c + 3, L.QJp,
-                                                          Qout + g0);
+                    Line<real> ln{sQy + 3 * L.TJp + c, L.TJp, erx + g0, crx + g0};
+                    const LineSums<real> ls = march<real, REC, MARCH_UPDATE>(
+                        ln, P, ma, mb, dtdx, irdx, mt, split, mfpr, nullptr, L.TJp, sDy + c, sQ + 3 * L.QJp + c + 3,
+                        L.QJp, Qout + g0);
+                    acc += ls.div;
+                    accm += ls.mass;
                 }
             }
             if (mfpr) {  // FP64 across threads, in a fixed order
-                double dacc = (double)acc;
+                const bool anchor = S.mass_target != nullptr;
+                double dacc = (double)(anchor ? accm : acc);
                 for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
                 if (lane == 0) red[warp] = dacc;
                 __syncthreads();
@@ -421,7 +444,10 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
                         if (tid < s) red[tid] += red[tid + s];
                         __syncthreads();
                     }
-                    if (tid == 0) S.corr_out[tr] = S.dt * red[0] / S.a2;
+                    // projection (discrete_operators.py:98-101): corr = dt m0 / a2; anchored FP32
+                    // form: the correction that brings sum(Q g) back to the target mass
+                    if (tid == 0)
+                        S.corr_out[tr] = S.mass_target ? (S.mass_target[tr] - red[0]) / S.a2 : S.dt * red[0] / S.a2;
                     __syncthreads();
                 }
                 if (tid == 0) *S.counter = 0u;
@@ -433,27 +459,37 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
 
 
 
-template <class real, int REC>
+template <class real, int REC, int SPL>
 int sweep_go(const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem, cudaStream_t st) {
     if (st == (cudaStream_t)-1) {  // prepare only: allow the largest layout
         size_t mx = 0;
         for (int c = 0; c < SWEEP_NTILE_CFG; ++c) mx = mx > sweep_smem_bytes<real>(c) ? mx : sweep_smem_bytes<real>(c);
-        CSADV_CUDA(cudaFuncSetAttribute(k_sweep<real, REC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+        CSADV_CUDA(cudaFuncSetAttribute(k_sweep<real, REC, SPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
         return CSADV_OK;
     }
-    k_sweep<real, REC><<<grid, SWEEP_THREADS, smem, st>>>(dsolves, work, nwork);
+    k_sweep<real, REC, SPL><<<grid, SWEEP_THREADS, smem, st>>>(dsolves, work, nwork);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
 
+template <class real, int REC>
+int sweep_split(int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
+                cudaStream_t st) {
+    switch (split) {
+        case SP_AVLT: return sweep_go<real, REC, SP_AVLT>(dsolves, work, nwork, grid, smem, st);
+        case SP_L04: return sweep_go<real, REC, SP_L04>(dsolves, work, nwork, grid, smem, st);
+        default: return sweep_go<real, REC, SP_PL07>(dsolves, work, nwork, grid, smem, st);
+    }
+}
+
 template <class real>
-int sweep_launch(int recon, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
+int sweep_launch(int recon, int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
                  cudaStream_t st) {
     switch (recon) {
-        case REC_PPM0: return sweep_go<real, REC_PPM0>(dsolves, work, nwork, grid, smem, st);
-        case REC_CW84: return sweep_go<real, REC_CW84>(dsolves, work, nwork, grid, smem, st);
-        case REC_PL07: return sweep_go<real, REC_PL07>(dsolves, work, nwork, grid, smem, st);
-        default: return sweep_go<real, REC_L04>(dsolves, work, nwork, grid, smem, st);
+        case REC_PPM0: return sweep_split<real, REC_PPM0>(split, dsolves, work, nwork, grid, smem, st);
+        case REC_CW84: return sweep_split<real, REC_CW84>(split, dsolves, work, nwork, grid, smem, st);
+        case REC_PL07: return sweep_split<real, REC_PL07>(split, dsolves, work, nwork, grid, smem, st);
+        default: return sweep_split<real, REC_L04>(split, dsolves, work, nwork, grid, smem, st);
     }
 }
 

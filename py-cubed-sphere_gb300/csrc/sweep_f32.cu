@@ -2,5 +2,5 @@
 #include "sweep.cuh"
 
 namespace csadv {
-template int sweep_launch<float>(int, const SweepSolve *, const int2 *, int, int, size_t, cudaStream_t);
+template int sweep_launch<float>(int, int, const SweepSolve *, const int2 *, int, int, size_t, cudaStream_t);
 }

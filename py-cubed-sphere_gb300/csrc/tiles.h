@@ -10,6 +10,11 @@
 
 namespace csadv {
 
+// a pair of the state's precision (edge and cell records of the line-marching kernel)
+template <class real> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
 // ---------------------------------------------------------------- per-edge tile kernel (k_fused)
 struct FusedArgs {
     Dims d;
@@ -54,11 +59,18 @@ struct SweepSolve {
     double *corr_out;       // [T] correction of Qout (MF-PR)
     double *partials;       // [T][6 ntiles]
     unsigned int *counter;  // arrival counter (MF-PR)
-    const void *ua, *vaT;   // departure-point winds: x-edges natural, y-edges transposed
-    const uint32_t *ub, *vbT;  // upwind flags (1: wind >= 0), the same two layouts, 32 per word
-    const void *gpc, *gpcT, *igpc, *igpcT, *gpu, *gpvT;  // metric planes in the state's precision
-    int wpitch;             // words per row of the flag arrays
+    // edge records {departure-point wind, +-metric at the edge; the sign is the upwind flag,
+    // + when the wind is >= 0}: x-edges natural (row i, column j), y-edges transposed (row j,
+    // column i); per panel plane, element type vec2 of the state's precision
+    const void *erx, *ery;
+    // cell records {metric, 1 / metric}: natural and transposed (one plane)
+    const void *crx, *cry;
+    const void *gpc;        // metric at the centres (state precision), for the pending correction
     int split, mt, mfpr;
+    const double *mass_target;  // FP32 form: per-tracer sum(Q g) that the MF-PR correction restores
+                                // (partials then hold sum(Q g)); null: the reference's projection
+    const double *lag_w;    // ET-DG ghost-cell weights and stencil starts: when set, the kernel
+    const int *lag_k;       // evaluates the ghost cells of its tiles itself; else it reads them
 };
 
 constexpr int SWEEP_THREADS = 256;

@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "tiles.h"
 
 namespace csadv {
 
@@ -27,6 +28,15 @@ struct WindParams {
     int vf;
     double prm[4];
 };
+
+// edge record {wind, +-g}: the sign carries the upwind flag (+: wind >= 0), g = |value|
+template <class V, class W>
+__device__ __forceinline__ V edge_record(W wind, W g, bool up) {
+    V r;
+    r.x = wind;
+    r.y = up ? g : -g;
+    return r;
+}
 
 static dim3 plane_grid(const Dims &d, int bx) { return dim3(ceil_div(d.pitch, bx), d.n + 1, NFACE); }
 
@@ -113,8 +123,10 @@ __global__ void k_wind_tables(Grid g, WindParams wp, W *tab0, W *tab1, int ncoef
 struct Clock {
     long long k;  // completed steps
     double dt;
-    double t;
+    double t;     // time of the current wind
     double f[4];  // deformational: k cos(pi t/T), sin(2 pi t/T), cos(2 pi t/T), 2 pi/T; vf 3: cos(pi t/5)
+    double t_old; // time of the previous wind (RK2 extrapolation)
+    double hn[4], ho[4];  // time-basis values at t and t_old (basis winds, see wind_basis_h)
 };
 
 __device__ void clock_factors(Clock *c, WindParams wp, int kind) {
@@ -131,15 +143,217 @@ __device__ void clock_factors(Clock *c, WindParams wp, int kind) {
     }
 }
 
-__global__ void k_clock_tick(Clock *c, WindParams wp, int kind) {
+__device__ void wind_basis_h(const WindParams &wp, int tkind, double t, double h[4]);
+
+// factors: 1 -> the time factors of the per-edge formula; 0 -> the time-basis values (the
+// wind at t_old is the one at the previous t, so each tick evaluates one new set)
+__global__ void k_clock_tick(Clock *c, WindParams wp, int kind, int factors) {
+    c->t_old = c->t;
     c->k += 1;
     c->t = (double)c->k * c->dt;
-    clock_factors(c, wp, kind);
+    if (factors) {
+        clock_factors(c, wp, kind);
+    } else {
+        for (int m = 0; m < 4; ++m) c->ho[m] = c->hn[m];
+        wind_basis_h(wp, kind, c->t, c->hn);
+    }
 }
-__global__ void k_clock_set(Clock *c, long long k, double t, WindParams wp, int kind) {
+__global__ void k_clock_set(Clock *c, long long k, double t, WindParams wp, int kind, int factors) {
+    c->t_old = c->t;
     c->k = k;
     c->t = t;
-    clock_factors(c, wp, kind);
+    if (factors) {
+        clock_factors(c, wp, kind);
+    } else {
+        wind_basis_h(wp, kind, c->t_old, c->ho);
+        wind_basis_h(wp, kind, c->t, c->hn);
+    }
+}
+
+// ---------------------------------------------------------------- time-dependent winds as a basis
+// For the fused engine a time-dependent wind is stored as u(edge, t) = sum_m C_m(edge) h_m(t)
+// on EVERY edge the step reads, ghost edges included: the reference's wind halo
+// (interpolation.py:347-532) is linear in the interior wind, so the ghost-edge coefficients
+// are the halo of each interior coefficient field, computed once.  A step then evaluates the
+// wind at the current and previous times directly (k_wind_step) instead of running the
+// wind update, the wind halo and the departure-point average as separate passes.
+//   deformational:  h = {1, K, K cos 2w, K sin 2w}, K = k cos(pi t/T), w = 2 pi t/T, from
+//                   sin^2(lon - w) = (1 - cos 2lon cos 2w - sin 2lon sin 2w) / 2 and
+//                   sin 2(lon - w) = sin 2lon cos 2w - cos 2lon sin 2w
+//   vf 3 / vf 4:    h = {cos(pi t/5)} / {1}
+__host__ __device__ inline int wind_nbasis(int tkind) { return tkind == 1 ? 4 : (tkind == 2 ? 1 : 0); }
+
+__device__ void wind_basis_h(const WindParams &wp, int tkind, double t, double h[4]) {
+    if (tkind == 1) {
+        const double Tp = wp.vf == 2 ? 5.0 : wp.prm[1], k = wp.vf == 2 ? 2.0 : wp.prm[0];
+        const double K = k * cos(PI * t / Tp), w2 = 4.0 * PI * t / Tp;
+        h[0] = 1.0;
+        h[1] = K;
+        h[2] = K * cos(w2);
+        h[3] = K * sin(w2);
+    } else {
+        h[0] = wp.vf == 3 ? cos(PI * t / 5.0) : 1.0;
+        h[1] = h[2] = h[3] = 0.0;
+    }
+}
+
+// coefficient field m on the interior edges (the other entries of u, v are left as they are)
+template <class W>
+__global__ void k_wind_basis(Grid g, WindParams wp, int m, int tkind, W *u, W *v) {
+    const Dims d = g.d;
+    const int N = d.N;
+    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long per = (long long)(N + 1) * N;
+    if (tid >= 2 * NFACE * per) return;
+    int which = (int)(tid / (NFACE * per));
+    long long r = tid % (NFACE * per);
+    int p = (int)(r / per);
+    int a = (int)((r % per) / N), b = (int)(r % N);
+    int i = which == 0 ? d.i0 + a : d.i0 + b;
+    int j = which == 0 ? d.i0 + b : d.i0 + a;
+    long long o = at(d, p, i, j);
+    const double *lon = which == 0 ? g.lon_pu : g.lon_pv, *lat = which == 0 ? g.lat_pu : g.lat_pv;
+    const double *const *cf = which == 0 ? g.cu : g.cv;
+    // contravariant = a * ulon + b * vlat  (sphgeo.py:120-125)
+    const double ca = which == 0 ? cf[3][o] / cf[4][o] : -cf[1][o] / cf[4][o];
+    const double cb = which == 0 ? -cf[2][o] / cf[4][o] : cf[0][o] / cf[4][o];
+    double c;
+    if (tkind == 1) {
+        const double L = lon[o], P = lat[o];
+        const double Tp = wp.vf == 2 ? 5.0 : wp.prm[1];
+        const double s2p = sin(2.0 * P), cp = cos(P), s2l = sin(2.0 * L), c2l = cos(2.0 * L);
+        switch (m) {
+            case 0: c = ca * (2.0 * PI / Tp) * cp; break;
+            case 1: c = ca * 0.5 * s2p; break;
+            case 2: c = -ca * 0.5 * s2p * c2l + cb * cp * s2l; break;
+            default: c = -ca * 0.5 * s2p * s2l - cb * cp * c2l; break;
+        }
+    } else {
+        double ulon, vlat;
+        wind_latlon(wp.vf, wp.prm, lon[o], lat[o], 0.0, ulon, vlat);  // vf 3 at t = 0 (h = 1); vf 4
+        c = ca * ulon + cb * vlat;
+    }
+    (which == 0 ? u : v)[o] = (W)c;
+}
+
+// the basis coefficients of edge o (M = 4: one vector load)
+template <class W, int M>
+struct Coefs {
+    W c[M];
+    __device__ __forceinline__ Coefs(const W *__restrict__ B, long long o) {
+        if constexpr (M == 4) {
+            if constexpr (sizeof(W) == 4) {
+                const float4 v = *reinterpret_cast<const float4 *>(B + o * 4);
+                c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+            } else {
+                const double2 a = *reinterpret_cast<const double2 *>(B + o * 4);
+                const double2 b = *reinterpret_cast<const double2 *>(B + o * 4 + 2);
+                c[0] = a.x; c[1] = a.y; c[2] = b.x; c[3] = b.y;
+            }
+        } else {
+#pragma unroll
+            for (int m = 0; m < M; ++m) c[m] = B[o * M + m];
+        }
+    }
+    __device__ __forceinline__ W at(const W *h) const {
+        W s = W(0);
+#pragma unroll
+        for (int m = 0; m < M; ++m) s += c[m] * h[m];
+        return s;
+    }
+};
+
+// edge records of one step from the basis (the wind at the clock's current and previous
+// times): x-edges natural, y-edges transposed (as k_wind_avgprep_t).  Block (32, 8) covers a 32 x 32 (i, j) tile; the
+// wind and its RK2 extrapolation are evaluated once per edge (tile + one row / column of
+// neighbours) into shared memory, then averaged.
+template <class W, int M, class V>
+__global__ void k_wind_step(Dims d, const W *__restrict__ bu, const W *__restrict__ bv, const Clock *__restrict__ clk,
+                            const W *__restrict__ gpu, const W *__restrict__ gpvT, V *erx, V *ery, int rk2, W dto2,
+                            W dx) {
+    __shared__ W hn[4], ho[4];
+    __shared__ W xs[34][32], ys[32][35];  // extrapolated winds: x-edges rows ib-1.., y-edges cols jb-1..
+    __shared__ W xn[32][32], yn[32][33];  // winds now
+    __shared__ W tv[32][33];
+    __shared__ unsigned char tf[32][33];
+    const int p = blockIdx.z, jb = blockIdx.x * 32, ib = blockIdx.y * 32;
+    const int lane = threadIdx.x, wy = threadIdx.y, tid = wy * 32 + lane;
+    if (tid < 8) (tid < 4 ? hn : ho)[tid & 3] = (W)(tid < 4 ? clk->hn[tid] : clk->ho[tid - 4]);
+    __syncthreads();
+    // the wind now and 1.5 u - 0.5 u_old (the RK2 extrapolation) of edge (i, j), zero outside the plane
+    for (int e = tid; e < 34 * 32; e += 256) {
+        const int r = e >> 5, c = e & 31, i = ib - 1 + r, j = jb + c;
+        W sn = W(0), so = W(0);
+        if (i >= 0 && i <= d.n && j < d.pitch) {
+            const Coefs<W, M> cf(bu, at(d, p, i, j));
+            sn = cf.at(hn);
+            so = cf.at(ho);
+        }
+        xs[r][c] = W(1.5) * sn - W(0.5) * so;
+        if (r >= 1 && r <= 32) xn[r - 1][c] = sn;
+    }
+    for (int e = tid; e < 32 * 34; e += 256) {
+        const int r = e / 34, c = e - r * 34, i = ib + r, j = jb - 1 + c;
+        W sn = W(0), so = W(0);
+        if (i <= d.n && j >= 0 && j < d.pitch) {
+            const Coefs<W, M> cf(bv, at(d, p, i, j));
+            sn = cf.at(hn);
+            so = cf.at(ho);
+        }
+        ys[r][c] = W(1.5) * sn - W(0.5) * so;
+        if (c >= 1 && c <= 32) yn[r][c - 1] = sn;
+    }
+    __syncthreads();
+    // averaged_velocity.py:14-62, given the wind and the three extrapolated winds along the line
+    auto average = [&](W u, W sm, W s0, W sp) {
+        const W a = u * dto2 / dx;
+        return (u >= W(0)) ? (W(1.0) - a) * s0 + a * sm : -a * sp + (W(1.0) + a) * s0;
+    };
+    for (int k = 0; k < 4; ++k) {
+        const int r = wy + 8 * k, i = ib + r, j = jb + lane;
+        const bool ok = i <= d.n && j < d.pitch;
+        const W u = xn[r][lane], v = yn[r][lane];
+        W au = u, av = v;
+        if (rk2) {
+            au = (j < d.n && i >= d.i0 && i <= d.iend) ? average(u, xs[r][lane], xs[r + 1][lane], xs[r + 2][lane])
+                                                       : W(0);
+            av = (i < d.n && j >= d.i0 && j <= d.iend) ? average(v, ys[r][lane], ys[r][lane + 1], ys[r][lane + 2])
+                                                       : W(0);
+        }
+        if (ok) erx[at(d, p, i, j)] = edge_record<V>(au, gpu[at2(d, i, j)], u >= W(0));
+        tv[r][lane] = av;
+        tf[r][lane] = (ok && v >= W(0)) ? 1 : 0;
+    }
+    __syncthreads();
+    for (int k = 0; k < 4; ++k) {
+        const int c = wy + 8 * k, j = jb + c, i = ib + lane;
+        if (j <= d.n && i < d.pitch) ery[at(d, p, j, i)] = edge_record<V>(tv[lane][c], gpvT[at2(d, j, i)], tf[lane][c] != 0);
+    }
+}
+
+// u, v <- the wind at the clock's current time, u_old, v_old <- at its previous time, on every
+// edge of the basis (for the staged operators used on a fused plan, e.g. csadv_divergence)
+template <class W>
+__global__ void k_wind_sync(Dims d, const W *__restrict__ bu, const W *__restrict__ bv, int M, WindParams wp,
+                            int tkind, const Clock *__restrict__ clk, W *u, W *v, W *uo, W *vo) {
+    __shared__ W hn[4], ho[4];
+    if (threadIdx.x < 8) (threadIdx.x < 4 ? hn : ho)[threadIdx.x & 3] =
+        (W)(threadIdx.x < 4 ? clk->hn[threadIdx.x] : clk->ho[threadIdx.x - 4]);
+    __syncthreads();
+    const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (o >= d.field) return;
+    W a = W(0), b = W(0), ao = W(0), bo = W(0);
+    for (int m = 0; m < M; ++m) {
+        const W cu = bu[o * M + m], cv = bv[o * M + m];
+        a += cu * hn[m];
+        b += cv * hn[m];
+        ao += cu * ho[m];
+        bo += cv * ho[m];
+    }
+    u[o] = a;
+    v[o] = b;
+    uo[o] = ao;
+    vo[o] = bo;
 }
 
 // update_adv: old <- current everywhere; current <- wind(t) on interior edges; non-interior
@@ -369,14 +583,14 @@ __global__ void k_wind_avgprep(Dims d, const W *__restrict__ U, const W *__restr
     }
 }
 
-// As k_wind_avgprep, for the line-marching kernel: x-edge winds and flags in the natural
-// layout, y-edge winds and flags transposed (row j, column i) through a shared 32 x 32 tile,
-// so that both stores stay coalesced.  Block (32, 8) covers rows i in [32 by, 32 by + 32) and
-// columns j in [32 bx, 32 bx + 32) of one panel plane.
-template <class W>
-__global__ void k_wind_avgprep_t(Dims d, const W *__restrict__ U, const W *__restrict__ Uo, const W *__restrict__ V,
-                                 const W *__restrict__ Vo, W *ua, W *vaT, uint32_t *ubits, uint32_t *vbitsT,
-                                 int wpitch, int rk2, W dto2, W dx) {
+// As k_wind_avgprep, for the line-marching kernel: edge records {departure-point wind, +-g},
+// x-edges in the natural layout, y-edges transposed (row j, column i) through a shared 32 x 32
+// tile, so that both stores stay coalesced.  Block (32, 8) covers rows i in [32 by, 32 by + 32)
+// and columns j in [32 bx, 32 bx + 32) of one panel plane.
+template <class W, class V>
+__global__ void k_wind_avgprep_t(Dims d, const W *__restrict__ U, const W *__restrict__ Uo, const W *__restrict__ V_,
+                                 const W *__restrict__ Vo, const W *__restrict__ gpu, const W *__restrict__ gpvT, V *erx,
+                                 V *ery, int rk2, W dto2, W dx) {
     __shared__ W tv[32][33];
     __shared__ unsigned char tf[32][33];
     const int p = blockIdx.z, jb = blockIdx.x * 32, ib = blockIdx.y * 32;
@@ -384,31 +598,26 @@ __global__ void k_wind_avgprep_t(Dims d, const W *__restrict__ U, const W *__res
     for (int k = 0; k < 4; ++k) {
         const int r = wy + 8 * k, i = ib + r, j = jb + lane;
         const bool ok = i <= d.n && j < d.pitch;
-        W u = W(0), v = W(0), av = W(0);
+        W v = W(0), av = W(0);
         if (ok) {
             const long long t = at(d, p, i, j);
-            u = U[t];
-            v = V[t];
+            const W u = U[t];
+            v = V_[t];
             W au = u;
             av = v;
             if (rk2) {
                 au = (j < d.n && i >= d.i0 && i <= d.iend) ? rk2_average(U, Uo, d, p, i, j, 0, dto2, dx) : W(0);
-                av = (i < d.n && j >= d.i0 && j <= d.iend) ? rk2_average(V, Vo, d, p, i, j, 1, dto2, dx) : W(0);
+                av = (i < d.n && j >= d.i0 && j <= d.iend) ? rk2_average(V_, Vo, d, p, i, j, 1, dto2, dx) : W(0);
             }
-            ua[t] = au;
+            erx[t] = edge_record<V>(au, gpu[at2(d, i, j)], u >= W(0));
         }
-        const unsigned bu = __ballot_sync(0xffffffffu, ok && u >= W(0));
-        if (ok && lane == 0) ubits[((long long)p * (d.n + 1) + i) * wpitch + (j >> 5)] = bu;
         tv[r][lane] = av;
         tf[r][lane] = (ok && v >= W(0)) ? 1 : 0;
     }
     __syncthreads();
     for (int k = 0; k < 4; ++k) {
         const int c = wy + 8 * k, j = jb + c, i = ib + lane;
-        const bool ok = j <= d.n && i < d.pitch;
-        if (ok) vaT[at(d, p, j, i)] = tv[lane][c];
-        const unsigned bv = __ballot_sync(0xffffffffu, ok && tf[lane][c]);
-        if (ok && lane == 0) vbitsT[((long long)p * (d.n + 1) + j) * wpitch + (i >> 5)] = bv;
+        if (j <= d.n && i < d.pitch) ery[at(d, p, j, i)] = edge_record<V>(tv[lane][c], gpvT[at2(d, j, i)], tf[lane][c] != 0);
     }
 }
 
@@ -490,7 +699,7 @@ static int setup_t(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, 
     for (void **p : wa) CSADV_CUDA(cudaMemsetAsync(*p, 0, F * sizeof(W), st));
     CSADV_CUDA(cudaMemsetAsync(cen, 0, 2 * F * sizeof(W), st));
     w.clock = clk;
-    Clock h{0, dt, 0.0, {0.0, 0.0, 0.0, 0.0}};
+    Clock h{0, dt, 0.0, {0.0, 0.0, 0.0, 0.0}, 0.0};
     CSADV_CUDA(cudaMemcpyAsync(clk, &h, sizeof(Clock), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaStreamSynchronize(st));
     if (!wind_time_dependent(o)) {
@@ -518,7 +727,8 @@ static int initial_t(const Options &o, const Grid &g, Winds &w, cudaStream_t st)
         long long tot = 2LL * NFACE * (d.N + 1) * d.N;
         k_wind_interior<W><<<ceil_div(tot, 128), 128, 0, st>>>(g, (W *)w.u_pu, (W *)w.v_pv, wparams(o), 0.0);
     } else {
-        k_clock_set<<<1, 1, 0, st>>>((Clock *)w.clock, 0, 0.0, wparams(o), w.tkind);
+        k_clock_set<<<1, 1, 0, st>>>((Clock *)w.clock, 0, 0.0, wparams(o), w.tkind, 1);
+        if (w.nbasis) k_clock_set<<<1, 1, 0, st>>>((Clock *)w.clock, 0, 0.0, wparams(o), w.tkind, 0);
         k_wind_update<W><<<plane_grid(d, 128), 128, 0, st>>>(d, (W *)w.u_pu, (W *)w.v_pv, (W *)w.u_old, (W *)w.v_old,
                                                             (const W *)w.tab[0], (const W *)w.tab[1], w.tkind,
                                                             (const Clock *)w.clock, 0);
@@ -530,10 +740,12 @@ static int initial_t(const Options &o, const Grid &g, Winds &w, cudaStream_t st)
 template <class W>
 static int update_t(const Options &o, const Grid &g, Winds &w, bool tick, long long k, double t, cudaStream_t st) {
     const Dims d = g.d;
+    if (w.tkind == 0) return CSADV_OK;  // static wind: nothing changes with time
     Clock *clk = (Clock *)w.clock;
-    if (tick) k_clock_tick<<<1, 1, 0, st>>>(clk, wparams(o), w.tkind);
-    else k_clock_set<<<1, 1, 0, st>>>(clk, k, t, wparams(o), w.tkind);
-    if (w.tkind != 0)
+    const int factors = w.nbasis == 0;
+    if (tick) k_clock_tick<<<1, 1, 0, st>>>(clk, wparams(o), w.tkind, factors);
+    else k_clock_set<<<1, 1, 0, st>>>(clk, k, t, wparams(o), w.tkind, factors);
+    if (w.nbasis == 0)  // with the basis, the step evaluates the wind itself
         k_wind_update<W><<<plane_grid(d, 128), 128, 0, st>>>(d, (W *)w.u_pu, (W *)w.v_pv, (W *)w.u_old, (W *)w.v_old,
                                                             (const W *)w.tab[0], (const W *)w.tab[1], w.tkind, clk,
                                                             o.et != ET_DG);
@@ -625,21 +837,96 @@ int wind_avgprep(const Options &o, const Grid &g, const Winds &w, double dt, rea
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
-template <class real>
-int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, real *ua, real *vaT, uint32_t *ub,
-                   uint32_t *vbT, int wpitch, cudaStream_t st) {
+// dst[o * M + m] = src[o]: the basis coefficients of an edge side by side (one vector load)
+template <class W>
+__global__ void k_interleave(const W *__restrict__ src, W *dst, long long n, int M, int m) {
+    const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (o < n) dst[o * M + m] = src[o];
+}
+
+template <class W>
+static int basis_setup_t(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, cudaStream_t st) {
+    const Dims d = g.d;
+    const int M = wind_nbasis(w.tkind);
+    if (M == 0 || o.et != ET_DG) return CSADV_OK;
+    for (int c = 0; c < 2; ++c) w.btab[c] = mem.alloc<W>((long long)M * d.field);
+    if (!mem.ok()) return CSADV_ERR_OOM;
+    const size_t F = (size_t)d.field * sizeof(W);
+    const long long tot = 2LL * NFACE * (d.N + 1) * d.N;
+    for (int m = 0; m < M; ++m) {
+        // the halo of coefficient field m, computed with the reference's wind-halo operators
+        CSADV_CUDA(cudaMemsetAsync(w.u_pu, 0, F, st));
+        CSADV_CUDA(cudaMemsetAsync(w.v_pv, 0, F, st));
+        k_wind_basis<W><<<ceil_div(tot, 128), 128, 0, st>>>(g, wparams(o), m, w.tkind, (W *)w.u_pu, (W *)w.v_pv);
+        CSADV_CUDA(cudaGetLastError());
+        int rc = wind_halo(o, g, w, st);
+        if (rc) return rc;
+        const int nb = ceil_div(d.field, 256);
+        k_interleave<W><<<nb, 256, 0, st>>>((const W *)w.u_pu, (W *)w.btab[0], d.field, M, m);
+        k_interleave<W><<<nb, 256, 0, st>>>((const W *)w.v_pv, (W *)w.btab[1], d.field, M, m);
+        CSADV_CUDA(cudaGetLastError());
+    }
+    CSADV_CUDA(cudaMemsetAsync(w.u_pu, 0, F, st));
+    CSADV_CUDA(cudaMemsetAsync(w.v_pv, 0, F, st));
+    w.nbasis = M;
+    return CSADV_OK;  // the clock's basis values are set by wind_initial (k_clock_set)
+}
+
+int wind_basis_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, cudaStream_t st) {
+    return o.precision == 64 ? basis_setup_t<double>(o, g, w, mem, st) : basis_setup_t<float>(o, g, w, mem, st);
+}
+
+template <class real, class V>
+int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
+              V *ery, cudaStream_t st) {
     const Dims d = g.d;
     dim3 grid(d.pitch / 32, ceil_div(d.n + 1, 32), NFACE);
-    k_wind_avgprep_t<real><<<grid, dim3(32, 8), 0, st>>>(d, (const real *)w.u_pu, (const real *)w.u_old,
-                                                          (const real *)w.v_pv, (const real *)w.v_old, ua, vaT, ub,
-                                                          vbT, wpitch, o.dp == 2, (real)(dt * 0.5), (real)g.dx);
+    const real *bu = (const real *)w.btab[0], *bv = (const real *)w.btab[1];
+    const Clock *clk = (const Clock *)w.clock;
+    if (w.nbasis == 4)
+        k_wind_step<real, 4, V><<<grid, dim3(32, 8), 0, st>>>(d, bu, bv, clk, gpu, gpvT, erx, ery, o.dp == 2,
+                                                               (real)(dt * 0.5), (real)g.dx);
+    else
+        k_wind_step<real, 1, V><<<grid, dim3(32, 8), 0, st>>>(d, bu, bv, clk, gpu, gpvT, erx, ery, o.dp == 2,
+                                                               (real)(dt * 0.5), (real)g.dx);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
-template int wind_avgprep_t<double>(const Options &, const Grid &, const Winds &, double, double *, double *,
-                                    uint32_t *, uint32_t *, int, cudaStream_t);
-template int wind_avgprep_t<float>(const Options &, const Grid &, const Winds &, double, float *, float *, uint32_t *,
-                                   uint32_t *, int, cudaStream_t);
+template int wind_step<double, double2>(const Options &, const Grid &, const Winds &, double, const double *,
+                                        const double *, double2 *, double2 *, cudaStream_t);
+template int wind_step<float, float2>(const Options &, const Grid &, const Winds &, double, const float *,
+                                      const float *, float2 *, float2 *, cudaStream_t);
+
+template <class W>
+static int sync_t(const Options &o, const Grid &g, const Winds &w, cudaStream_t st) {
+    const Dims d = g.d;
+    k_wind_sync<W><<<ceil_div(d.field, 256), 256, 0, st>>>(d, (const W *)w.btab[0], (const W *)w.btab[1], w.nbasis,
+                                                            wparams(o), w.tkind, (const Clock *)w.clock, (W *)w.u_pu,
+                                                            (W *)w.v_pv, (W *)w.u_old, (W *)w.v_old);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+int wind_sync(const Options &o, const Grid &g, const Winds &w, cudaStream_t st) {
+    if (w.nbasis == 0) return CSADV_OK;
+    return o.precision == 64 ? sync_t<double>(o, g, w, st) : sync_t<float>(o, g, w, st);
+}
+
+template <class real, class V>
+int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT,
+                   V *erx, V *ery, cudaStream_t st) {
+    const Dims d = g.d;
+    dim3 grid(d.pitch / 32, ceil_div(d.n + 1, 32), NFACE);
+    k_wind_avgprep_t<real, V><<<grid, dim3(32, 8), 0, st>>>(d, (const real *)w.u_pu, (const real *)w.u_old,
+                                                             (const real *)w.v_pv, (const real *)w.v_old, gpu, gpvT,
+                                                             erx, ery, o.dp == 2, (real)(dt * 0.5), (real)g.dx);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+template int wind_avgprep_t<double, double2>(const Options &, const Grid &, const Winds &, double, const double *,
+                                             const double *, double2 *, double2 *, cudaStream_t);
+template int wind_avgprep_t<float, float2>(const Options &, const Grid &, const Winds &, double, const float *,
+                                           const float *, float2 *, float2 *, cudaStream_t);
 template int wind_avgprep<double>(const Options &, const Grid &, const Winds &, double, double *, double *, uint32_t *,
                                   uint32_t *, int, cudaStream_t);
 template int wind_avgprep<float>(const Options &, const Grid &, const Winds &, double, float *, float *, uint32_t *,

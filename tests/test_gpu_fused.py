@@ -165,3 +165,17 @@ def test_fp32_staged_and_fused_agree():
             pl.advance(20)
             outs.append(pl.get_tracer())
     assert rel(outs[1], outs[0]) < 1e-5
+
+
+def test_fp32_mass_anchored_over_long_run():
+    # FP32 state with MF-PR: the correction restores each tracer's sum(Q g) as it was set, so
+    # the mass stays within 1e-6 relative over thousands of steps (without the anchor, FP32
+    # rounding of the update makes it drift like a random walk)
+    c = (2, 2, 1, 3, 1, 3)
+    with plan(32, -0.5, c, 102, precision=32, wind_param=(0.48, 5.0, 0, 0), ntracers=2) as pl:
+        pl.init_tracer(101, ic_param=(0.3, 0.2, 5.0, 0.0), tracer=0)
+        pl.init_tracer(102, tracer=1)
+        m0 = [pl.mass(t) for t in range(2)]
+        pl.advance(2000)
+        for t in range(2):
+            assert abs(pl.mass(t) - m0[t]) <= 1e-6 * abs(m0[t])
