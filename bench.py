@@ -60,7 +60,7 @@ def dt_for_cfl(make_plan):
 def profiled_traffic(key):
     """DRAM bytes (read + write) of one launch of the step kernel on this workload, from the
     committed ncu summary (a `key = value` line); None when absent."""
-    path = os.path.join(ROOT, "profiles", "k_fused_N384_T2.md")
+    path = os.path.join(ROOT, "profiles", "k_sweep_N384_T2.md")
     try:
         for ln in open(path):
             if ln.strip().startswith(key + " ="):
@@ -419,7 +419,7 @@ def bench_gpu(args):
     alg = 6 * N_CELLS * N_CELLS * (NTRACERS * 2 * s_q + 3 * 4)
     kms = f32["kernel_ms"]
     achieved = alg / (kms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_fused<float, PPM-CW84>", "achieved": round(achieved, 1),
+    roof = {"bound": "hbm", "kernel": "k_sweep<float, PPM-CW84, AVLT>", "achieved": round(achieved, 1),
             "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
             "traffic": None, "kernel_ms": round(kms, 5), "alg_bytes_per_launch": alg,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}

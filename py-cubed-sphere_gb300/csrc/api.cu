@@ -296,8 +296,8 @@ IcParams ic_params(const csadv_plan *pl, const double *ic_param) {
 
 namespace csadv {
 
-int plan_pre_step(csadv_plan *pl, cudaStream_t st) {
-    int rc = fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
+int plan_pre_step(csadv_plan *pl, cudaStream_t st, bool ghosts) {
+    int rc = ghosts ? fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st) : CSADV_OK;
     if (!rc && wind_time_dependent(pl->opt)) {
         if (!pl->w.nbasis) rc = wind_halo(pl->opt, pl->grid, pl->w, st);
         if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);

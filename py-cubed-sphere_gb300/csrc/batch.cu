@@ -3,9 +3,9 @@
 // A batch advances every attached plan by one step per step with ONE launch of the
 // line-marching step kernel for all of them: each plan contributes its own descriptor
 // (two, one per buffer parity) and its tiles to a work table, so solves of different N,
-// tracer counts, winds and tile shapes share the launch.  The per-plan work around the
-// kernel (ghost cells; for time-dependent winds the wind halo, departure-point winds and the
-// next wind update) is launched per plan on the same stream.  A step is captured as a CUDA
+// tracer counts, winds and tile shapes share the launch.  The ghost cells of all solves are
+// filled by one launch too (a second work table over the same descriptors); only the wind
+// work of time-dependent winds (one wind pass and the next clock tick) is launched per plan.  A step is captured as a CUDA
 // graph per parity and replayed while the membership does not change.
 //
 // Results: the kernel's MF-PR sums run in a fixed order per solve (its tiles, then its
@@ -28,10 +28,11 @@ struct csadv_batch {
     std::vector<int> base_cur;       // each plan's buffer parity when the tables were built
     csadv::DeviceArena mem;
     SweepSolve *dsolves = nullptr;   // [capacity][2]
-    int2 *dwork[2] = {nullptr, nullptr};
-    void *work_mem = nullptr;        // both tables, grown on demand
+    int2 *dwork[2] = {nullptr, nullptr};   // step-kernel work tables (per phase)
+    int2 *dhwork[2] = {nullptr, nullptr};  // ghost-cell work tables (per phase)
+    void *work_mem = nullptr;        // all four tables, grown on demand
     int work_cap = 0;                // entries per table
-    int nwork = 0;
+    int nwork = 0, nhwork = 0;
     size_t smem = 0;
     int precision = 0, recon = 0, split = 0;
     int phase = 0;                   // steps since the tables were built, mod 2
@@ -87,40 +88,55 @@ int batch_rebuild(csadv_batch *b, cudaStream_t st) {
     for (int m = 0; m < M; ++m) order[m] = m;
     std::stable_sort(order.begin(), order.end(),
                      [&](int x, int y) { return b->plans[x]->f.nitems > b->plans[y]->f.nitems; });
-    int total = 0;
+    int total = 0, htotal = 0;
     for (int m = 0; m < M; ++m) {
         csadv_plan *pl = b->plans[m];
         CSADV_CUDA(cudaMemcpyAsync(b->dsolves + 2 * m, pl->f.dsolve, 2 * sizeof(SweepSolve), cudaMemcpyDeviceToDevice,
                                    st));
         b->base_cur.push_back(pl->cur);
         total += pl->f.nitems;
+        htotal += pl->T * halo_blocks(pl->grid.d);
         b->smem = b->smem > pl->f.smem ? b->smem : pl->f.smem;
     }
-    if (total > b->work_cap) {
+    const int need = total > htotal ? total : htotal;
+    if (need > b->work_cap) {
         if (b->work_mem) {
             CSADV_CUDA(cudaStreamSynchronize(st));
             CSADV_CUDA(cudaFree(b->work_mem));
             b->work_mem = nullptr;
         }
-        int cap = total + total / 2 + 64;
-        CSADV_CUDA(cudaMalloc(&b->work_mem, 2 * (size_t)cap * sizeof(int2)));
+        int cap = need + need / 2 + 64;
+        CSADV_CUDA(cudaMalloc(&b->work_mem, 4 * (size_t)cap * sizeof(int2)));
         b->work_cap = cap;
         b->dwork[0] = (int2 *)b->work_mem;
         b->dwork[1] = b->dwork[0] + cap;
+        b->dhwork[0] = b->dwork[1] + cap;
+        b->dhwork[1] = b->dhwork[0] + cap;
     }
-    std::vector<int2> h(2 * (size_t)total);
-    int e = 0;
+    // step kernel: the tiles of each solve, largest solves first; ghost cells: per solve and
+    // tracer the blocks of its ghost-cell strip
+    std::vector<int2> h(2 * (size_t)total), hh(2 * (size_t)htotal);
+    int e = 0, eh = 0;
     for (int m : order) {
         const csadv_plan *pl = b->plans[m];
         for (int it = 0; it < pl->f.nitems; ++it, ++e) {
             h[e] = make_int2(2 * m + pl->cur, it);
             h[total + e] = make_int2(2 * m + (1 - pl->cur), it);
         }
+        const int hb = pl->T * halo_blocks(pl->grid.d);
+        for (int it = 0; it < hb; ++it, ++eh) {
+            hh[eh] = make_int2(2 * m + pl->cur, it);
+            hh[htotal + eh] = make_int2(2 * m + (1 - pl->cur), it);
+        }
     }
     CSADV_CUDA(cudaMemcpyAsync(b->dwork[0], h.data(), (size_t)total * sizeof(int2), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(b->dwork[1], h.data() + total, (size_t)total * sizeof(int2), cudaMemcpyHostToDevice, st));
-    CSADV_CUDA(cudaStreamSynchronize(st));  // h goes out of scope
+    CSADV_CUDA(cudaMemcpyAsync(b->dhwork[0], hh.data(), (size_t)htotal * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaMemcpyAsync(b->dhwork[1], hh.data() + htotal, (size_t)htotal * sizeof(int2), cudaMemcpyHostToDevice,
+                               st));
+    CSADV_CUDA(cudaStreamSynchronize(st));  // h, hh go out of scope
     b->nwork = total;
+    b->nhwork = htotal;
     b->precision = b->plans.front()->opt.precision;
     b->recon = b->plans.front()->opt.recon;
     b->split = b->plans.front()->opt.opsplit;
@@ -137,8 +153,12 @@ bool batch_stale(const csadv_batch *b) {
 }
 
 int batch_step_work(csadv_batch *b, int kind, cudaStream_t st) {
+    // ghost cells of every solve in one launch, then each plan's wind work (time-dependent winds)
+    int rc0 = b->precision == 64 ? launch_halo_batch<double>(b->dsolves, b->dhwork[b->phase], b->nhwork, st)
+                                 : launch_halo_batch<float>(b->dsolves, b->dhwork[b->phase], b->nhwork, st);
+    if (rc0) return rc0;
     for (csadv_plan *pl : b->plans) {
-        int rc = plan_pre_step(pl, st);
+        int rc = plan_pre_step(pl, st, false);
         if (rc) return rc;
     }
     if (b->prof) CSADV_CUDA(cudaEventRecord(b->pev[0], st));

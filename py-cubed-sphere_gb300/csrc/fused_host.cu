@@ -239,6 +239,8 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.mass_target = f.mass_target;
         s.lag_w = f.inline_ghosts ? g.lag_w : nullptr;
         s.lag_k = f.inline_ghosts ? g.lag_k : nullptr;
+        s.hlag_w = g.lag_w;
+        s.hlag_k = g.lag_k;
     }
     f.nitems = NFACE * h[0].ntiles;
     f.smem = o.precision == 64 ? sweep_smem_bytes<double>(f.scfg) : sweep_smem_bytes<float>(f.scfg);

@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "halo.cuh"
 #include "internal.h"
+#include "tiles.h"
 
 namespace csadv {
 
@@ -43,6 +44,43 @@ __global__ void k_halo_dg(real *F0, long long fstride, Dims d, const double *__r
     if (s == SIDE_N || s == SIDE_S) return;  // corner blocks are filled from the E/W sides
     F[at(d, p, gi, gj)] = (real)ghost_value(S, d, W, K, p, gi, gj);
 }
+
+// ghost cells of many solves in one launch: item (s, b) of the work table is block b % nb of
+// tracer b / nb of solve s (descriptor s: its input buffer and pending correction), nb =
+// halo_blocks; the same work per thread as k_halo_dg
+template <class real>
+__global__ void k_halo_batch(const SweepSolve *__restrict__ solves, const int2 *__restrict__ work, int nwork) {
+    for (int wk = blockIdx.x; wk < nwork; wk += gridDim.x) {
+        const int2 it = work[wk];
+        const SweepSolve &S = solves[it.x];
+        const Dims d = S.d;
+        const int n = d.n, nb = halo_blocks(d);
+        const int tr = it.y / nb;
+        const int tid = (it.y % nb) * 128 + threadIdx.x;
+        if (tid >= NFACE * 4 * NG * n) continue;
+        real *F = (real *)S.Qin + (long long)tr * d.field;
+        const bool hc = S.corr_in != nullptr;
+        Src<real> src{F, (const real *)S.gpc, hc ? (real)S.corr_in[tr] : real(0), hc};
+        const int k = tid % n, dep = (tid / n) % NG, s = (tid / (n * NG)) % 4, p = tid / (n * NG * 4);
+        int gi, gj;
+        ghost_ij(d, s, dep, k, gi, gj);
+        if (is_interior(d, k)) {
+            F[at(d, p, gi, gj)] = (real)side_ghost(src, d, S.hlag_w, S.hlag_k, p, s, dep, k);
+        } else if (s == SIDE_E || s == SIDE_W) {  // corner blocks, from the E/W sides
+            F[at(d, p, gi, gj)] = (real)ghost_value(src, d, S.hlag_w, S.hlag_k, p, gi, gj);
+        }
+    }
+}
+
+template <class real>
+int launch_halo_batch(const SweepSolve *dsolves, const int2 *work, int nwork, cudaStream_t st) {
+    if (nwork <= 0) return CSADV_OK;
+    k_halo_batch<real><<<nwork, 128, 0, st>>>(dsolves, work, nwork);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+template int launch_halo_batch<double>(const SweepSolve *, const int2 *, int, cudaStream_t);
+template int launch_halo_batch<float>(const SweepSolve *, const int2 *, int, cudaStream_t);
 
 template <class real>
 __global__ void k_halo_adjacent(real *Qx, real *Qy, Dims d) {

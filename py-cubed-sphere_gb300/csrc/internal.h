@@ -75,6 +75,8 @@ bool wind_time_dependent(const Options &o);
 int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st);
 std::vector<double> linspace(double start, double stop, int num);
 
+struct SweepSolve;
+
 // Per-tracer scratch of the staged engine (type-erased; element type = real)
 struct Scratch {
     void *Qx, *Qy, *qLx, *qRx, *qLy, *qRy, *fx, *fy, *div;
@@ -85,6 +87,9 @@ template <class real> int launch_halo_dg(real *F, const Grid &g, cudaStream_t st
 template <class real> int launch_halo_adjacent(real *Qx, real *Qy, const Grid &g, cudaStream_t st);
 template <class real>
 int launch_halo_dg_tracers(real *F, int T, const Grid &g, const double *corr, const real *greal, cudaStream_t st);
+// ghost cells of the input buffers of many solves (work items: solve descriptor, block)
+template <class real>
+int launch_halo_batch(const SweepSolve *dsolves, const int2 *work, int nwork, cudaStream_t st);
 template <class real>
 int staged_divergence(const Options &o, const Grid &g, const Winds &w, double dt, real *Q, const Scratch &s,
                       double *partials, int npart, cudaStream_t st);
@@ -116,7 +121,6 @@ int wind_avgprep(const Options &o, const Grid &g, const Winds &w, double dt, rea
 int wind_cfl(const Options &o, const Grid &g, const Winds &w, double dt, double *dev_tmp, double &cfl, cudaStream_t st);
 
 // ---------------------------------------------------------------- fused engine state
-struct SweepSolve;
 struct FusedState {
     bool on = false;
     int tile = 1;               // 0-3: k_fused (FUSED_TILES), 4-7: k_sweep (SWEEP_TILES[tile - 4])

@@ -82,7 +82,7 @@ namespace csadv {
 // the plan's fused-step work split for batches: per-plan work before the step kernel (ghost
 // cells; for time-dependent winds the wind halo and departure-point winds) and after it
 // (kind 1: the wind update of the next step); single stream
-int plan_pre_step(csadv_plan *pl, cudaStream_t st);
+int plan_pre_step(csadv_plan *pl, cudaStream_t st, bool ghosts = true);
 int plan_post_step(csadv_plan *pl, int kind, cudaStream_t st);
 int plan_select_device(csadv_plan *pl);
 int graph_kernel_nodes(cudaGraph_t g);

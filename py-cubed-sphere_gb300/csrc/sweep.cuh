@@ -41,6 +41,36 @@ __device__ __forceinline__ real csign(real a, real b) { return copysign(a, b); }
 template <>
 __device__ __forceinline__ float csign<float>(float a, float b) { return copysignf(a, b); }
 
+// Decisions of the limiters.  GB300 runs FP64 arithmetic at 1/64 of the FP32 rate, so in FP64
+// the comparisons and minima are taken on the bit patterns with integer instructions, leaving
+// the FP64 pipe to the arithmetic.  The results equal the floating-point ones for finite
+// inputs (the sign of a product differs only if the product of two non-zero values underflows
+// to zero).
+template <class real>
+struct Pred {
+    __device__ static __forceinline__ bool prod_pos(real a, real b) { return a * b > real(0); }
+    __device__ static __forceinline__ bool prod_nonpos(real a, real b) { return a * b <= real(0); }
+    __device__ static __forceinline__ bool abs_lt(real a, real b) { return RealOps<real>::ab(a) < RealOps<real>::ab(b); }
+    // a, b >= 0
+    __device__ static __forceinline__ real min_nonneg(real a, real b) { return RealOps<real>::fmn(a, b); }
+    // p > d and p < -d, with d >= 0
+    __device__ static __forceinline__ bool gt_nonneg(real p, real d) { return p > d; }
+    __device__ static __forceinline__ bool lt_neg(real p, real d) { return -d > p; }
+};
+template <>
+struct Pred<double> {
+    static constexpr long long MAG = 0x7fffffffffffffffLL;
+    __device__ static __forceinline__ long long b(double x) { return __double_as_longlong(x); }
+    __device__ static __forceinline__ bool prod_pos(double x, double y) {
+        return (b(x) ^ b(y)) >= 0 && (b(x) & MAG) != 0 && (b(y) & MAG) != 0;
+    }
+    __device__ static __forceinline__ bool prod_nonpos(double x, double y) { return !prod_pos(x, y); }
+    __device__ static __forceinline__ bool abs_lt(double x, double y) { return (b(x) & MAG) < (b(y) & MAG); }
+    __device__ static __forceinline__ double min_nonneg(double x, double y) { return b(x) < b(y) ? x : y; }
+    __device__ static __forceinline__ bool gt_nonneg(double p, double d) { return b(p) > b(d); }
+    __device__ static __forceinline__ bool lt_neg(double p, double d) { return b(p) < 0 && (b(p) & MAG) > b(d); }
+};
+
 // --------------------------------------------------------------------------- reconstructions
 // CW84 limited slope of the cell q0 between qm and qp (reconstruction_1d.py:64-100);
 // min(...) * sign(d0) written as copysign: equal for every finite input
@@ -50,8 +80,9 @@ __device__ __forceinline__ real cw84_slope(real qm, real q0, real qp) {
     const real d0 = real(0.5) * (qp - qm);
     const real d1 = real(2.0) * (qp - q0);
     const real d2 = real(2.0) * (q0 - qm);
-    const real s = csign(O::fmn(O::fmn(O::ab(d0), O::ab(d1)), O::ab(d2)), d0);
-    return ((qp - q0) * (q0 - qm) > real(0)) ? s : real(0);
+    using B = Pred<real>;
+    const real s = csign(B::min_nonneg(B::min_nonneg(O::ab(d0), O::ab(d1)), O::ab(d2)), d0);
+    return B::prod_pos(qp - q0, q0 - qm) ? s : real(0);
 }
 // value at the edge between cells a and b from their values and slopes
 template <class real>
@@ -61,19 +92,19 @@ __device__ __forceinline__ real cw84_edge(real qa, real qb, real sa, real sb) {
 // CW84 monotonicity limiter of the parabola (L, R) of a cell with mean qc (reconstruction_1d.py:102-153)
 template <class real>
 __device__ __forceinline__ void cw84_limit(real qc, real &L, real &R) {
-    using O = RealOps<real>;
+    using B = Pred<real>;
     const real dq = R - L;
     const real q6 = real(6) * qc - real(3) * (R + L);
-    const bool flat = (R - qc) * (qc - L) <= real(0);
+    const bool flat = B::prod_nonpos(R - qc, qc - L);
     R = flat ? qc : R;
     L = flat ? qc : L;
-    const bool over = O::ab(dq) < O::ab(q6);
+    const bool over = B::abs_lt(dq, q6);
     const real DL = R - L;
     const real mid = qc - real(0.5) * (R + L);
     const real d2 = Div<real>::by(DL * DL, real(6.0), real(1.0 / 6.0));
     const real prod = DL * mid;
-    const bool ml = over && prod > d2;
-    const bool mr = over && !ml && -d2 > prod;
+    const bool ml = over && B::gt_nonneg(prod, d2);
+    const bool mr = over && !ml && B::lt_neg(prod, d2);
     const real Ln = real(3.0) * qc - real(2.0) * R;
     const real Rn = real(3.0) * qc - real(2.0) * L;
     L = ml ? Ln : L;
@@ -86,7 +117,8 @@ __device__ __forceinline__ real l04_mono(real qm, real q0, real qp) {
     const real dq = real(0.25) * (qp - qm);
     const real dmin = O::fmx(O::fmx(qm, q0), qp) - q0;
     const real dmax = q0 - O::fmn(O::fmn(qm, q0), qp);
-    return csign(O::fmn(O::fmn(O::ab(dq), dmin), dmax), dq);
+    using B = Pred<real>;
+    return csign(B::min_nonneg(B::min_nonneg(O::ab(dq), dmin), dmax), dq);
 }
 template <class real>
 __device__ __forceinline__ real l04_edge(real qa, real qb, real ma, real mb) {
@@ -96,9 +128,10 @@ __device__ __forceinline__ real l04_edge(real qa, real qb, real ma, real mb) {
 template <class real>
 __device__ __forceinline__ void l04_limit(real q0, real mono, real &L, real &R) {
     using O = RealOps<real>;
+    using B = Pred<real>;
     const real m2 = real(2.0) * mono;
-    L = q0 - csign(O::fmn(real(2.0) * O::ab(mono), O::ab(L - q0)), m2);
-    R = q0 + csign(O::fmn(real(2.0) * O::ab(mono), O::ab(R - q0)), m2);
+    L = q0 - csign(B::min_nonneg(real(2.0) * O::ab(mono), O::ab(L - q0)), m2);
+    R = q0 + csign(B::min_nonneg(real(2.0) * O::ab(mono), O::ab(R - q0)), m2);
 }
 // PPM-0 4-point edge value between cells a and b (reconstruction_1d.py:33-44)
 template <class real>

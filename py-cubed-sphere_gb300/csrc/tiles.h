@@ -71,7 +71,12 @@ struct SweepSolve {
                                 // (partials then hold sum(Q g)); null: the reference's projection
     const double *lag_w;    // ET-DG ghost-cell weights and stencil starts: when set, the kernel
     const int *lag_k;       // evaluates the ghost cells of its tiles itself; else it reads them
+    const double *hlag_w;   // the same tables for the batched ghost-cell kernel (always set)
+    const int *hlag_k;
 };
+
+// blocks of the batched ghost-cell kernel per tracer of a solve (128 ghost-cell columns each)
+__host__ __device__ inline int halo_blocks(const Dims &d) { return (NFACE * 4 * NG * d.n + 127) / 128; }
 
 constexpr int SWEEP_THREADS = 256;
 // tile shapes of the sweep kernel: {ti, tj} (ti + 6 and tj + 6 fill whole warps)
