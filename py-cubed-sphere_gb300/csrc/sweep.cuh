@@ -208,9 +208,9 @@ struct LineSums {
 };
 
 #ifndef CSADV_SWEEP_UNROLL
-#define CSADV_SWEEP_UNROLL 1
+#define CSADV_SWEEP_UNROLL 2
 #endif
-constexpr int SWEEP_UNROLL = CSADV_SWEEP_UNROLL;  // march loop unrolling
+constexpr int SWEEP_UNROLL = CSADV_SWEEP_UNROLL;  // march loop unrolling (2: measured best, FP32 and FP64)
 
 // March over cells [ma - 1, mb]: fluxes through edges [ma, mb], outputs for cells [ma, mb).
 //   MARCH_SPLIT : split field of the first pass -> out[k * os]
