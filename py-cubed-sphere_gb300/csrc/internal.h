@@ -163,6 +163,10 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
 template <class real>
 int sweep_launch(int recon, int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
                  cudaStream_t st);
+// the FP32 form runs the paired-tracer kernel (sweep2.cuh)
+template <>
+int sweep_launch<float>(int recon, int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid,
+                        size_t smem, cudaStream_t st);
 // edge records of the line-marching kernel from the reference-layout winds (static winds: once)
 template <class real, class V>
 int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT,

@@ -340,8 +340,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
         const Dims d = S.d;
         const int ti = S.ti, tj = S.tj, ntiles = S.ntiles, nitems = NFACE * ntiles;
         const int tile = it.y % ntiles, p = it.y / ntiles;
-        const int I0 = d.i0 + (tile / S.ntj) * ti, J0 = d.i0 + (tile % S.ntj) * tj;
-        const int ni = min(ti, d.iend - I0), nj = min(tj, d.iend - J0);
+        int I0, ni, J0, nj;
+        sweep_tile(S, tile, I0, ni, J0, nj);
         const SweepSmem L = sweep_smem(ti, tj);
         real *sQ = sm, *sQx = sm + L.oQx, *sQy = sm + L.oQy, *sDy = sm + L.oDy;
         const int P = d.pitch;

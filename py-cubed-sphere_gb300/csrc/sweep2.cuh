@@ -1,0 +1,619 @@
+// Paired-tracer line-marching step kernel of the FP32 form (k_sweep2).
+//
+// Same phases, tiles, work table and MF-PR bookkeeping as k_sweep (sweep.cuh), organised for
+// instruction throughput, which is what bounds the FP32 step (its HBM traffic is a few percent of
+// the bandwidth):
+//   * The tracers of a solve are advanced two at a time.  A thread marches one grid line for a
+//     pair of tracers (t, t+1) whose values of a cell sit in one 64-bit register (lanes x and y);
+//     the arithmetic of both runs in Blackwell's packed FP32 instructions (add/sub/mul/fma
+//     .f32x2), comparisons, minima and selections run per lane.
+//   * What depends only on the wind and the metric (edge and cell records and their loads, the
+//     Courant number, the upwind flag, the flux coefficients, addresses, loop control) is done
+//     once for both tracers.
+//   * Every operation is rounded once, in the packed and in the one-lane form alike (no
+//     contraction is left to the compiler), so a solve's odd last tracer, marched alone, gets
+//     the bits it would get as a member of a pair.
+//   * Shared-memory row pitches are compile-time constants (61 and 55 cells: odd, so 8-byte
+//     pairs are conflict-free along rows and along columns), the march loop is peeled so its
+//     body carries no conditions, and its loads run one cell (smem, cell records) and two edges
+//     (edge records) ahead; the reads past a line's end stay inside the tile buffers and the
+//     padded global planes.
+// Arithmetic follows the reference's formulas (reconstruction_1d.py:26-192, flux.py:20-128,
+// discrete_operators.py:49-101), evaluated in FP32 with some products regrouped (e.g. c^2/3 is
+// formed once per edge); the FP32 form's accuracy bounds are stated against the FP64 form.
+#pragma once
+#include "fused.cuh"
+#include "halo.cuh"
+
+namespace csadv {
+namespace pairk {
+
+typedef unsigned long long u64;
+
+// ------------------------------------------------------------------ one- and two-lane arithmetic
+__device__ __forceinline__ float vadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float vsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+__device__ __forceinline__ u64 &bits(float2 &v) { return reinterpret_cast<u64 &>(v); }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) {
+    float2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(bits(d)) : "l"(bits(a)), "l"(bits(b)));
+    return d;
+}
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) {
+    float2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(bits(d)) : "l"(bits(a)), "l"(bits(b)));
+    return d;
+}
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) {
+    float2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(bits(d)) : "l"(bits(a)), "l"(bits(b)));
+    return d;
+}
+__device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(bits(d)) : "l"(bits(a)), "l"(bits(b)), "l"(bits(c)));
+    return d;
+}
+
+template <class V> struct Lanes;
+template <> struct Lanes<float> { static constexpr int n = 1; };
+template <> struct Lanes<float2> { static constexpr int n = 2; };
+
+template <class V> __device__ __forceinline__ V bc(float s);
+template <> __device__ __forceinline__ float bc<float>(float s) { return s; }
+template <> __device__ __forceinline__ float2 bc<float2>(float s) { return make_float2(s, s); }
+
+__device__ __forceinline__ float lane(const float &v, int) { return v; }
+__device__ __forceinline__ float lane(const float2 &v, int l) { return l ? v.y : v.x; }
+__device__ __forceinline__ void set_lane(float &v, int, float x) { v = x; }
+__device__ __forceinline__ void set_lane(float2 &v, int l, float x) {
+    if (l) v.y = x;
+    else v.x = x;
+}
+
+// ------------------------------------------------------------------ reconstructions
+// CW84 limited slope of the cell between qm and qp (reconstruction_1d.py:64-100), with the
+// differences qp - q0 (dp, d1 = 2 dp) and q0 - qm (dm, d2 = 2 dm) supplied: the march carries
+// them from one cell to the next
+template <class V>
+__device__ __forceinline__ V cw84_slope(V qm, V qp, V dp, V d1, V dm, V d2) {
+    const V d0 = vmul(vsub(qp, qm), bc<V>(0.5f));
+    const V pr = vmul(dp, dm);
+    V s;
+#pragma unroll
+    for (int l = 0; l < Lanes<V>::n; ++l) {
+        const float m = fminf(fminf(fabsf(lane(d0, l)), fabsf(lane(d1, l))), fabsf(lane(d2, l)));
+        set_lane(s, l, lane(pr, l) > 0.f ? copysignf(m, lane(d0, l)) : 0.f);
+    }
+    return s;
+}
+// value at the edge between cells a and b from their means and slopes
+template <class V>
+__device__ __forceinline__ V cw84_edge(V qa, V qb, V sa, V sb) {
+    return vfma(vadd(qb, qa), bc<V>(0.5f), vmul(vsub(sb, sa), bc<V>(-1.0f / 6.0f)));
+}
+// CW84 monotonicity limiter of the parabola (L, R) of the cell with mean qc
+// (reconstruction_1d.py:102-153)
+template <class V>
+__device__ __forceinline__ void cw84_limit(V qc, V &L, V &R) {
+    const V dq = vsub(R, L);
+    const V q6 = vfma(qc, bc<V>(6.f), vmul(vadd(R, L), bc<V>(-3.f)));
+    const V pf = vmul(vsub(R, qc), vsub(qc, L));
+#pragma unroll
+    for (int l = 0; l < Lanes<V>::n; ++l) {
+        if (lane(pf, l) <= 0.f) {
+            set_lane(R, l, lane(qc, l));
+            set_lane(L, l, lane(qc, l));
+        }
+    }
+    const V DL = vsub(R, L);
+    const V mid = vfma(vadd(R, L), bc<V>(-0.5f), qc);
+    const V d2 = vmul(vmul(DL, DL), bc<V>(1.0f / 6.0f));
+    const V prod = vmul(DL, mid);
+    const V q3 = vmul(qc, bc<V>(3.f));
+    const V Ln = vfma(R, bc<V>(-2.f), q3);
+    const V Rn = vfma(L, bc<V>(-2.f), q3);
+#pragma unroll
+    for (int l = 0; l < Lanes<V>::n; ++l) {
+        const bool over = fabsf(lane(dq, l)) < fabsf(lane(q6, l));
+        const bool ml = over && lane(prod, l) > lane(d2, l);
+        const bool mr = over && !ml && -lane(d2, l) > lane(prod, l);
+        if (ml) set_lane(L, l, lane(Ln, l));
+        if (mr) set_lane(R, l, lane(Rn, l));
+    }
+}
+// L04 monotone slope of the cell q0 between qm and qp (reconstruction_1d.py:155-172)
+template <class V>
+__device__ __forceinline__ V l04_mono(V qm, V q0, V qp) {
+    const V dq = vmul(vsub(qp, qm), bc<V>(0.25f));
+    V r;
+#pragma unroll
+    for (int l = 0; l < Lanes<V>::n; ++l) {
+        const float a = lane(qm, l), b = lane(q0, l), c = lane(qp, l);
+        const float dmin = __fsub_rn(fmaxf(fmaxf(a, b), c), b);
+        const float dmax = __fsub_rn(b, fminf(fminf(a, b), c));
+        set_lane(r, l, copysignf(fminf(fminf(fabsf(lane(dq, l)), dmin), dmax), lane(dq, l)));
+    }
+    return r;
+}
+template <class V>
+__device__ __forceinline__ V l04_edge(V qa, V qb, V ma, V mb) {
+    return vfma(vadd(qb, qa), bc<V>(0.5f), vmul(vsub(mb, ma), bc<V>(-1.0f / 3.0f)));
+}
+// L04 limiter (reconstruction_1d.py:174-192)
+template <class V>
+__device__ __forceinline__ void l04_limit(V q0, V mono, V &L, V &R) {
+    const V dL = vsub(L, q0), dR = vsub(R, q0);
+#pragma unroll
+    for (int l = 0; l < Lanes<V>::n; ++l) {
+        const float m2 = __fmul_rn(2.f, lane(mono, l)), a = fabsf(m2);
+        set_lane(L, l, __fsub_rn(lane(q0, l), copysignf(fminf(a, fabsf(lane(dL, l))), m2)));
+        set_lane(R, l, __fadd_rn(lane(q0, l), copysignf(fminf(a, fabsf(lane(dR, l))), m2)));
+    }
+}
+// PPM-0 4-point edge value between cells a and b (reconstruction_1d.py:33-44)
+template <class V>
+__device__ __forceinline__ V ppm0_edge(V qam, V qa, V qb, V qbp) {
+    return vfma(vadd(qb, qa), bc<V>(7.0f / 12.0f), vmul(vadd(qbp, qam), bc<V>(-1.0f / 12.0f)));
+}
+
+// Marching reconstruction: init() with the window q(ma-3..ma+1) prepares cell ma-1; cell() with
+// the window w = q(m-2..m+2) gives the parabola (L, R) of cell m and advances.
+template <int REC, class V>
+struct Recon {
+    V s, E, dp, d1;  // slope of the current cell, its left edge value; q(m+1) - q(m) and twice it
+    __device__ __forceinline__ void init(const V w[5]) {
+        if (REC == REC_CW84) {
+            const V dpa = vsub(w[2], w[1]), dma = vsub(w[1], w[0]);
+            const V sa = cw84_slope(w[0], w[2], dpa, vadd(dpa, dpa), dma, vadd(dma, dma));
+            dp = vsub(w[3], w[2]);
+            d1 = vadd(dp, dp);
+            s = cw84_slope(w[1], w[3], dp, d1, dpa, vadd(dpa, dpa));
+            E = cw84_edge(w[1], w[2], sa, s);
+        } else if (REC == REC_L04) {
+            const V sa = l04_mono(w[0], w[1], w[2]);
+            s = l04_mono(w[1], w[2], w[3]);
+            E = l04_edge(w[1], w[2], sa, s);
+        } else if (REC == REC_PPM0) {
+            E = ppm0_edge(w[0], w[1], w[2], w[3]);
+        }
+    }
+    __device__ __forceinline__ void cell(const V w[5], V &L, V &R) {
+        if (REC == REC_CW84) {
+            const V dpn = vsub(w[4], w[3]);
+            const V d1n = vadd(dpn, dpn);
+            const V sn = cw84_slope(w[2], w[4], dpn, d1n, dp, d1);
+            const V En = cw84_edge(w[2], w[3], s, sn);
+            L = E;
+            R = En;
+            cw84_limit(w[2], L, R);
+            s = sn;
+            E = En;
+            dp = dpn;
+            d1 = d1n;
+        } else if (REC == REC_L04) {
+            const V sn = l04_mono(w[2], w[3], w[4]);
+            const V En = l04_edge(w[2], w[3], s, sn);
+            L = E;
+            R = En;
+            l04_limit(w[2], s, L, R);
+            s = sn;
+            E = En;
+        } else if (REC == REC_PPM0) {
+            const V En = ppm0_edge(w[1], w[2], w[3], w[4]);
+            L = E;
+            R = En;
+            E = En;
+        } else {  // PL07 hybrid 5-point values (reconstruction_1d.py:46-62)
+            const V a1 = bc<V>(2.0f / 60.0f), a2 = bc<V>(-13.0f / 60.0f), a3 = bc<V>(47.0f / 60.0f),
+                    a4 = bc<V>(27.0f / 60.0f), a5 = bc<V>(-3.0f / 60.0f);
+            R = vfma(a5, w[4], vfma(a4, w[3], vfma(a3, w[2], vfma(a2, w[1], vmul(a1, w[0])))));
+            L = vfma(a1, w[4], vfma(a2, w[3], vfma(a3, w[2], vfma(a4, w[1], vmul(a5, w[0])))));
+        }
+    }
+};
+
+// ------------------------------------------------------------------ the march
+enum { M_SPLIT = 0, M_DIFF = 1, M_UPDATE = 2 };
+
+// One grid line of the tile for one or two tracers.  Cell m (tile-local, 0 = the tile's first
+// interior cell along the line) is at win[m * SS] in shared memory; the records of edge m (its
+// left edge) and of cell m are erec[m * P] and crec[m * P] in global memory.  Cells [ma, mb) get
+// outputs, from the fluxes through edges [ma, mb]:
+//   M_SPLIT : split field of the first pass -> out[k * OS]             (discrete_operators.py:49-73)
+//   M_DIFF  : flux difference F(k+1) - F(k) -> out[k * OS]
+//   M_UPDATE: Q(k) - dt div(k) -> qo0/qo1[k * P] (lanes x/y), with the y-flux differences
+//             dy[k * OS] and Q(k) at qc[k * PAIR_QJP]; sums of div g and of the new Q g per lane
+//             into acc / accm (MF-PR, discrete_operators.py:80-101)
+template <int REC, int SPL, int MODE, int SS, int OS, class V>
+struct Marcher {
+    static constexpr bool MT0 = SPL != SP_PL07;
+    const V *win;
+    const float2 *ef, *cf;  // next edge / cell record to load
+    int P;
+    float dtdx;
+    V w[5];
+    Recon<REC, V> rc;
+    float2 eA, eB, cC, cP;  // edges m, m+1; cells m, m-1
+    V pL, pR, pQ, Fp;       // previous cell's (metric-weighted) parabola and mean; flux through edge m-1
+    float cmp;              // g u dt/dx at edge m-1 (SP-L04, SP-PL07)
+    V *out;
+    const V *dy, *qc;
+    float *qo0, *qo1;
+    V acc, accm;
+
+    __device__ __forceinline__ void start(const V *line, const float2 *erec, const float2 *crec, int P_, int ma) {
+        P = P_;
+        const V *s = line + (ma - 3) * SS;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) w[k] = s[k * SS];
+        win = s + 5 * SS;
+        rc.init(w);
+        const float2 *e = erec + (long long)(ma - 1) * P;
+        eA = __ldg(e);
+        eB = __ldg(e + P);
+        ef = e + 2 * (long long)P;
+        const float2 *c = crec + (long long)(ma - 1) * P;
+        cC = __ldg(c);
+        cf = c + P;
+    }
+
+    // iteration m: parabola of cell m; with FLUX the flux through edge m; with OUT the output of
+    // cell m - 1
+    template <bool FLUX, bool OUT>
+    __device__ __forceinline__ void step(const bool mfpr) {
+        const V wn = *win;
+        win += SS;
+        const float2 eN = __ldg(ef);
+        ef += P;
+        const float2 cN = __ldg(cf);
+        cf += P;
+
+        V L, R;
+        rc.cell(w, L, R);
+        V cL = L, cR = R, cQ = w[2];
+        const float gl = fabsf(eA.y);
+        if (MT0) {  // flux.py:28-31
+            cL = vmul(L, bc<V>(gl));
+            cR = vmul(R, bc<V>(fabsf(eB.y)));
+            cQ = vmul(w[2], bc<V>(cC.x));
+        }
+        if (FLUX) {
+            // upwind PPM flux through edge m (flux.py:20-128): the parabola of cell m-1 when the
+            // wind is >= 0, of cell m otherwise
+            const float u = eA.x;
+            const bool up = !signbit(eA.y);
+            const float c = __fmul_rn(u, dtdx);
+            const float hc = __fmul_rn(0.5f, c);
+            const float hs = up ? hc : -hc;
+            const float c3 = __fmul_rn(__fmul_rn(c, c), 1.0f / 3.0f);
+            V e, e2, eQ;
+#pragma unroll
+            for (int l = 0; l < Lanes<V>::n; ++l) {
+                set_lane(e, l, up ? lane(pR, l) : lane(cL, l));
+                set_lane(e2, l, up ? lane(pL, l) : lane(cR, l));
+                set_lane(eQ, l, up ? lane(pQ, l) : lane(cQ, l));
+            }
+            const V sdq = vsub(e, e2);
+            const V q6 = vfma(eQ, bc<V>(6.f), vmul(vadd(e, e2), bc<V>(-3.f)));
+            const V t1 = vmul(vsub(q6, sdq), bc<V>(hs));
+            V F = vfma(q6, bc<V>(-c3), vadd(e, t1));
+            F = vmul(F, bc<V>(u));
+            if (!MT0) F = vmul(F, bc<V>(gl));
+            const float cm = __fmul_rn(gl, c);
+            if (OUT) {
+                const V dF = vsub(F, Fp);  // F(k+1) - F(k), k = m - 1
+                if (MODE == M_SPLIT) {
+                    const V q = w[1];
+                    V o;
+                    if (SPL == SP_AVLT) {  // Q + dF / 2 with dF = -(F(k+1) - F(k)) dt/dx / g
+                        o = vfma(dF, bc<V>(__fmul_rn(cP.y, -0.5f * dtdx)), q);
+                    } else if (SPL == SP_L04) {  // (Q g + dF / 2 + (c_k+1 - c_k) Q / 2) / g
+                        const float a = __fadd_rn(cP.x, __fmul_rn(0.5f, __fsub_rn(cm, cmp)));
+                        o = vmul(vfma(q, bc<V>(a), vmul(dF, bc<V>(-0.5f * dtdx))), bc<V>(cP.y));
+                    } else {  // (Q + (Q + dF) / (1 - (c_k+1 - c_k))) / 2
+                        const float r = __frcp_rn(__fsub_rn(1.f, __fsub_rn(cm, cmp)));
+                        o = vmul(vadd(q, vmul(vfma(dF, bc<V>(-dtdx), q), bc<V>(r))), bc<V>(0.5f));
+                    }
+                    *out = o;
+                    out += OS;
+                } else if (MODE == M_DIFF) {
+                    *out = dF;
+                    out += OS;
+                } else {
+                    const V sdiv = vadd(dF, *dy);
+                    dy += OS;
+                    const V qn = vfma(sdiv, bc<V>(-__fmul_rn(dtdx, cP.y)), *qc);
+                    qc += PAIR_QJP;
+                    *qo0 = lane(qn, 0);
+                    qo0 += P;
+                    if (Lanes<V>::n == 2) {
+                        *qo1 = lane(qn, 1);
+                        qo1 += P;
+                    }
+                    if (mfpr) {
+                        acc = vfma(sdiv, bc<V>(__fmul_rn(cP.y, __fmul_rn(irdx, cP.x))), acc);
+                        accm = vfma(qn, bc<V>(cP.x), accm);
+                    }
+                }
+            }
+            Fp = F;
+            cmp = cm;
+        }
+        pL = cL;
+        pR = cR;
+        pQ = cQ;
+        cP = cC;
+        eA = eB;
+        eB = eN;
+        cC = cN;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) w[k] = w[k + 1];
+        w[4] = wn;
+    }
+    float irdx;
+
+    // march over cells [ma - 1, mb]
+    __device__ __forceinline__ void run(int ma, int mb, bool mfpr) {
+        step<false, false>(mfpr);
+        step<true, false>(mfpr);
+#pragma unroll 2
+        for (int m = ma + 1; m <= mb; ++m) step<true, true>(mfpr);
+    }
+};
+
+// ------------------------------------------------------------------ one tile, one or two tracers
+// Phases as in k_sweep: P0 Q (+ halo) -> shared; P1 first-pass x- and y-lines -> Qx, Qy;
+// P2 y-lines of Qx -> dY; P3 x-lines of Qy -> div, update, MF-PR partial(s).
+template <int REC, int SPL, class V>
+__device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, int tr, int I0, int ni, int J0, int nj,
+                                          unsigned char *smem_raw, double *red) {
+    constexpr int NL = Lanes<V>::n;
+    constexpr int QJP = PAIR_QJP, TJP = PAIR_TJP;
+    const int tid = threadIdx.x, lane_id = tid & 31, warp = tid >> 5;
+    constexpr int NWARP = SWEEP_THREADS / 32;
+    const Dims d = S.d;
+    const int P = d.pitch;
+    const long long pofs = (long long)p * d.plane;
+    const PairSmem L = pair_smem(S.ti);
+    V *sm = (V *)smem_raw;
+    V *sQ = sm, *sQx = sm + L.oQx, *sQy = sm + L.oQy, *sDy = sm + L.oDy;
+    const float dtdx = (float)(S.dt / S.dx);
+    const float irdx = (float)(1.0 / S.dx);
+    const bool mfpr = S.mfpr != 0;
+    const float2 *erx = (const float2 *)S.erx + pofs, *ery = (const float2 *)S.ery + pofs;
+    const float2 *crx = (const float2 *)S.crx, *cry = (const float2 *)S.cry;
+    const float *gpc = (const float *)S.gpc;
+    const bool hc = S.corr_in != nullptr;
+    const bool inline_ghosts = S.lag_w != nullptr;
+
+    // P0: Q on the tile + 3 halo cells; interior cells with the pending MF-PR correction
+    {
+        const float *Qt[2];
+        float corr[2];
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+            Qt[l] = (const float *)S.Qin + (long long)(tr + l) * d.field + pofs;
+            corr[l] = hc ? (float)S.corr_in[tr + l] : 0.f;
+        }
+        for (int r = warp; r < ni + 6; r += NWARP) {
+            const int i = I0 - 3 + r;
+            const bool irow = i >= d.i0 && i < d.iend;
+            for (int c = lane_id; c < nj + 6; c += 32) {
+                const int j = J0 - 3 + c;
+                const long long o = (long long)i * P + j;
+                V v;
+                if (irow && j >= d.i0 && j < d.iend) {
+                    const float g = hc ? __ldg(gpc + o) : 0.f;
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) {
+                        float x = __ldg(Qt[l] + o);
+                        if (hc) x = corrected(x, g, corr[l]);
+                        set_lane(v, l, x);
+                    }
+                } else if (!inline_ghosts) {
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) set_lane(v, l, __ldg(Qt[l] + o));
+                } else {
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) {
+                        const Src<float> src{(const float *)S.Qin + (long long)(tr + l) * d.field, gpc, corr[l], hc};
+                        set_lane(v, l, (float)ghost_value(src, d, S.lag_w, S.lag_k, p, i, j));
+                    }
+                }
+                sQ[r * QJP + c] = v;
+            }
+        }
+    }
+    __syncthreads();
+    // P1: x-lines over columns c in [-3, nj+3), cells [0, ni) -> Qx;
+    //     y-lines over rows r in [-3, ni+3), cells [0, nj) -> Qy
+    {
+        const int LX = round32(nj + 6), LY = round32(ni + 6);
+        const int jx = S.s1x * LX, jy = S.s1y * LY;
+        for (int job = tid; job < jx + jy; job += SWEEP_THREADS) {
+            if (job < jx) {
+                const int seg = job / LX, c = job - seg * LX - 3;
+                const int ma = ni * seg / S.s1x, mb = ni * (seg + 1) / S.s1x;
+                if (c >= nj + 3 || ma >= mb) continue;
+                const long long g0 = (long long)I0 * P + J0 + c;
+                Marcher<REC, SPL, M_SPLIT, QJP, QJP, V> mr;
+                mr.dtdx = dtdx;
+                mr.irdx = irdx;
+                mr.start(sQ + 3 * QJP + c + 3, erx + g0, crx + g0, P, ma);
+                mr.out = sQx + ma * QJP + c + 3;
+                mr.run(ma, mb, false);
+            } else {
+                const int jj = job - jx;
+                const int seg = jj / LY, r = jj - seg * LY - 3;
+                const int ma = nj * seg / S.s1y, mb = nj * (seg + 1) / S.s1y;
+                if (r >= ni + 3 || ma >= mb) continue;
+                const long long g0 = (long long)J0 * P + I0 + r;
+                Marcher<REC, SPL, M_SPLIT, 1, 1, V> mr;
+                mr.dtdx = dtdx;
+                mr.irdx = irdx;
+                mr.start(sQ + (r + 3) * QJP + 3, ery + g0, cry + g0, P, ma);
+                mr.out = sQy + (r + 3) * TJP + ma;
+                mr.run(ma, mb, false);
+            }
+        }
+    }
+    __syncthreads();
+    // P2: y-lines of Qx over rows [0, ni): second-pass y-flux differences -> dY
+    {
+        const int LY = round32(ni);
+        const int jy = S.s2y * LY;
+        for (int job = tid; job < jy; job += SWEEP_THREADS) {
+            const int seg = job / LY, r = job - seg * LY;
+            const int ma = nj * seg / S.s2y, mb = nj * (seg + 1) / S.s2y;
+            if (r >= ni || ma >= mb) continue;
+            const long long g0 = (long long)J0 * P + I0 + r;
+            Marcher<REC, SPL, M_DIFF, 1, 1, V> mr;
+            mr.dtdx = dtdx;
+            mr.irdx = irdx;
+            mr.start(sQx + r * QJP + 3, ery + g0, cry + g0, P, ma);
+            mr.out = sDy + r * TJP + ma;
+            mr.run(ma, mb, false);
+        }
+    }
+    __syncthreads();
+    // P3: x-lines of Qy over columns [0, nj): second-pass x fluxes, div, update, MF-PR partials
+    V acc = bc<V>(0.f), accm = bc<V>(0.f);
+    {
+        const int LX = round32(nj);
+        const int jx = S.s2x * LX;
+        float *Qo0 = (float *)S.Qout + (long long)tr * d.field + pofs;
+        for (int job = tid; job < jx; job += SWEEP_THREADS) {
+            const int seg = job / LX, c = job - seg * LX;
+            const int ma = ni * seg / S.s2x, mb = ni * (seg + 1) / S.s2x;
+            if (c >= nj || ma >= mb) continue;
+            const long long g0 = (long long)I0 * P + J0 + c;
+            Marcher<REC, SPL, M_UPDATE, TJP, TJP, V> mr;
+            mr.dtdx = dtdx;
+            mr.irdx = irdx;
+            mr.start(sQy + 3 * TJP + c, erx + g0, crx + g0, P, ma);
+            mr.dy = sDy + ma * TJP + c;
+            mr.qc = sQ + (ma + 3) * QJP + c + 3;
+            mr.qo0 = Qo0 + g0 + (long long)ma * P;
+            mr.qo1 = mr.qo0 + d.field;
+            mr.acc = acc;
+            mr.accm = accm;
+            mr.run(ma, mb, mfpr);
+            acc = mr.acc;
+            accm = mr.accm;
+        }
+    }
+    if (mfpr) {  // FP64 across threads, in a fixed order, per tracer
+        const bool anchor = S.mass_target != nullptr;
+        const int nitems = NFACE * S.ntiles;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+            double dacc = (double)(anchor ? lane(accm, l) : lane(acc, l));
+            for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
+            if (lane_id == 0) red[l * NWARP + warp] = dacc;
+        }
+        __syncthreads();
+        if (tid < NL) {
+            double s = 0.0;
+            for (int w = 0; w < NWARP; ++w) s += red[tid * NWARP + w];
+            S.partials[(long long)(tr + tid) * nitems + item] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// SPL: the splitting (SP_AVLT, SP_L04 with MT-0; SP_PL07 with MT-PL07), fixed per kernel
+template <int REC, int SPL>
+__global__ void __launch_bounds__(SWEEP_THREADS, 2) k_sweep2(const SweepSolve *__restrict__ solves,
+                                                           const int2 *__restrict__ work, int nwork) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red[SWEEP_THREADS];
+    __shared__ int last;
+    const int tid = threadIdx.x;
+
+    for (int wk = blockIdx.x; wk < nwork; wk += gridDim.x) {
+        const int2 it = work ? work[wk] : make_int2(0, wk);
+        const SweepSolve &S = solves[it.x];
+        const int ntiles = S.ntiles, nitems = NFACE * ntiles;
+        const int tile = it.y % ntiles, p = it.y / ntiles;
+        int I0, ni, J0, nj;
+        sweep_tile(S, tile, I0, ni, J0, nj);
+        const int T = S.T;
+        for (int tr = 0; tr < T; tr += 2) {
+            if (tr + 1 < T)
+                tile_pass<REC, SPL, float2>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
+            else
+                tile_pass<REC, SPL, float>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
+        }
+        if (S.mfpr) {
+            // the last item of the solve to finish sums its partials: corr = dt m0 / a2, or (FP32
+            // mass anchor) the correction that restores the recorded mass
+            if (tid == 0) {
+                __threadfence();
+                const unsigned int prev = atomicAdd(S.counter, 1u);
+                last = prev == (unsigned int)nitems - 1u;
+            }
+            __syncthreads();
+            if (last) {
+                __threadfence();
+                for (int tr = 0; tr < T; ++tr) {
+                    double a = 0.0;
+                    const volatile double *pp = S.partials + (long long)tr * nitems;
+                    for (int b = tid; b < nitems; b += SWEEP_THREADS) a += pp[b];
+                    red[tid] = a;
+                    __syncthreads();
+                    for (int s = SWEEP_THREADS / 2; s > 0; s >>= 1) {
+                        if (tid < s) red[tid] += red[tid + s];
+                        __syncthreads();
+                    }
+                    if (tid == 0)
+                        S.corr_out[tr] = S.mass_target ? (S.mass_target[tr] - red[0]) / S.a2 : S.dt * red[0] / S.a2;
+                    __syncthreads();
+                }
+                if (tid == 0) *S.counter = 0u;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <int REC, int SPL>
+int go(const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem, cudaStream_t st) {
+    if (st == (cudaStream_t)-1) {  // prepare only: allow the largest layout
+        size_t mx = 0;
+        for (int c = 0; c < SWEEP_NTILE_CFG; ++c) mx = mx > sweep_smem_bytes<float>(c) ? mx : sweep_smem_bytes<float>(c);
+        CSADV_CUDA(cudaFuncSetAttribute(k_sweep2<REC, SPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+        return CSADV_OK;
+    }
+    k_sweep2<REC, SPL><<<grid, SWEEP_THREADS, smem, st>>>(dsolves, work, nwork);
+    CSADV_CUDA(cudaGetLastError());
+    return CSADV_OK;
+}
+
+template <int REC>
+int split(int spl, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem, cudaStream_t st) {
+    switch (spl) {
+        case SP_AVLT: return go<REC, SP_AVLT>(dsolves, work, nwork, grid, smem, st);
+        case SP_L04: return go<REC, SP_L04>(dsolves, work, nwork, grid, smem, st);
+        default: return go<REC, SP_PL07>(dsolves, work, nwork, grid, smem, st);
+    }
+}
+
+}  // namespace pairk
+
+// the FP32 form's step kernel: tracers in pairs (k_sweep2)
+template <>
+int sweep_launch<float>(int recon, int spl, const SweepSolve *dsolves, const int2 *work, int nwork, int grid,
+                        size_t smem, cudaStream_t st) {
+    switch (recon) {
+        case REC_PPM0: return pairk::split<REC_PPM0>(spl, dsolves, work, nwork, grid, smem, st);
+        case REC_CW84: return pairk::split<REC_CW84>(spl, dsolves, work, nwork, grid, smem, st);
+        case REC_PL07: return pairk::split<REC_PL07>(spl, dsolves, work, nwork, grid, smem, st);
+        default: return pairk::split<REC_L04>(spl, dsolves, work, nwork, grid, smem, st);
+    }
+}
+
+}  // namespace csadv

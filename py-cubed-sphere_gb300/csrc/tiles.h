@@ -79,9 +79,11 @@ struct SweepSolve {
 __host__ __device__ inline int halo_blocks(const Dims &d) { return (NFACE * 4 * NG * d.n + 127) / 128; }
 
 constexpr int SWEEP_THREADS = 256;
-// tile shapes of the sweep kernel: {ti, tj} (ti + 6 and tj + 6 fill whole warps)
-constexpr int SWEEP_TILES[][2] = {{58, 58}, {58, 26}, {26, 58}, {26, 26}};
+// largest tile shapes of the sweep kernels: {ti, tj}; the N cells of each direction are split into
+// nearly equal tiles no larger than these (sweep_tile)
+constexpr int SWEEP_TILES[][2] = {{55, 55}, {55, 26}, {26, 55}, {26, 26}};
 constexpr int SWEEP_NTILE_CFG = 4;
+constexpr int SWEEP_TMAX = 55;  // largest ti, tj of any shape
 
 __host__ __device__ __forceinline__ int odd_up(int x) { return x | 1; }
 __host__ __device__ __forceinline__ int round32(int x) { return (x + 31) & ~31; }
@@ -123,9 +125,47 @@ inline void sweep_config(SweepSolve &s, int cfg) {
     s.ntiles = ((N + s.ti - 1) / s.ti) * s.ntj;
 }
 
+// Rows [I0, I0 + ni) and columns [J0, J0 + nj) (panel indices) of tile `tile` of a solve.  The
+// N interior cells of each direction are split into nearly equal parts (sizes differ by at
+// most one and never exceed the configured shape), so no CTA carries a full tile while another
+// carries a ragged remainder.
+__host__ __device__ __forceinline__ void sweep_tile(const SweepSolve &s, int tile, int &I0, int &ni, int &J0,
+                                                    int &nj) {
+    const int N = s.d.N, nti = s.ntiles / s.ntj;
+    const int a = tile / s.ntj, b = tile - a * s.ntj;
+    const int ia = N * a / nti, ib = N * (a + 1) / nti;
+    const int ja = N * b / s.ntj, jb = N * (b + 1) / s.ntj;
+    I0 = s.d.i0 + ia;
+    ni = ib - ia;
+    J0 = s.d.i0 + ja;
+    nj = jb - ja;
+}
+
+// Shared-memory layout of the paired-tracer FP32 kernel (k_sweep2): one 8-byte pair of
+// tracer values per cell, row pitches fixed at compile time for every tile shape (odd numbers of
+// pairs: conflict-free along rows and along columns), ti rows.  Units: pairs.
+constexpr int PAIR_QJP = SWEEP_TMAX + 6;  // rows of the Q and Qx tiles (tj + 6 cells)
+constexpr int PAIR_TJP = SWEEP_TMAX;      // rows of the Qy and dY tiles (tj cells)
+struct PairSmem {
+    int oQx, oQy, oDy, total;
+};
+__host__ __device__ __forceinline__ PairSmem pair_smem(int ti) {
+    PairSmem s;
+    s.oQx = (ti + 6) * PAIR_QJP;
+    s.oQy = s.oQx + ti * PAIR_QJP;
+    s.oDy = s.oQy + (ti + 6) * PAIR_TJP;
+    s.total = s.oDy + ti * PAIR_TJP + 8;  // + a few pairs: the marching loads run one cell past a line
+    return s;
+}
+
 template <class real>
 inline size_t sweep_smem_bytes(int cfg) {
     return (size_t)sweep_smem(SWEEP_TILES[cfg][0], SWEEP_TILES[cfg][1]).total * sizeof(real);
+}
+// the FP32 form runs the paired-tracer kernel
+template <>
+inline size_t sweep_smem_bytes<float>(int cfg) {
+    return (size_t)pair_smem(SWEEP_TILES[cfg][0]).total * 2 * sizeof(float);
 }
 
 }  // namespace csadv
