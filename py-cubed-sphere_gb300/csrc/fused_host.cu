@@ -221,6 +221,8 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         sweep_config(s, f.scfg);
         s.dt = dt;
         s.dx = g.dx;
+        s.dtdx = (float)(dt / g.dx);
+        s.irdx = (float)(1.0 / g.dx);
         s.a2 = g.a2;
         s.Qin = f.Qbuf[b];
         s.Qout = f.Qbuf[1 - b];

@@ -30,6 +30,11 @@ namespace pairk {
 
 typedef unsigned long long u64;
 
+#ifndef CSADV_PAIR_UNROLL
+#define CSADV_PAIR_UNROLL 2
+#endif
+constexpr int PAIR_UNROLL = CSADV_PAIR_UNROLL;  // march loop unrolling
+
 // ------------------------------------------------------------------ one- and two-lane arithmetic
 __device__ __forceinline__ float vadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float vsub(float a, float b) { return __fsub_rn(a, b); }
@@ -75,141 +80,150 @@ __device__ __forceinline__ void set_lane(float2 &v, int l, float x) {
 }
 
 // ------------------------------------------------------------------ reconstructions
-// CW84 limited slope of the cell between qm and qp (reconstruction_1d.py:64-100), with the
-// differences qp - q0 (dp, d1 = 2 dp) and q0 - qm (dm, d2 = 2 dm) supplied: the march carries
-// them from one cell to the next
+// The reconstructions work in doubled units: slopes, edge values and parabolas are carried as
+// twice their value (2 L, 2 R, 2 q), which is exact, removes the halving constants from the
+// packed arithmetic (every constant pair of a packed operation occupies two registers), and
+// leaves every comparison of the limiters unchanged.  The flux folds the factor 1/2 into the
+// wind (F = F2 u / 2).
+
+// twice the CW84 limited slope of the cell between qm and qp (reconstruction_1d.py:64-100):
+// with dp = qp - q0, dm = q0 - qm: copysign(min(|qp - qm|, 4|dp|, 4|dm|), qp - qm) when
+// dp dm > 0, else 0; D1 = 4 dp and D2 = 4 dm are supplied (the march carries them)
 template <class V>
-__device__ __forceinline__ V cw84_slope(V qm, V qp, V dp, V d1, V dm, V d2) {
-    const V d0 = vmul(vsub(qp, qm), bc<V>(0.5f));
+__device__ __forceinline__ V cw84_slope2(V qm, V qp, V dp, V D1, V dm, V D2) {
+    const V D0 = vsub(qp, qm);
     const V pr = vmul(dp, dm);
     V s;
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
-        const float m = fminf(fminf(fabsf(lane(d0, l)), fabsf(lane(d1, l))), fabsf(lane(d2, l)));
-        set_lane(s, l, lane(pr, l) > 0.f ? copysignf(m, lane(d0, l)) : 0.f);
+        const float m = fminf(fminf(fabsf(lane(D0, l)), fabsf(lane(D1, l))), fabsf(lane(D2, l)));
+        set_lane(s, l, lane(pr, l) > 0.f ? copysignf(m, lane(D0, l)) : 0.f);
     }
     return s;
 }
-// value at the edge between cells a and b from their means and slopes
 template <class V>
-__device__ __forceinline__ V cw84_edge(V qa, V qb, V sa, V sb) {
-    return vfma(vadd(qb, qa), bc<V>(0.5f), vmul(vsub(sb, sa), bc<V>(-1.0f / 6.0f)));
+__device__ __forceinline__ V times4(V x) {
+    const V t = vadd(x, x);
+    return vadd(t, t);
 }
-// CW84 monotonicity limiter of the parabola (L, R) of the cell with mean qc
-// (reconstruction_1d.py:102-153)
+// twice the value at the edge between cells a and b from their means and doubled slopes:
+// (qa + qb) - (Sb - Sa) / 6
 template <class V>
-__device__ __forceinline__ void cw84_limit(V qc, V &L, V &R) {
-    const V dq = vsub(R, L);
-    const V q6 = vfma(qc, bc<V>(6.f), vmul(vadd(R, L), bc<V>(-3.f)));
-    const V pf = vmul(vsub(R, qc), vsub(qc, L));
+__device__ __forceinline__ V cw84_edge2(V qa, V qb, V Sa, V Sb) {
+    return vfma(vsub(Sb, Sa), bc<V>(-1.0f / 6.0f), vadd(qa, qb));
+}
+// CW84 monotonicity limiter (reconstruction_1d.py:102-153) on the doubled parabola (L2, R2) of
+// the cell with doubled mean Q2.  With dq = R - L and q6 = 6 q - 3 (R + L) taken before the
+// flattening, the reference's overshoot tests (R - L)(q - (R + L)/2) >< +-(R - L)^2 / 6 on the
+// flattened values read dq q6 >< +-dq^2 when the cell is not flattened and never fire when it
+// is; 3 q - 2 R = q - 2 (R - q) and 3 q - 2 L = q + 2 (q - L).
+template <class V>
+__device__ __forceinline__ void cw84_limit2(V Q2, V &L2, V &R2) {
+    const V dq = vsub(R2, L2);
+    const V q6 = vmul(vsub(vadd(Q2, Q2), vadd(R2, L2)), bc<V>(3.f));
+    const V u = vsub(R2, Q2), v = vsub(Q2, L2);
+    const V pf = vmul(u, v);
+    const V a = vmul(dq, q6), b = vmul(dq, dq);
+    const V Ln = vsub(Q2, vadd(u, u)), Rn = vadd(Q2, vadd(v, v));
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
-        if (lane(pf, l) <= 0.f) {
-            set_lane(R, l, lane(qc, l));
-            set_lane(L, l, lane(qc, l));
-        }
-    }
-    const V DL = vsub(R, L);
-    const V mid = vfma(vadd(R, L), bc<V>(-0.5f), qc);
-    const V d2 = vmul(vmul(DL, DL), bc<V>(1.0f / 6.0f));
-    const V prod = vmul(DL, mid);
-    const V q3 = vmul(qc, bc<V>(3.f));
-    const V Ln = vfma(R, bc<V>(-2.f), q3);
-    const V Rn = vfma(L, bc<V>(-2.f), q3);
-#pragma unroll
-    for (int l = 0; l < Lanes<V>::n; ++l) {
-        const bool over = fabsf(lane(dq, l)) < fabsf(lane(q6, l));
-        const bool ml = over && lane(prod, l) > lane(d2, l);
-        const bool mr = over && !ml && -lane(d2, l) > lane(prod, l);
-        if (ml) set_lane(L, l, lane(Ln, l));
-        if (mr) set_lane(R, l, lane(Rn, l));
+        const bool flat = lane(pf, l) <= 0.f;
+        const bool over = !flat && fabsf(lane(dq, l)) < fabsf(lane(q6, l));
+        const bool ml = over && lane(a, l) > lane(b, l);
+        const bool mr = over && !ml && -lane(b, l) > lane(a, l);
+        set_lane(L2, l, flat ? lane(Q2, l) : (ml ? lane(Ln, l) : lane(L2, l)));
+        set_lane(R2, l, flat ? lane(Q2, l) : (mr ? lane(Rn, l) : lane(R2, l)));
     }
 }
-// L04 monotone slope of the cell q0 between qm and qp (reconstruction_1d.py:155-172)
+// twice the L04 monotone slope of the cell q0 between qm and qp (reconstruction_1d.py:155-172)
 template <class V>
-__device__ __forceinline__ V l04_mono(V qm, V q0, V qp) {
-    const V dq = vmul(vsub(qp, qm), bc<V>(0.25f));
+__device__ __forceinline__ V l04_mono2(V qm, V q0, V qp) {
+    const V dq = vmul(vsub(qp, qm), bc<V>(0.5f));
     V r;
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
         const float a = lane(qm, l), b = lane(q0, l), c = lane(qp, l);
         const float dmin = __fsub_rn(fmaxf(fmaxf(a, b), c), b);
         const float dmax = __fsub_rn(b, fminf(fminf(a, b), c));
-        set_lane(r, l, copysignf(fminf(fminf(fabsf(lane(dq, l)), dmin), dmax), lane(dq, l)));
+        const float m = fminf(fminf(fabsf(lane(dq, l)), __fadd_rn(dmin, dmin)), __fadd_rn(dmax, dmax));
+        set_lane(r, l, copysignf(m, lane(dq, l)));
     }
     return r;
 }
+// twice the L04 edge value: (qa + qb) - (Mb - Ma) / 3 with doubled slopes
 template <class V>
-__device__ __forceinline__ V l04_edge(V qa, V qb, V ma, V mb) {
-    return vfma(vadd(qb, qa), bc<V>(0.5f), vmul(vsub(mb, ma), bc<V>(-1.0f / 3.0f)));
+__device__ __forceinline__ V l04_edge2(V qa, V qb, V Ma, V Mb) {
+    return vfma(vsub(Mb, Ma), bc<V>(-1.0f / 3.0f), vadd(qa, qb));
 }
-// L04 limiter (reconstruction_1d.py:174-192)
+// L04 limiter (reconstruction_1d.py:174-192) on doubled values: L = q - copysign(min(2|m|,
+// |L - q|), m), R = q + copysign(min(2|m|, |R - q|), m)
 template <class V>
-__device__ __forceinline__ void l04_limit(V q0, V mono, V &L, V &R) {
-    const V dL = vsub(L, q0), dR = vsub(R, q0);
+__device__ __forceinline__ void l04_limit2(V Q2, V M2, V &L2, V &R2) {
+    const V dL = vsub(L2, Q2), dR = vsub(R2, Q2);
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
-        const float m2 = __fmul_rn(2.f, lane(mono, l)), a = fabsf(m2);
-        set_lane(L, l, __fsub_rn(lane(q0, l), copysignf(fminf(a, fabsf(lane(dL, l))), m2)));
-        set_lane(R, l, __fadd_rn(lane(q0, l), copysignf(fminf(a, fabsf(lane(dR, l))), m2)));
+        const float m = lane(M2, l), a = __fadd_rn(fabsf(m), fabsf(m));
+        set_lane(L2, l, __fsub_rn(lane(Q2, l), copysignf(fminf(a, fabsf(lane(dL, l))), m)));
+        set_lane(R2, l, __fadd_rn(lane(Q2, l), copysignf(fminf(a, fabsf(lane(dR, l))), m)));
     }
 }
-// PPM-0 4-point edge value between cells a and b (reconstruction_1d.py:33-44)
+// twice the PPM-0 4-point edge value between cells a and b (reconstruction_1d.py:33-44)
 template <class V>
-__device__ __forceinline__ V ppm0_edge(V qam, V qa, V qb, V qbp) {
-    return vfma(vadd(qb, qa), bc<V>(7.0f / 12.0f), vmul(vadd(qbp, qam), bc<V>(-1.0f / 12.0f)));
+__device__ __forceinline__ V ppm0_edge2(V qam, V qa, V qb, V qbp) {
+    return vfma(vadd(qb, qa), bc<V>(7.0f / 6.0f), vmul(vadd(qbp, qam), bc<V>(-1.0f / 6.0f)));
 }
 
 // Marching reconstruction: init() with the window q(ma-3..ma+1) prepares cell ma-1; cell() with
-// the window w = q(m-2..m+2) gives the parabola (L, R) of cell m and advances.
+// the window w = q(m-2..m+2) gives the doubled parabola (L2, R2) of cell m and advances.
 template <int REC, class V>
 struct Recon {
-    V s, E, dp, d1;  // slope of the current cell, its left edge value; q(m+1) - q(m) and twice it
+    V s, E, dp, D1;  // doubled slope of the current cell, doubled left edge value; q(m+1) - q(m), 4 times it
     __device__ __forceinline__ void init(const V w[5]) {
         if (REC == REC_CW84) {
             const V dpa = vsub(w[2], w[1]), dma = vsub(w[1], w[0]);
-            const V sa = cw84_slope(w[0], w[2], dpa, vadd(dpa, dpa), dma, vadd(dma, dma));
+            const V D1a = times4(dpa);
+            const V sa = cw84_slope2(w[0], w[2], dpa, D1a, dma, times4(dma));
             dp = vsub(w[3], w[2]);
-            d1 = vadd(dp, dp);
-            s = cw84_slope(w[1], w[3], dp, d1, dpa, vadd(dpa, dpa));
-            E = cw84_edge(w[1], w[2], sa, s);
+            D1 = times4(dp);
+            s = cw84_slope2(w[1], w[3], dp, D1, dpa, D1a);
+            E = cw84_edge2(w[1], w[2], sa, s);
         } else if (REC == REC_L04) {
-            const V sa = l04_mono(w[0], w[1], w[2]);
-            s = l04_mono(w[1], w[2], w[3]);
-            E = l04_edge(w[1], w[2], sa, s);
+            const V sa = l04_mono2(w[0], w[1], w[2]);
+            s = l04_mono2(w[1], w[2], w[3]);
+            E = l04_edge2(w[1], w[2], sa, s);
         } else if (REC == REC_PPM0) {
-            E = ppm0_edge(w[0], w[1], w[2], w[3]);
+            E = ppm0_edge2(w[0], w[1], w[2], w[3]);
         }
     }
     __device__ __forceinline__ void cell(const V w[5], V &L, V &R) {
         if (REC == REC_CW84) {
             const V dpn = vsub(w[4], w[3]);
-            const V d1n = vadd(dpn, dpn);
-            const V sn = cw84_slope(w[2], w[4], dpn, d1n, dp, d1);
-            const V En = cw84_edge(w[2], w[3], s, sn);
+            const V D1n = times4(dpn);
+            const V sn = cw84_slope2(w[2], w[4], dpn, D1n, dp, D1);
+            const V En = cw84_edge2(w[2], w[3], s, sn);
             L = E;
             R = En;
-            cw84_limit(w[2], L, R);
+            cw84_limit2(vadd(w[2], w[2]), L, R);
             s = sn;
             E = En;
             dp = dpn;
-            d1 = d1n;
+            D1 = D1n;
         } else if (REC == REC_L04) {
-            const V sn = l04_mono(w[2], w[3], w[4]);
-            const V En = l04_edge(w[2], w[3], s, sn);
+            const V sn = l04_mono2(w[2], w[3], w[4]);
+            const V En = l04_edge2(w[2], w[3], s, sn);
             L = E;
             R = En;
-            l04_limit(w[2], s, L, R);
+            l04_limit2(vadd(w[2], w[2]), s, L, R);
             s = sn;
             E = En;
         } else if (REC == REC_PPM0) {
-            const V En = ppm0_edge(w[1], w[2], w[3], w[4]);
+            const V En = ppm0_edge2(w[1], w[2], w[3], w[4]);
             L = E;
             R = En;
             E = En;
-        } else {  // PL07 hybrid 5-point values (reconstruction_1d.py:46-62)
-            const V a1 = bc<V>(2.0f / 60.0f), a2 = bc<V>(-13.0f / 60.0f), a3 = bc<V>(47.0f / 60.0f),
-                    a4 = bc<V>(27.0f / 60.0f), a5 = bc<V>(-3.0f / 60.0f);
+        } else {  // PL07 hybrid 5-point values (reconstruction_1d.py:46-62), doubled
+            const V a1 = bc<V>(2.0f / 30.0f), a2 = bc<V>(-13.0f / 30.0f), a3 = bc<V>(47.0f / 30.0f),
+                    a4 = bc<V>(27.0f / 30.0f), a5 = bc<V>(-3.0f / 30.0f);
             R = vfma(a5, w[4], vfma(a4, w[3], vfma(a3, w[2], vfma(a2, w[1], vmul(a1, w[0])))));
             L = vfma(a1, w[4], vfma(a2, w[3], vfma(a3, w[2], vfma(a4, w[1], vmul(a5, w[0])))));
         }
@@ -220,7 +234,7 @@ struct Recon {
 enum { M_SPLIT = 0, M_DIFF = 1, M_UPDATE = 2 };
 
 // One grid line of the tile for one or two tracers.  Cell m (tile-local, 0 = the tile's first
-// interior cell along the line) is at win[m * SS] in shared memory; the records of edge m (its
+// interior cell along the line) is at line[m * SS] in shared memory; the records of edge m (its
 // left edge) and of cell m are erec[m * P] and crec[m * P] in global memory.  Cells [ma, mb) get
 // outputs, from the fluxes through edges [ma, mb]:
 //   M_SPLIT : split field of the first pass -> out[k * OS]             (discrete_operators.py:49-73)
@@ -228,9 +242,10 @@ enum { M_SPLIT = 0, M_DIFF = 1, M_UPDATE = 2 };
 //   M_UPDATE: Q(k) - dt div(k) -> qo0/qo1[k * P] (lanes x/y), with the y-flux differences
 //             dy[k * OS] and Q(k) at qc[k * PAIR_QJP]; sums of div g and of the new Q g per lane
 //             into acc / accm (MF-PR, discrete_operators.py:80-101)
-template <int REC, int SPL, int MODE, int SS, int OS, class V>
+template <int REC, int SPL, int MODE, class V>
 struct Marcher {
     static constexpr bool MT0 = SPL != SP_PL07;
+    int SS, OS;             // strides of the line and of the output in shared memory (elements)
     const V *win;
     const float2 *ef, *cf;  // next edge / cell record to load
     int P;
@@ -245,7 +260,10 @@ struct Marcher {
     float *qo0, *qo1;
     V acc, accm;
 
-    __device__ __forceinline__ void start(const V *line, const float2 *erec, const float2 *crec, int P_, int ma) {
+    __device__ __forceinline__ void start(const V *line, int ss, int os, const float2 *erec, const float2 *crec, int P_,
+                                          int ma) {
+        SS = ss;
+        OS = os;
         P = P_;
         const V *s = line + (ma - 3) * SS;
 #pragma unroll
@@ -264,7 +282,7 @@ struct Marcher {
     // iteration m: parabola of cell m; with FLUX the flux through edge m; with OUT the output of
     // cell m - 1
     template <bool FLUX, bool OUT>
-    __device__ __forceinline__ void step(const bool mfpr) {
+    __device__ __forceinline__ void step() {
         const V wn = *win;
         win += SS;
         const float2 eN = __ldg(ef);
@@ -272,18 +290,21 @@ struct Marcher {
         const float2 cN = __ldg(cf);
         cf += P;
 
-        V L, R;
+        V L, R;  // doubled
         rc.cell(w, L, R);
-        V cL = L, cR = R, cQ = w[2];
+        V cL = L, cR = R, cQ;
         const float gl = fabsf(eA.y);
         if (MT0) {  // flux.py:28-31
             cL = vmul(L, bc<V>(gl));
             cR = vmul(R, bc<V>(fabsf(eB.y)));
-            cQ = vmul(w[2], bc<V>(cC.x));
+            cQ = vmul(w[2], bc<V>(__fadd_rn(cC.x, cC.x)));
+        } else {
+            cQ = vadd(w[2], w[2]);
         }
         if (FLUX) {
             // upwind PPM flux through edge m (flux.py:20-128): the parabola of cell m-1 when the
-            // wind is >= 0, of cell m otherwise
+            // wind is >= 0, of cell m otherwise; F = e + c/2 (q6 -+ dq) - q6 c^2 / 3 in doubled
+            // units, times u / 2
             const float u = eA.x;
             const bool up = !signbit(eA.y);
             const float c = __fmul_rn(u, dtdx);
@@ -298,11 +319,10 @@ struct Marcher {
                 set_lane(eQ, l, up ? lane(pQ, l) : lane(cQ, l));
             }
             const V sdq = vsub(e, e2);
-            const V q6 = vfma(eQ, bc<V>(6.f), vmul(vadd(e, e2), bc<V>(-3.f)));
+            const V q6 = vmul(vsub(vadd(eQ, eQ), vadd(e, e2)), bc<V>(3.f));
             const V t1 = vmul(vsub(q6, sdq), bc<V>(hs));
             V F = vfma(q6, bc<V>(-c3), vadd(e, t1));
-            F = vmul(F, bc<V>(u));
-            if (!MT0) F = vmul(F, bc<V>(gl));
+            F = vmul(F, bc<V>(MT0 ? __fmul_rn(0.5f, u) : __fmul_rn(__fmul_rn(0.5f, u), gl)));
             const float cm = __fmul_rn(gl, c);
             if (OUT) {
                 const V dF = vsub(F, Fp);  // F(k+1) - F(k), k = m - 1
@@ -334,10 +354,9 @@ struct Marcher {
                         *qo1 = lane(qn, 1);
                         qo1 += P;
                     }
-                    if (mfpr) {
-                        acc = vfma(sdiv, bc<V>(__fmul_rn(cP.y, __fmul_rn(irdx, cP.x))), acc);
-                        accm = vfma(qn, bc<V>(cP.x), accm);
-                    }
+                    // (accumulated unconditionally: a branch here would cost more than the sums)
+                    acc = vfma(sdiv, bc<V>(__fmul_rn(cP.y, __fmul_rn(irdx, cP.x))), acc);
+                    accm = vfma(qn, bc<V>(cP.x), accm);
                 }
             }
             Fp = F;
@@ -357,17 +376,18 @@ struct Marcher {
     float irdx;
 
     // march over cells [ma - 1, mb]
-    __device__ __forceinline__ void run(int ma, int mb, bool mfpr) {
-        step<false, false>(mfpr);
-        step<true, false>(mfpr);
-#pragma unroll 2
-        for (int m = ma + 1; m <= mb; ++m) step<true, true>(mfpr);
+    __device__ __forceinline__ void run(int ma, int mb) {
+        step<false, false>();
+        step<true, false>();
+#pragma unroll PAIR_UNROLL
+        for (int m = ma + 1; m <= mb; ++m) step<true, true>();
     }
 };
 
 // ------------------------------------------------------------------ one tile, one or two tracers
 // Phases as in k_sweep: P0 Q (+ halo) -> shared; P1 first-pass x- and y-lines -> Qx, Qy;
-// P2 y-lines of Qx -> dY; P3 x-lines of Qy -> div, update, MF-PR partial(s).
+// P2 y-lines of Qx -> dY; P3 x-lines of Qy -> div, update, MF-PR partial(s).  Every phase has
+// at most one line segment per thread (the segment counts are chosen so).
 template <int REC, int SPL, class V>
 __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, int tr, int I0, int ni, int J0, int nj,
                                           unsigned char *smem_raw, double *red) {
@@ -381,16 +401,37 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
     const PairSmem L = pair_smem(S.ti);
     V *sm = (V *)smem_raw;
     V *sQ = sm, *sQx = sm + L.oQx, *sQy = sm + L.oQy, *sDy = sm + L.oDy;
-    const float dtdx = (float)(S.dt / S.dx);
-    const float irdx = (float)(1.0 / S.dx);
-    const bool mfpr = S.mfpr != 0;
+    const float dtdx = S.dtdx, irdx = S.irdx;
     const float2 *erx = (const float2 *)S.erx + pofs, *ery = (const float2 *)S.ery + pofs;
     const float2 *crx = (const float2 *)S.crx, *cry = (const float2 *)S.cry;
     const float *gpc = (const float *)S.gpc;
     const bool hc = S.corr_in != nullptr;
-    const bool inline_ghosts = S.lag_w != nullptr;
 
-    // P0: Q on the tile + 3 halo cells; interior cells with the pending MF-PR correction
+    // The first-pass lines read the edge and cell records of the tile from global memory, one to
+    // two cells ahead of their use; after the records have left L2 (the first pair of a step)
+    // that is not far enough to hide a DRAM access, so every thread first asks L2 for a few
+    // 128-byte lines of them (x-lines: rows I0-1 .. I0+ni+2 of erx, crx from column J0-3;
+    // y-lines: the same of the transposed ery, cry), which then arrive while Q is loaded.
+    if (tr == 0) {
+        const int rx = ni + 4, ry = nj + 4, nl = 5;  // rows per array; lines per row (<= 61 records)
+        const int total = 2 * (rx + ry) * nl;
+        for (int k = tid; k < total; k += SWEEP_THREADS) {
+            const int l = k % nl, rowk = k / nl;
+            const float2 *base;
+            if (rowk < 2 * rx) {
+                const int row = rowk >> 1;
+                base = ((rowk & 1) ? crx : erx) + (long long)(I0 - 1 + row) * P + (J0 - 3);
+            } else {
+                const int row = (rowk - 2 * rx) >> 1;
+                base = ((rowk & 1) ? cry : ery) + (long long)(J0 - 1 + row) * P + (I0 - 3);
+            }
+            const char *a = (const char *)base + 128 * l;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+        }
+    }
+
+    // P0: Q on the tile + 3 halo cells; interior cells with the pending MF-PR correction.  Warp w
+    // takes rows w, w + 8, ...; all loads of a thread are issued before its first store.
     {
         const float *Qt[2];
         float corr[2];
@@ -399,84 +440,126 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
             Qt[l] = (const float *)S.Qin + (long long)(tr + l) * d.field + pofs;
             corr[l] = hc ? (float)S.corr_in[tr + l] : 0.f;
         }
-        for (int r = warp; r < ni + 6; r += NWARP) {
-            const int i = I0 - 3 + r;
-            const bool irow = i >= d.i0 && i < d.iend;
-            for (int c = lane_id; c < nj + 6; c += 32) {
-                const int j = J0 - 3 + c;
-                const long long o = (long long)i * P + j;
-                V v;
-                if (irow && j >= d.i0 && j < d.iend) {
-                    const float g = hc ? __ldg(gpc + o) : 0.f;
+        if (S.lag_w == nullptr) {
+            constexpr int RR = 4, CC = (SWEEP_TMAX + 6 + 31) / 32;  // cells per batch: RR x CC
+            for (int r0 = warp; r0 < ni + 6; r0 += RR * NWARP) {
+                float q[RR][CC][NL], g[RR][CC];
 #pragma unroll
-                    for (int l = 0; l < NL; ++l) {
-                        float x = __ldg(Qt[l] + o);
-                        if (hc) x = corrected(x, g, corr[l]);
-                        set_lane(v, l, x);
-                    }
-                } else if (!inline_ghosts) {
+                for (int a = 0; a < RR; ++a) {
+                    const int r = r0 + a * NWARP, i = I0 - 3 + r;
+                    const float *q0 = Qt[0] + (long long)i * P + J0 - 3 + lane_id;
 #pragma unroll
-                    for (int l = 0; l < NL; ++l) set_lane(v, l, __ldg(Qt[l] + o));
-                } else {
+                    for (int b = 0; b < CC; ++b) {
+                        if (r < ni + 6 && lane_id + 32 * b < nj + 6) {
 #pragma unroll
-                    for (int l = 0; l < NL; ++l) {
-                        const Src<float> src{(const float *)S.Qin + (long long)(tr + l) * d.field, gpc, corr[l], hc};
-                        set_lane(v, l, (float)ghost_value(src, d, S.lag_w, S.lag_k, p, i, j));
+                            for (int l = 0; l < NL; ++l) q[a][b][l] = __ldg(q0 + 32 * b + (l ? d.field : 0));
+                            g[a][b] = hc ? __ldg(gpc + (q0 - Qt[0]) + 32 * b) : 0.f;
+                        }
                     }
                 }
-                sQ[r * QJP + c] = v;
+#pragma unroll
+                for (int a = 0; a < RR; ++a) {
+                    const int r = r0 + a * NWARP, i = I0 - 3 + r;
+#pragma unroll
+                    for (int b = 0; b < CC; ++b) {
+                        const int c = lane_id + 32 * b, j = J0 - 3 + c;
+                        if (r < ni + 6 && c < nj + 6) {
+                            const bool in = hc && i >= d.i0 && i < d.iend && j >= d.i0 && j < d.iend;
+                            V v;
+#pragma unroll
+                            for (int l = 0; l < NL; ++l)
+                                set_lane(v, l, in ? corrected(q[a][b][l], g[a][b], corr[l]) : q[a][b][l]);
+                            sQ[r * QJP + c] = v;
+                        }
+                    }
+                }
+            }
+        } else {  // ghost cells evaluated here from the neighbouring panels (ET-DG)
+            for (int r = warp; r < ni + 6; r += NWARP) {
+                const int i = I0 - 3 + r;
+                const bool irow = i >= d.i0 && i < d.iend;
+                for (int c = lane_id; c < nj + 6; c += 32) {
+                    const int j = J0 - 3 + c;
+                    const long long o = (long long)i * P + j;
+                    V v;
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) {
+                        float x;
+                        if (irow && j >= d.i0 && j < d.iend) {
+                            x = __ldg(Qt[l] + o);
+                            if (hc) x = corrected(x, __ldg(gpc + o), corr[l]);
+                        } else {
+                            const Src<float> src{(const float *)S.Qin + (long long)(tr + l) * d.field, gpc, corr[l], hc};
+                            x = (float)ghost_value(src, d, S.lag_w, S.lag_k, p, i, j);
+                        }
+                        set_lane(v, l, x);
+                    }
+                    sQ[r * QJP + c] = v;
+                }
             }
         }
     }
     __syncthreads();
     // P1: x-lines over columns c in [-3, nj+3), cells [0, ni) -> Qx;
     //     y-lines over rows r in [-3, ni+3), cells [0, nj) -> Qy
+    // (one code path for both directions: the line's strides and records are arguments)
     {
         const int LX = round32(nj + 6), LY = round32(ni + 6);
-        const int jx = S.s1x * LX, jy = S.s1y * LY;
-        for (int job = tid; job < jx + jy; job += SWEEP_THREADS) {
-            if (job < jx) {
-                const int seg = job / LX, c = job - seg * LX - 3;
-                const int ma = ni * seg / S.s1x, mb = ni * (seg + 1) / S.s1x;
-                if (c >= nj + 3 || ma >= mb) continue;
-                const long long g0 = (long long)I0 * P + J0 + c;
-                Marcher<REC, SPL, M_SPLIT, QJP, QJP, V> mr;
-                mr.dtdx = dtdx;
-                mr.irdx = irdx;
-                mr.start(sQ + 3 * QJP + c + 3, erx + g0, crx + g0, P, ma);
-                mr.out = sQx + ma * QJP + c + 3;
-                mr.run(ma, mb, false);
-            } else {
-                const int jj = job - jx;
-                const int seg = jj / LY, r = jj - seg * LY - 3;
-                const int ma = nj * seg / S.s1y, mb = nj * (seg + 1) / S.s1y;
-                if (r >= ni + 3 || ma >= mb) continue;
-                const long long g0 = (long long)J0 * P + I0 + r;
-                Marcher<REC, SPL, M_SPLIT, 1, 1, V> mr;
-                mr.dtdx = dtdx;
-                mr.irdx = irdx;
-                mr.start(sQ + (r + 3) * QJP + 3, ery + g0, cry + g0, P, ma);
-                mr.out = sQy + (r + 3) * TJP + ma;
-                mr.run(ma, mb, false);
-            }
+        const int jx = S.s1x * LX, job = tid;
+        bool go = false;
+        const V *line = nullptr;
+        V *out = nullptr;
+        const float2 *er = nullptr, *cr = nullptr;
+        int ss = 1, os = 1, ma = 0, mb = 0;
+        if (job < jx) {
+            const int seg = job / LX, c = job - seg * LX - 3;
+            ma = ni * seg / S.s1x;
+            mb = ni * (seg + 1) / S.s1x;
+            go = c < nj + 3 && ma < mb;
+            const long long g0 = (long long)I0 * P + J0 + c;
+            line = sQ + 3 * QJP + c + 3;
+            ss = os = QJP;
+            er = erx + g0;
+            cr = crx + g0;
+            out = sQx + ma * QJP + c + 3;
+        } else if (job < jx + S.s1y * LY) {
+            const int jj = job - jx;
+            const int seg = jj / LY, r = jj - seg * LY - 3;
+            ma = nj * seg / S.s1y;
+            mb = nj * (seg + 1) / S.s1y;
+            go = r < ni + 3 && ma < mb;
+            const long long g0 = (long long)J0 * P + I0 + r;
+            line = sQ + (r + 3) * QJP + 3;
+            er = ery + g0;
+            cr = cry + g0;
+            out = sQy + (r + 3) * TJP + ma;
+        }
+        if (go) {
+            Marcher<REC, SPL, M_SPLIT, V> mr;
+            mr.dtdx = dtdx;
+            mr.irdx = irdx;
+            mr.start(line, ss, os, er, cr, P, ma);
+            mr.out = out;
+            mr.run(ma, mb);
         }
     }
     __syncthreads();
     // P2: y-lines of Qx over rows [0, ni): second-pass y-flux differences -> dY
     {
         const int LY = round32(ni);
-        const int jy = S.s2y * LY;
-        for (int job = tid; job < jy; job += SWEEP_THREADS) {
+        const int job = tid;
+        if (job < S.s2y * LY) {
             const int seg = job / LY, r = job - seg * LY;
             const int ma = nj * seg / S.s2y, mb = nj * (seg + 1) / S.s2y;
-            if (r >= ni || ma >= mb) continue;
-            const long long g0 = (long long)J0 * P + I0 + r;
-            Marcher<REC, SPL, M_DIFF, 1, 1, V> mr;
-            mr.dtdx = dtdx;
-            mr.irdx = irdx;
-            mr.start(sQx + r * QJP + 3, ery + g0, cry + g0, P, ma);
-            mr.out = sDy + r * TJP + ma;
-            mr.run(ma, mb, false);
+            if (r < ni && ma < mb) {
+                const long long g0 = (long long)J0 * P + I0 + r;
+                Marcher<REC, SPL, M_DIFF, V> mr;
+                mr.dtdx = dtdx;
+                mr.irdx = irdx;
+                mr.start(sQx + r * QJP + 3, 1, 1, ery + g0, cry + g0, P, ma);
+                mr.out = sDy + r * TJP + ma;
+                mr.run(ma, mb);
+            }
         }
     }
     __syncthreads();
@@ -484,36 +567,36 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
     V acc = bc<V>(0.f), accm = bc<V>(0.f);
     {
         const int LX = round32(nj);
-        const int jx = S.s2x * LX;
-        float *Qo0 = (float *)S.Qout + (long long)tr * d.field + pofs;
-        for (int job = tid; job < jx; job += SWEEP_THREADS) {
+        const int job = tid;
+        if (job < S.s2x * LX) {
             const int seg = job / LX, c = job - seg * LX;
             const int ma = ni * seg / S.s2x, mb = ni * (seg + 1) / S.s2x;
-            if (c >= nj || ma >= mb) continue;
-            const long long g0 = (long long)I0 * P + J0 + c;
-            Marcher<REC, SPL, M_UPDATE, TJP, TJP, V> mr;
-            mr.dtdx = dtdx;
-            mr.irdx = irdx;
-            mr.start(sQy + 3 * TJP + c, erx + g0, crx + g0, P, ma);
-            mr.dy = sDy + ma * TJP + c;
-            mr.qc = sQ + (ma + 3) * QJP + c + 3;
-            mr.qo0 = Qo0 + g0 + (long long)ma * P;
-            mr.qo1 = mr.qo0 + d.field;
-            mr.acc = acc;
-            mr.accm = accm;
-            mr.run(ma, mb, mfpr);
-            acc = mr.acc;
-            accm = mr.accm;
+            if (c < nj && ma < mb) {
+                const long long g0 = (long long)I0 * P + J0 + c;
+                Marcher<REC, SPL, M_UPDATE, V> mr;
+                mr.dtdx = dtdx;
+                mr.irdx = irdx;
+                mr.start(sQy + 3 * TJP + c, TJP, TJP, erx + g0, crx + g0, P, ma);
+                mr.dy = sDy + ma * TJP + c;
+                mr.qc = sQ + (ma + 3) * QJP + c + 3;
+                mr.qo0 = (float *)S.Qout + (long long)tr * d.field + pofs + g0 + (long long)ma * P;
+                mr.qo1 = mr.qo0 + d.field;
+                mr.acc = acc;
+                mr.accm = accm;
+                mr.run(ma, mb);
+                acc = mr.acc;
+                accm = mr.accm;
+            }
         }
     }
-    if (mfpr) {  // FP64 across threads, in a fixed order, per tracer
+    if (S.mfpr) {  // per tracer: FP32 within a warp (fixed butterfly order), FP64 across warps
         const bool anchor = S.mass_target != nullptr;
         const int nitems = NFACE * S.ntiles;
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
-            double dacc = (double)(anchor ? lane(accm, l) : lane(acc, l));
-            for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
-            if (lane_id == 0) red[l * NWARP + warp] = dacc;
+            float x = anchor ? lane(accm, l) : lane(acc, l);
+            for (int o = 16; o > 0; o >>= 1) x = __fadd_rn(x, __shfl_xor_sync(0xffffffffu, x, o));
+            if (lane_id == 0) red[l * NWARP + warp] = (double)x;
         }
         __syncthreads();
         if (tid < NL) {

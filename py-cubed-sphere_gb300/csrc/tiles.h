@@ -53,6 +53,7 @@ struct SweepSolve {
     int ntj, ntiles;        // tiles along j; tiles per panel (items = 6 ntiles)
     int s1x, s1y, s2y, s2x; // segments per line in P1 (x, y), P2, P3
     double dt, dx, a2;
+    float dtdx, irdx;       // dt / dx and 1 / dx rounded to FP32 (the FP32 kernel's step constants)
     const void *Qin;        // T fields, ghost cells filled
     void *Qout;             // T fields, interior written
     const double *corr_in;  // [T] pending MF-PR correction of Qin, or null
