@@ -104,7 +104,12 @@ int csadv_get_dt(const csadv_plan *plan, double *dt);
 /* q0_adv (advection_ic.py:208-210) evaluated on the device at the interior cell centres
  * (the reference's Q0 is a point value, advection_vars.py:105). */
 int csadv_init_tracer(csadv_plan *plan, int tracer, int ic, const double *ic_param, void *stream);
-/* simulation.Q = host array  /  host array = simulation.Q */
+/* simulation.Q = host array  /  host array = simulation.Q
+ * The host array is FP64 in the reference's layout.  Page-locked host memory (csadv_host_alloc,
+ * cudaMallocHost, cudaHostRegister) is read or written by the device directly, in one pass over
+ * the interconnect; pageable memory is staged through a device buffer.  csadv_set_tracer is
+ * ordered on the stream: the array must stay unchanged until the stream has passed the call.
+ * csadv_get_tracer returns when the array holds the field. */
 int csadv_set_tracer(csadv_plan *plan, int tracer, const double *host, int layout, void *stream);
 int csadv_get_tracer(csadv_plan *plan, int tracer, double *host, int layout, void *stream);
 
@@ -140,6 +145,12 @@ int csadv_set_graphs(csadv_plan *plan, int enable);
  * kernel; the whole step for the staged engine) and accumulate their durations in
  * csadv_stats.main_ms.  Profiled steps launch directly (no graph) and synchronise. */
 int csadv_set_profiling(csadv_plan *plan, int enable);
+/* Where the ET-DG ghost cells of a fused plan come from (interpolation.py:154-314): enable = 1
+ * (the default for FP32 plans) has the step kernel evaluate the ghost cells of its tiles from the
+ * neighbouring panels itself; enable = 0 fills them with a separate ghost-cell launch before each
+ * step (the default for FP64 plans).  Both give the same bits.  CSADV_ERR_UNSUPPORTED for a plan
+ * that does not run the line-marching step kernel.  Outside stream capture. */
+int csadv_set_inline_ghosts(csadv_plan *plan, int enable);
 typedef struct csadv_stats {
     long long steps;            /* steps advanced */
     long long kernel_launches;  /* kernels launched by steps (graph kernel nodes count once per replay) */

@@ -77,6 +77,7 @@ _SIGS = {
     "csadv_divergence": ([_vp, _c_int, _vp, _vp], _c_int),
     "csadv_set_graphs": ([_vp, _c_int], _c_int),
     "csadv_set_profiling": ([_vp, _c_int], _c_int),
+    "csadv_set_inline_ghosts": ([_vp, _c_int], _c_int),
     "csadv_get_stats": ([_vp, ctypes.POINTER(Stats)], _c_int),
     "csadv_reset_stats": ([_vp], _c_int),
     "csadv_batch_create": ([_c_int, ctypes.POINTER(_vp)], _c_int),

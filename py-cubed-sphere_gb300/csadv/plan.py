@@ -131,6 +131,9 @@ class Plan:
     def set_profiling(self, enable):
         L.check(L.lib().csadv_set_profiling(self._h, int(bool(enable))), "csadv_set_profiling")
 
+    def set_inline_ghosts(self, enable):
+        L.check(L.lib().csadv_set_inline_ghosts(self._h, int(bool(enable))), "csadv_set_inline_ghosts")
+
     def stats(self):
         st = L.Stats()
         L.check(L.lib().csadv_get_stats(self._h, ctypes.byref(st)), "csadv_get_stats")

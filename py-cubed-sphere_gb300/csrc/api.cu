@@ -191,7 +191,7 @@ int do_time_step(csadv_plan *pl, cudaStream_t st) {
 
 // the stored state equals the true state (no pending MF-PR correction)
 int settle(csadv_plan *pl, cudaStream_t st) {
-    if (!pl->f.on) return CSADV_OK;
+    if (!pl->f.on || pl->f.settled) return CSADV_OK;
     return fused_materialize(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
 }
 
@@ -257,6 +257,7 @@ int run_step(csadv_plan *pl, int kind, cudaStream_t st) {
         if (rc) return rc;
     }
     pl->stats.steps += 1;
+    if (pl->f.on) pl->f.settled = false;
     if (pl->prof) {
         CSADV_CUDA(cudaEventSynchronize(pl->pev[1]));
         float ms = 0.f;
@@ -460,6 +461,19 @@ int csadv_init_tracer(csadv_plan *pl, int tracer, int ic, const double *ic_param
     return rc;
 }
 
+// Page-locked host memory (cudaMallocHost, csadv_host_alloc, cudaHostRegister) is mapped into the
+// device's address space: the layout conversion then reads or writes the caller's array directly
+// (one pass over the interconnect, no staging copy).  Returns the device-side address of `host`, or
+// null for pageable memory, which goes through a copy into the plan's staging buffer.
+static double *mapped_host(const void *host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? (double *)a.devicePointer : nullptr;
+}
+
 int csadv_set_tracer(csadv_plan *pl, int tracer, const double *host, int layout, void *stream) {
     if (!pl || !host || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
     if (layout != CSADV_LAYOUT_FULL && layout != CSADV_LAYOUT_INTERIOR) return CSADV_ERR_ARG;
@@ -468,9 +482,13 @@ int csadv_set_tracer(csadv_plan *pl, int tracer, const double *host, int layout,
     cudaStream_t st = S(stream);
     int rc = settle(pl, st);
     if (rc) return rc;
-    CSADV_CUDA(cudaMemcpyAsync(pl->stage, host, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyHostToDevice, st));
-    rc = pl->opt.precision == 64 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, true, st)
-                                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, true, st);
+    double *src = mapped_host(host);
+    if (!src) {
+        CSADV_CUDA(cudaMemcpyAsync(pl->stage, host, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyHostToDevice, st));
+        src = pl->stage;
+    }
+    rc = pl->opt.precision == 64 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), src, layout, true, st)
+                                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), src, layout, true, st);
     if (!rc && pl->f.on) rc = fused_anchor_mass(pl->opt, pl->grid, pl->f, pl->cur, tracer, st);
     return rc;
 }
@@ -489,11 +507,13 @@ int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void 
         rc = fused_ghosts_to_current(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
         if (rc) return rc;
     }
+    double *dst = mapped_host(host);
     rc = pl->opt.precision == 64
-                 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), pl->stage, layout, false, st)
-                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), pl->stage, layout, false, st);
+                 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), dst ? dst : pl->stage, layout, false, st)
+                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), dst ? dst : pl->stage, layout, false, st);
     if (rc) return rc;
-    CSADV_CUDA(cudaMemcpyAsync(host, pl->stage, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (!dst)
+        CSADV_CUDA(cudaMemcpyAsync(host, pl->stage, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyDeviceToHost, st));
     CSADV_CUDA(cudaStreamSynchronize(st));
     return CSADV_OK;
 }
@@ -579,6 +599,21 @@ int csadv_set_graphs(csadv_plan *pl, int enable) {
     if (!pl) return CSADV_ERR_ARG;
     pl->drop_graphs();
     pl->graphs = enable != 0;
+    return CSADV_OK;
+}
+
+int csadv_set_inline_ghosts(csadv_plan *pl, int enable) {
+    if (!pl) return CSADV_ERR_ARG;
+    if (!pl->f.on || !pl->f.sweep) return CSADV_ERR_UNSUPPORTED;
+    if (pl->f.inline_ghosts == (enable != 0)) return CSADV_OK;
+    cudaStream_t st = (cudaStream_t)0;
+    int rc = settle(pl, st);
+    if (rc) return rc;
+    pl->f.inline_ghosts = enable != 0;
+    rc = fused_set_tile(pl->opt, pl->grid, pl->T, pl->dt, pl->f, pl->f.tile, st);
+    if (rc) return rc;
+    pl->drop_graphs();
+    batch_touch(pl);
     return CSADV_OK;
 }
 

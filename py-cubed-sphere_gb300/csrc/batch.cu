@@ -95,7 +95,7 @@ int batch_rebuild(csadv_batch *b, cudaStream_t st) {
                                    st));
         b->base_cur.push_back(pl->cur);
         total += pl->f.nitems;
-        htotal += pl->T * halo_blocks(pl->grid.d);
+        if (!pl->f.inline_ghosts) htotal += pl->T * halo_blocks(pl->grid.d);
         b->smem = b->smem > pl->f.smem ? b->smem : pl->f.smem;
     }
     const int need = total > htotal ? total : htotal;
@@ -123,7 +123,7 @@ int batch_rebuild(csadv_batch *b, cudaStream_t st) {
             h[e] = make_int2(2 * m + pl->cur, it);
             h[total + e] = make_int2(2 * m + (1 - pl->cur), it);
         }
-        const int hb = pl->T * halo_blocks(pl->grid.d);
+        const int hb = pl->f.inline_ghosts ? 0 : pl->T * halo_blocks(pl->grid.d);
         for (int it = 0; it < hb; ++it, ++eh) {
             hh[eh] = make_int2(2 * m + pl->cur, it);
             hh[htotal + eh] = make_int2(2 * m + (1 - pl->cur), it);
@@ -154,6 +154,7 @@ bool batch_stale(const csadv_batch *b) {
 
 int batch_step_work(csadv_batch *b, int kind, cudaStream_t st) {
     // ghost cells of every solve in one launch, then each plan's wind work (time-dependent winds)
+    // (solves whose step kernel evaluates their ghost cells itself have no items in it)
     int rc0 = b->precision == 64 ? launch_halo_batch<double>(b->dsolves, b->dhwork[b->phase], b->nhwork, st)
                                  : launch_halo_batch<float>(b->dsolves, b->dhwork[b->phase], b->nhwork, st);
     if (rc0) return rc0;
@@ -209,6 +210,7 @@ int batch_run_step(csadv_batch *b, int kind, cudaStream_t st) {
     for (csadv_plan *pl : b->plans) {
         pl->cur = 1 - pl->cur;
         pl->k += 1;
+        pl->f.settled = false;
         pl->stats.steps += 1;
     }
     b->phase ^= 1;

@@ -97,6 +97,8 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     const Dims d = g.d;
     const size_t es = o.precision == 64 ? sizeof(double) : sizeof(float);
     f.on = true;
+    // the FP32 step kernel evaluates the ET-DG ghost cells of its tiles itself (no ghost-cell launch)
+    f.inline_ghosts = o.precision == 32;
     f.Qbuf[1] = mem.alloc<char>((long long)T * d.field * es);
     for (int b = 0; b < 2; ++b) f.corr[b] = mem.alloc<double>(T);
     int maxb = 0;
@@ -243,6 +245,8 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.lag_k = f.inline_ghosts ? g.lag_k : nullptr;
         s.hlag_w = g.lag_w;
         s.hlag_k = g.lag_k;
+        s.lag_wf = f.inline_ghosts ? g.lag_wf : nullptr;
+        s.hlag_wf = g.lag_wf;
     }
     f.nitems = NFACE * h[0].ntiles;
     f.smem = o.precision == 64 ? sweep_smem_bytes<double>(f.scfg) : sweep_smem_bytes<float>(f.scfg);
@@ -363,6 +367,7 @@ int fused_materialize(const Options &o, const Grid &g, int T, FusedState &f, int
         k_materialize<float><<<grid, 256, 0, st>>>((float *)f.Qbuf[cur], d, (const float *)f.g_pc, f.corr[cur]);
     CSADV_CUDA(cudaGetLastError());
     CSADV_CUDA(cudaMemsetAsync(f.corr[cur], 0, T * sizeof(double), st));
+    f.settled = true;
     return CSADV_OK;
 }
 

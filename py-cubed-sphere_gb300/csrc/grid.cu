@@ -222,12 +222,19 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     if (rc != CSADV_OK) return rc;
     double *lag_w = mem.alloc<double>(lw.size());
     int *lag_k = mem.alloc<int>(lk.size());
+    float2 *lag_wf = mem.alloc<float2>(lw.size());
+    std::vector<float2> lwf(lw.size());
+    for (size_t e = 0; e < lw.size(); ++e) {
+        const float hi = (float)lw[e];
+        lwf[e] = make_float2(hi, (float)(lw[e] - (double)hi));
+    }
     if (!mem.ok()) return CSADV_ERR_OOM;
     for (double *g : {g_pc, g_pu, g_pv}) CSADV_CUDA(cudaMemsetAsync(g, 0, P1 * sizeof(double), st));
     CSADV_CUDA(cudaMemcpyAsync(xs_dev, xc.data(), xc.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(xs_dev + xc.size(), xe.data(), xe.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(lag_w, lw.data(), lw.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(lag_k, lk.data(), lk.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaMemcpyAsync(lag_wf, lwf.data(), lwf.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
     const double *xcd = xs_dev, *xed = xs_dev + xc.size();
     const int n = d.n;
     PointOut o;
@@ -256,6 +263,7 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     for (int c = 0; c < 4; ++c) grid.cc[c] = cc[c];
     grid.lag_w = lag_w;
     grid.lag_k = lag_k;
+    grid.lag_wf = lag_wf;
     grid.a2 = a2h;
     return CSADV_OK;
 }

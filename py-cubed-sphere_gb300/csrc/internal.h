@@ -123,6 +123,7 @@ int wind_cfl(const Options &o, const Grid &g, const Winds &w, double dt, double 
 // ---------------------------------------------------------------- fused engine state
 struct FusedState {
     bool on = false;
+    bool settled = true;        // host record: no MF-PR correction is pending in Qbuf[cur]
     int tile = 1;               // 0-3: k_fused (FUSED_TILES), 4-7: k_sweep (SWEEP_TILES[tile - 4])
     void *Qbuf[2] = {nullptr, nullptr};
     double *corr[2] = {nullptr, nullptr};  // [T] pending MF-PR correction of Qbuf[b]

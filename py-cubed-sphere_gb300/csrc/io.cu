@@ -33,17 +33,43 @@ __device__ __forceinline__ long long host_index(const Dims &d, int layout, int p
     return ((long long)(i - d.i0) * d.N + (j - d.i0)) * NFACE + p;
 }
 
-template <class real>
-__global__ void k_io(Dims d, real *Q, double *stage, int layout, int to_native) {
+// Reference layout A[i][j][p] (p fastest) <-> native planes, 128 cells per block: the block's
+// 768 host values form one contiguous range, copied between the host array and shared memory
+// with consecutive lanes on consecutive addresses (16 bytes per lane when the host array is
+// 16-byte aligned), so the interconnect sees whole lines; each thread then moves the six panel
+// values of one cell, consecutive threads on consecutive columns of each plane.  `host` may be a
+// device buffer or page-locked host memory mapped into the device.
+constexpr int IO_B = 128;
+template <class real, bool VEC>
+__global__ void k_io(Dims d, real *Q, double *host, int layout, int to_native) {
+    __shared__ __align__(16) double s[IO_B * NFACE];
     const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
     const int off = layout == CSADV_LAYOUT_FULL ? 0 : d.i0;
-    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (tid >= (long long)NFACE * m * m) return;
-    // host-contiguous order: p fastest
-    int p = (int)(tid % NFACE), j = off + (int)((tid / NFACE) % m), i = off + (int)(tid / ((long long)NFACE * m));
-    long long o = at(d, p, i, j);
-    if (to_native) Q[o] = (real)stage[tid];
-    else stage[tid] = (double)Q[o];
+    const long long cell0 = (long long)blockIdx.x * IO_B, ncell = (long long)m * m;
+    const int nc = (int)(ncell - cell0 < IO_B ? ncell - cell0 : IO_B);
+    double *h = host + cell0 * NFACE;
+    const int tid = threadIdx.x;
+    const long long cell = cell0 + tid;
+    const long long o = (long long)(off + cell / m) * d.pitch + off + cell % m;
+    if (to_native) {
+        if (VEC)
+            for (int e = tid; e < nc * NFACE / 2; e += IO_B) ((double2 *)s)[e] = ((const double2 *)h)[e];
+        else
+            for (int e = tid; e < nc * NFACE; e += IO_B) s[e] = h[e];
+        __syncthreads();
+        if (tid < nc)
+#pragma unroll
+            for (int p = 0; p < NFACE; ++p) Q[p * d.plane + o] = (real)s[tid * NFACE + p];
+    } else {
+        if (tid < nc)
+#pragma unroll
+            for (int p = 0; p < NFACE; ++p) s[tid * NFACE + p] = (double)Q[p * d.plane + o];
+        __syncthreads();
+        if (VEC)
+            for (int e = tid; e < nc * NFACE / 2; e += IO_B) ((double2 *)h)[e] = ((const double2 *)s)[e];
+        else
+            for (int e = tid; e < nc * NFACE; e += IO_B) h[e] = s[e];
+    }
 }
 
 template <class real>
@@ -143,8 +169,11 @@ int init_tracer(const Grid &g, int ic, int vf, const IcParams &prm, real *Q, cud
 template <class real>
 int tracer_io(const Grid &g, real *Q, double *dev_stage, int layout, bool to_native, cudaStream_t st) {
     const int m = layout == CSADV_LAYOUT_FULL ? g.d.n : g.d.N;
-    long long tot = (long long)NFACE * m * m;
-    k_io<real><<<ceil_div(tot, 256), 256, 0, st>>>(g.d, Q, dev_stage, layout, to_native ? 1 : 0);
+    const long long tot = (long long)m * m;
+    if (((uintptr_t)dev_stage & 15) == 0)
+        k_io<real, true><<<ceil_div(tot, IO_B), IO_B, 0, st>>>(g.d, Q, dev_stage, layout, to_native ? 1 : 0);
+    else
+        k_io<real, false><<<ceil_div(tot, IO_B), IO_B, 0, st>>>(g.d, Q, dev_stage, layout, to_native ? 1 : 0);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }

@@ -440,62 +440,75 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
             Qt[l] = (const float *)S.Qin + (long long)(tr + l) * d.field + pofs;
             corr[l] = hc ? (float)S.corr_in[tr + l] : 0.f;
         }
-        if (S.lag_w == nullptr) {
-            constexpr int RR = 4, CC = (SWEEP_TMAX + 6 + 31) / 32;  // cells per batch: RR x CC
-            for (int r0 = warp; r0 < ni + 6; r0 += RR * NWARP) {
-                float q[RR][CC][NL], g[RR][CC];
+        // interior cells, and ghost cells as the ghost-cell kernel filled them (or, with inline
+        // ghost cells, left for the evaluation below)
+        const bool inl = S.lag_w != nullptr;
+        constexpr int RR = 4, CC = (SWEEP_TMAX + 6 + 31) / 32;  // cells per batch: RR x CC
+        for (int r0 = warp; r0 < ni + 6; r0 += RR * NWARP) {
+            float q[RR][CC][NL], g[RR][CC];
 #pragma unroll
-                for (int a = 0; a < RR; ++a) {
-                    const int r = r0 + a * NWARP, i = I0 - 3 + r;
-                    const float *q0 = Qt[0] + (long long)i * P + J0 - 3 + lane_id;
+            for (int a = 0; a < RR; ++a) {
+                const int r = r0 + a * NWARP, i = I0 - 3 + r;
+                const float *q0 = Qt[0] + (long long)i * P + J0 - 3 + lane_id;
 #pragma unroll
-                    for (int b = 0; b < CC; ++b) {
-                        if (r < ni + 6 && lane_id + 32 * b < nj + 6) {
+                for (int b = 0; b < CC; ++b) {
+                    if (r < ni + 6 && lane_id + 32 * b < nj + 6) {
 #pragma unroll
-                            for (int l = 0; l < NL; ++l) q[a][b][l] = __ldg(q0 + 32 * b + (l ? d.field : 0));
-                            g[a][b] = hc ? __ldg(gpc + (q0 - Qt[0]) + 32 * b) : 0.f;
-                        }
-                    }
-                }
-#pragma unroll
-                for (int a = 0; a < RR; ++a) {
-                    const int r = r0 + a * NWARP, i = I0 - 3 + r;
-#pragma unroll
-                    for (int b = 0; b < CC; ++b) {
-                        const int c = lane_id + 32 * b, j = J0 - 3 + c;
-                        if (r < ni + 6 && c < nj + 6) {
-                            const bool in = hc && i >= d.i0 && i < d.iend && j >= d.i0 && j < d.iend;
-                            V v;
-#pragma unroll
-                            for (int l = 0; l < NL; ++l)
-                                set_lane(v, l, in ? corrected(q[a][b][l], g[a][b], corr[l]) : q[a][b][l]);
-                            sQ[r * QJP + c] = v;
-                        }
+                        for (int l = 0; l < NL; ++l) q[a][b][l] = __ldg(q0 + 32 * b + (l ? d.field : 0));
+                        g[a][b] = hc ? __ldg(gpc + (q0 - Qt[0]) + 32 * b) : 0.f;
                     }
                 }
             }
-        } else {  // ghost cells evaluated here from the neighbouring panels (ET-DG)
-            for (int r = warp; r < ni + 6; r += NWARP) {
-                const int i = I0 - 3 + r;
-                const bool irow = i >= d.i0 && i < d.iend;
-                for (int c = lane_id; c < nj + 6; c += 32) {
-                    const int j = J0 - 3 + c;
-                    const long long o = (long long)i * P + j;
-                    V v;
 #pragma unroll
-                    for (int l = 0; l < NL; ++l) {
-                        float x;
-                        if (irow && j >= d.i0 && j < d.iend) {
-                            x = __ldg(Qt[l] + o);
-                            if (hc) x = corrected(x, __ldg(gpc + o), corr[l]);
-                        } else {
-                            const Src<float> src{(const float *)S.Qin + (long long)(tr + l) * d.field, gpc, corr[l], hc};
-                            x = (float)ghost_value(src, d, S.lag_w, S.lag_k, p, i, j);
-                        }
-                        set_lane(v, l, x);
+            for (int a = 0; a < RR; ++a) {
+                const int r = r0 + a * NWARP, i = I0 - 3 + r;
+#pragma unroll
+                for (int b = 0; b < CC; ++b) {
+                    const int c = lane_id + 32 * b, j = J0 - 3 + c;
+                    const bool interior = i >= d.i0 && i < d.iend && j >= d.i0 && j < d.iend;
+                    if (r < ni + 6 && c < nj + 6 && (interior || !inl)) {
+                        V v;
+#pragma unroll
+                        for (int l = 0; l < NL; ++l)
+                            set_lane(v, l, interior && hc ? corrected(q[a][b][l], g[a][b], corr[l]) : q[a][b][l]);
+                        sQ[r * QJP + c] = v;
                     }
-                    sQ[r * QJP + c] = v;
                 }
+            }
+        }
+        if (inl) {
+            // inline ghost cells (ET-DG, interpolation.py:154-314): the part of the tile's 3-cell
+            // ring outside the panel, from the neighbouring panels' interior values, with the
+            // same device functions (and so the same bits) as the ghost-cell kernel.  Strips:
+            // rows [-3, 0) / [ni, ni+3) over the full width at the panel's first / last row; then
+            // columns [-3, 0) / [nj, nj+3) at its first / last column, over the ring's rows that
+            // those row strips do not cover.
+            const bool wr = I0 == d.i0, er = I0 + ni == d.iend;
+            const int W6 = nj + 6, r_lo = wr ? 0 : -3, nr = (er ? ni : ni + 3) - r_lo;
+            const int cw = wr ? 3 * W6 : 0, ce = er ? 3 * W6 : 0;
+            const int cs = J0 == d.i0 ? 3 * nr : 0, cn = J0 + nj == d.iend ? 3 * nr : 0;
+            for (int k = tid; k < cw + ce + cs + cn; k += SWEEP_THREADS) {
+                int r, c;
+                if (k < cw) {
+                    r = -3 + k / W6;
+                    c = -3 + k % W6;
+                } else if (k < cw + ce) {
+                    r = ni + (k - cw) / W6;
+                    c = -3 + (k - cw) % W6;
+                } else if (k < cw + ce + cs) {
+                    r = r_lo + (k - cw - ce) / 3;
+                    c = -3 + (k - cw - ce) % 3;
+                } else {
+                    r = r_lo + (k - cw - ce - cs) / 3;
+                    c = nj + (k - cw - ce - cs) % 3;
+                }
+                V v;
+#pragma unroll
+                for (int l = 0; l < NL; ++l) {
+                    const Src<float> src{(const float *)S.Qin + (long long)(tr + l) * d.field, gpc, corr[l], hc};
+                    set_lane(v, l, ghost_value_f(src, d, S.lag_wf, S.lag_k, p, I0 + r, J0 + c));
+                }
+                sQ[(r + 3) * QJP + c + 3] = v;
             }
         }
     }

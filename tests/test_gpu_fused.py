@@ -179,3 +179,53 @@ def test_fp32_mass_anchored_over_long_run():
         pl.advance(2000)
         for t in range(2):
             assert abs(pl.mass(t) - m0[t]) <= 1e-6 * abs(m0[t])
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+def test_inline_ghost_cells_match_ghost_cell_kernel(prec):
+    """The step kernel's own ghost cells (the FP32 default) and the separate ghost-cell launch
+    (the FP64 default) give the same bits: N = 48 (one tile per panel: every tile touches all
+    four panel edges and the corners), N = 120 (interior tiles too), three tracers (a pair and
+    an odd one), time-dependent wind with RK2 and MF-PR, several steps; the full-layout fields
+    (ghost cells included) agree as well."""
+    for N in (48, 120):
+        c = (2, 2, 1, 3, 1, 3)
+        with plan(N, 0.004, c, 2, ntracers=3, precision=prec, engine=FUSED, tile=5) as a, \
+                plan(N, 0.004, c, 2, ntracers=3, precision=prec, engine=FUSED, tile=5) as b:
+            a.set_inline_ghosts(True)
+            b.set_inline_ghosts(False)
+            for pl in (a, b):
+                for t in range(3):
+                    pl.init_tracer(101 + t % 3, ic_param=(0.4 * t, 0.3, 5.0, 0.0) if t == 0 else None, tracer=t)
+                pl.advance(4)
+            for t in range(3):
+                np.testing.assert_array_equal(a.get_tracer(t), b.get_tracer(t))
+                np.testing.assert_array_equal(a.get_tracer(t, full=True), b.get_tracer(t, full=True))
+            assert a.mass(2) == b.mass(2)
+
+
+def test_fp32_ghost_cells_equal_fp64_interpolation_rounded():
+    """The FP32 form sums the Lagrange interpolation in double-float arithmetic (FP64 weights as
+    two FP32 words).  On the same FP32-representable field, its ghost cells equal the FP64 form's
+    ghost cells rounded to FP32 to one unit in the last place; the side strips exactly, for all
+    but a tiny fraction (values next to a rounding boundary).  The corner blocks interpolate
+    side-strip values that the FP32 form holds in FP32 (the reference's two-level rule applied
+    to an FP32 array), so there the two forms differ by a rounding."""
+    rng = np.random.default_rng(11)
+    N = 40
+    q = (1.0 + 0.5 * rng.standard_normal((N, N, 6))).astype(np.float32).astype(np.float64)
+    full = {}
+    for prec in (64, 32):
+        with plan(N, 1e-4, (2, 2, 1, 3, 1, 3), 1, precision=prec, engine=FUSED) as pl:
+            pl.set_tracer(q)
+            pl.advance(1)
+            full[prec] = pl.get_tracer(full=True)
+    inside = np.zeros(N + 8, bool)
+    inside[4:N + 4] = True
+    ghost = ~np.outer(inside, inside)
+    side = np.outer(inside, ~inside) | np.outer(~inside, inside)
+    ulp = np.abs(full[64].astype(np.float32).view(np.int32).astype(np.int64) -
+                 full[32].astype(np.float32).view(np.int32).astype(np.int64))
+    assert ulp[ghost & ~side].max() <= 4  # corner blocks: weights up to ~2 on inputs one rounding apart
+    assert ulp[side].max() <= 1
+    assert np.count_nonzero(ulp[side]) <= max(2, ulp[side].size // 1000)

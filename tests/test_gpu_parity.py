@@ -114,6 +114,47 @@ def test_set_get_roundtrip_and_layouts():
             pl.set_tracer(np.zeros((5, 5, 6)))
 
 
+def test_set_get_page_locked_host_memory():
+    """Page-locked host arrays are read and written by the device directly (no staging copy):
+    the same fields as through pageable arrays, for both layouts, FP64 and FP32 state, across a
+    step with a pending MF-PR correction."""
+    import ctypes
+    from csadv import Plan, _lib
+    L = _lib.lib()
+    rng = np.random.default_rng(7)
+    N, n = 16, 24
+    bufs = []
+    try:
+        for shp in ((n, n, 6), (N, N, 6)):
+            p = ctypes.c_void_p()
+            _lib.check(L.csadv_host_alloc(ctypes.byref(p), int(np.prod(shp)) * 8))
+            bufs.append((p, np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_double)), shape=shp)))
+        for prec in (64, 32):
+            with Plan(N, 0.01, recon=2, dp=2, opsplit=1, et=3, mt=1, mf=3, vf=2, ntracers=2, precision=prec) as pa, \
+                    Plan(N, 0.01, recon=2, dp=2, opsplit=1, et=3, mt=1, mf=3, vf=2, ntracers=2, precision=prec) as pb:
+                full = 1.0 + 0.1 * rng.standard_normal((n, n, 6))
+                bufs[0][1][...] = full
+                pa.set_tracer(full, tracer=1)
+                _lib.check(L.csadv_set_tracer(pb._h, 1, bufs[0][0], _lib.LAYOUT_FULL, pb.stream))
+                pa.init_tracer(2)
+                pb.init_tracer(2)
+                pa.advance(3)
+                pb.advance(3)
+                for t in range(2):
+                    for k, full_layout in ((0, True), (1, False)):
+                        _lib.check(L.csadv_get_tracer(pb._h, t, bufs[k][0],
+                                                      _lib.LAYOUT_FULL if full_layout else _lib.LAYOUT_INTERIOR,
+                                                      pb.stream))
+                        np.testing.assert_array_equal(bufs[k][1], pa.get_tracer(t, full=full_layout))
+                inner = rng.standard_normal((N, N, 6))
+                bufs[1][1][...] = inner
+                _lib.check(L.csadv_set_tracer(pb._h, 0, bufs[1][0], _lib.LAYOUT_INTERIOR, pb.stream))
+                np.testing.assert_array_equal(pb.get_tracer(0), inner if prec == 64 else inner.astype(np.float32))
+    finally:
+        for p, _ in bufs:
+            L.csadv_host_free(p)
+
+
 def test_several_tracers_equal_single_runs():
     c, vf, dt = (2, 2, 1, 3, 1, 3), 2, 0.01
     with plan(16, dt, c, vf, ntracers=3) as pl:
