@@ -124,6 +124,7 @@ struct Winds {
     // fused engine: the time-dependent wind as coefficient fields of a time basis on every
     // edge (ghost edges included), nbasis fields per direction; 0 = not used
     void *btab[2] = {nullptr, nullptr};
+    void *btabT = nullptr;        // FP32: the y-edge coefficients transposed ([j][i], as the y-edge records)
     int nbasis = 0;
 };
 

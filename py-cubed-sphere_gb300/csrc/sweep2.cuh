@@ -407,6 +407,10 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
     const float *gpc = (const float *)S.gpc;
     const bool hc = S.corr_in != nullptr;
 
+    // the pending MF-PR corrections of the pair, rounded to FP32 once per CTA (GB300 converts from
+    // FP64 at the FP64 rate) and shared through shared memory
+    float *scorr = (float *)(red + SWEEP_THREADS - 2);
+    if (tid < NL) scorr[tid] = hc ? (float)S.corr_in[tr + tid] : 0.f;
     // The first-pass lines read the edge and cell records of the tile from global memory, one to
     // two cells ahead of their use; after the records have left L2 (the first pair of a step)
     // that is not far enough to hide a DRAM access, so every thread first asks L2 for a few
@@ -429,6 +433,7 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
             asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
         }
     }
+    __syncthreads();
 
     // P0: Q on the tile + 3 halo cells; interior cells with the pending MF-PR correction.  Warp w
     // takes rows w, w + 8, ...; all loads of a thread are issued before its first store.
@@ -438,7 +443,7 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
             Qt[l] = (const float *)S.Qin + (long long)(tr + l) * d.field + pofs;
-            corr[l] = hc ? (float)S.corr_in[tr + l] : 0.f;
+            corr[l] = scorr[l];
         }
         // interior cells, and ghost cells as the ghost-cell kernel filled them (or, with inline
         // ghost cells, left for the evaluation below)

@@ -127,7 +127,16 @@ struct Clock {
     double f[4];  // deformational: k cos(pi t/T), sin(2 pi t/T), cos(2 pi t/T), 2 pi/T; vf 3: cos(pi t/5)
     double t_old; // time of the previous wind (RK2 extrapolation)
     double hn[4], ho[4];  // time-basis values at t and t_old (basis winds, see wind_basis_h)
+    float hnf[4], hof[4]; // the same rounded to FP32 (GB300 converts FP64 at the FP64 rate: once here,
+                          // not in every thread of the FP32 record kernel)
 };
+
+__device__ __forceinline__ void clock_round(Clock *c) {
+    for (int m = 0; m < 4; ++m) {
+        c->hnf[m] = (float)c->hn[m];
+        c->hof[m] = (float)c->ho[m];
+    }
+}
 
 __device__ void clock_factors(Clock *c, WindParams wp, int kind) {
     const double t = c->t;
@@ -156,6 +165,7 @@ __global__ void k_clock_tick(Clock *c, WindParams wp, int kind, int factors) {
     } else {
         for (int m = 0; m < 4; ++m) c->ho[m] = c->hn[m];
         wind_basis_h(wp, kind, c->t, c->hn);
+        clock_round(c);
     }
 }
 __global__ void k_clock_set(Clock *c, long long k, double t, WindParams wp, int kind, int factors) {
@@ -167,6 +177,7 @@ __global__ void k_clock_set(Clock *c, long long k, double t, WindParams wp, int 
     } else {
         wind_basis_h(wp, kind, c->t_old, c->ho);
         wind_basis_h(wp, kind, c->t, c->hn);
+        clock_round(c);
     }
 }
 
@@ -240,7 +251,13 @@ __global__ void k_wind_basis(Grid g, WindParams wp, int m, int tkind, W *u, W *v
 template <class W, int M>
 struct Coefs {
     W c[M];
-    __device__ __forceinline__ Coefs(const W *__restrict__ B, long long o) {
+    Coefs() = default;
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int m = 0; m < M; ++m) c[m] = W(0);
+    }
+    __device__ __forceinline__ Coefs(const W *__restrict__ B, long long o) { load(B, o); }
+    __device__ __forceinline__ void load(const W *__restrict__ B, long long o) {
         if constexpr (M == 4) {
             if constexpr (sizeof(W) == 4) {
                 const float4 v = *reinterpret_cast<const float4 *>(B + o * 4);
@@ -280,28 +297,39 @@ __global__ void k_wind_step(Dims d, const W *__restrict__ bu, const W *__restric
     const int lane = threadIdx.x, wy = threadIdx.y, tid = wy * 32 + lane;
     if (tid < 8) (tid < 4 ? hn : ho)[tid & 3] = (W)(tid < 4 ? clk->hn[tid] : clk->ho[tid - 4]);
     __syncthreads();
-    // the wind now and 1.5 u - 0.5 u_old (the RK2 extrapolation) of edge (i, j), zero outside the plane
-    for (int e = tid; e < 34 * 32; e += 256) {
-        const int r = e >> 5, c = e & 31, i = ib - 1 + r, j = jb + c;
-        W sn = W(0), so = W(0);
-        if (i >= 0 && i <= d.n && j < d.pitch) {
-            const Coefs<W, M> cf(bu, at(d, p, i, j));
-            sn = cf.at(hn);
-            so = cf.at(ho);
+    // the wind now and 1.5 u - 0.5 u_old (the RK2 extrapolation) of edge (i, j), zero outside the
+    // plane; every coefficient load of a thread is issued before the first is used
+    constexpr int NE = (34 * 32 + 255) / 256;
+    Coefs<W, M> cx[NE], cy[NE];
+#pragma unroll
+    for (int q = 0; q < NE; ++q) {
+        const int e = tid + 256 * q;
+        {
+            const int r = e >> 5, c = e & 31, i = ib - 1 + r, j = jb + c;
+            if (e < 34 * 32 && i >= 0 && i <= d.n && j < d.pitch) cx[q].load(bu, at(d, p, i, j));
+            else cx[q].zero();
         }
-        xs[r][c] = W(1.5) * sn - W(0.5) * so;
-        if (r >= 1 && r <= 32) xn[r - 1][c] = sn;
+        {
+            const int r = e / 34, c = e - r * 34, i = ib + r, j = jb - 1 + c;
+            if (e < 32 * 34 && i <= d.n && j >= 0 && j < d.pitch) cy[q].load(bv, at(d, p, i, j));
+            else cy[q].zero();
+        }
     }
-    for (int e = tid; e < 32 * 34; e += 256) {
-        const int r = e / 34, c = e - r * 34, i = ib + r, j = jb - 1 + c;
-        W sn = W(0), so = W(0);
-        if (i <= d.n && j >= 0 && j < d.pitch) {
-            const Coefs<W, M> cf(bv, at(d, p, i, j));
-            sn = cf.at(hn);
-            so = cf.at(ho);
+#pragma unroll
+    for (int q = 0; q < NE; ++q) {
+        const int e = tid + 256 * q;
+        if (e < 34 * 32) {
+            const int r = e >> 5, c = e & 31;
+            const W sn = cx[q].at(hn), so = cx[q].at(ho);
+            xs[r][c] = W(1.5) * sn - W(0.5) * so;
+            if (r >= 1 && r <= 32) xn[r - 1][c] = sn;
         }
-        ys[r][c] = W(1.5) * sn - W(0.5) * so;
-        if (c >= 1 && c <= 32) yn[r][c - 1] = sn;
+        if (e < 32 * 34) {
+            const int r = e / 34, c = e - r * 34;
+            const W sn = cy[q].at(hn), so = cy[q].at(ho);
+            ys[r][c] = W(1.5) * sn - W(0.5) * so;
+            if (c >= 1 && c <= 32) yn[r][c - 1] = sn;
+        }
     }
     __syncthreads();
     // averaged_velocity.py:14-62, given the wind and the three extrapolated winds along the line
@@ -844,6 +872,80 @@ __global__ void k_interleave(const W *__restrict__ src, W *dst, long long n, int
     if (o < n) dst[o * M + m] = src[o];
 }
 
+// dst(a, b) = src(b, a) for the M interleaved coefficients of every edge of each plane, a <= n,
+// b < n (the y-edge index range); zero elsewhere
+template <class W>
+__global__ void k_transpose_coefs(const W *__restrict__ src, W *dst, Dims d, int M) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= d.field) return;
+    const int p = (int)(t / d.plane);
+    const long long r = t % d.plane;
+    const int a = (int)(r / d.pitch), b = (int)(r % d.pitch);
+    const bool in = a <= d.n && b < d.n;
+    for (int m = 0; m < M; ++m) dst[t * M + m] = in ? src[(p * d.plane + (long long)b * d.pitch + a) * M + m] : W(0);
+}
+
+// Edge records of one step of the FP32 form from the basis: the x problem (coefficients bu, metric
+// gpu, records erx) and the y problem in transposed coordinates (bvT, gpvT, ery) are the same
+// computation, blockIdx.z = problem * 6 + panel.  A block covers 32 x 32 edges (rows ib.., columns
+// jb..): the wind at the clock's current and previous times and the RK2 extrapolation
+// 1.5 u - 0.5 u_old on rows ib-1 .. ib+32 into shared memory, then the departure-point average
+// along the row index (averaged_velocity.py:14-62) and the record {u_avg, +-g}.  Every coefficient
+// load of a thread is issued before the first is used.
+template <int M>
+__global__ void __launch_bounds__(256) k_wind_rec(Dims d, const float *__restrict__ bu, const float *__restrict__ bvT,
+                                                  const Clock *__restrict__ clk, const float *__restrict__ gpu,
+                                                  const float *__restrict__ gpvT, float2 *erx, float2 *ery, int rk2,
+                                                  float c_half) {
+    __shared__ float sx[34][33];  // extrapolated winds, rows ib-1 .. ib+32
+    __shared__ float sn[32][33];  // winds now, rows ib .. ib+31
+    const bool ydir = blockIdx.z >= NFACE;
+    const int p = blockIdx.z - (ydir ? NFACE : 0);
+    const float *B = ydir ? bvT : bu;
+    const float *G = ydir ? gpvT : gpu;
+    float2 *E = (ydir ? ery : erx) + p * d.plane;
+    const int jb = blockIdx.x * 32, ib = blockIdx.y * 32, lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
+    const int j = jb + lane;
+    float hn[M], ho[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        hn[m] = clk->hnf[m];
+        ho[m] = clk->hof[m];
+    }
+    constexpr int NQ = 5;  // rows wy + 8 q, q < 5, cover the 34 rows
+    Coefs<float, M> c[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const int r = wy + 8 * q, i = ib - 1 + r;
+        if (r < 34 && i >= 0 && i <= d.n && j < d.pitch) c[q].load(B, p * d.plane + (long long)i * d.pitch + j);
+        else c[q].zero();
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const int r = wy + 8 * q;
+        if (r < 34) {
+            const float un = c[q].at(hn), uo = c[q].at(ho);
+            sx[r][lane] = 1.5f * un - 0.5f * uo;
+            if (r >= 1 && r <= 32) sn[r - 1][lane] = un;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int r = wy + 8 * k, i = ib + r;
+        if (i > d.n || j >= d.pitch) continue;
+        const float u = sn[r][lane];
+        float au = u;
+        if (rk2) {
+            const float a = u * c_half;
+            au = (j < d.n && i >= d.i0 && i <= d.iend)
+                     ? (u >= 0.f ? (1.f - a) * sx[r + 1][lane] + a * sx[r][lane] : -a * sx[r + 2][lane] + (1.f + a) * sx[r + 1][lane])
+                     : 0.f;
+        }
+        E[(long long)i * d.pitch + j] = edge_record<float2>(au, G[(long long)i * d.pitch + j], u >= 0.f);
+    }
+}
+
 template <class W>
 static int basis_setup_t(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, cudaStream_t st) {
     const Dims d = g.d;
@@ -868,6 +970,12 @@ static int basis_setup_t(const Options &o, const Grid &g, Winds &w, DeviceArena 
     }
     CSADV_CUDA(cudaMemsetAsync(w.u_pu, 0, F, st));
     CSADV_CUDA(cudaMemsetAsync(w.v_pv, 0, F, st));
+    if (sizeof(W) == 4) {  // the FP32 record kernel reads the y coefficients transposed
+        w.btabT = mem.alloc<W>((long long)M * d.field);
+        if (!mem.ok()) return CSADV_ERR_OOM;
+        k_transpose_coefs<W><<<ceil_div(d.field, 256), 256, 0, st>>>((const W *)w.btab[1], (W *)w.btabT, d, M);
+        CSADV_CUDA(cudaGetLastError());
+    }
     w.nbasis = M;
     return CSADV_OK;  // the clock's basis values are set by wind_initial (k_clock_set)
 }
@@ -883,6 +991,18 @@ int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const 
     dim3 grid(d.pitch / 32, ceil_div(d.n + 1, 32), NFACE);
     const real *bu = (const real *)w.btab[0], *bv = (const real *)w.btab[1];
     const Clock *clk = (const Clock *)w.clock;
+    if (sizeof(real) == 4 && w.btabT) {
+        dim3 g2(d.pitch / 32, ceil_div(d.n + 1, 32), 2 * NFACE);
+        const float ch = (float)(dt * 0.5 / g.dx);
+        if (w.nbasis == 4)
+            k_wind_rec<4><<<g2, 256, 0, st>>>(d, (const float *)bu, (const float *)w.btabT, clk, (const float *)gpu,
+                                              (const float *)gpvT, (float2 *)erx, (float2 *)ery, o.dp == 2, ch);
+        else
+            k_wind_rec<1><<<g2, 256, 0, st>>>(d, (const float *)bu, (const float *)w.btabT, clk, (const float *)gpu,
+                                              (const float *)gpvT, (float2 *)erx, (float2 *)ery, o.dp == 2, ch);
+        CSADV_CUDA(cudaGetLastError());
+        return CSADV_OK;
+    }
     if (w.nbasis == 4)
         k_wind_step<real, 4, V><<<grid, dim3(32, 8), 0, st>>>(d, bu, bv, clk, gpu, gpvT, erx, ery, o.dp == 2,
                                                                (real)(dt * 0.5), (real)g.dx);
