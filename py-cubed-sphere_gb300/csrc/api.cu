@@ -139,7 +139,11 @@ int do_update_winds(csadv_plan *pl, bool tick, long long k, double t, cudaStream
 
 int ensure_side(csadv_plan *pl) {
     if (!pl->side) {
-        CSADV_CUDA(cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking));
+        // lowest priority: with pipelined winds the step kernel's CTAs go first, the next step's
+        // wind records fill the SMs it leaves free
+        int least = 0, greatest = 0;
+        CSADV_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CSADV_CUDA(cudaStreamCreateWithPriority(&pl->side, cudaStreamNonBlocking, least));
         for (auto &e : pl->sev) CSADV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     return CSADV_OK;
@@ -153,6 +157,26 @@ int fused_step_work(csadv_plan *pl, int kind, cudaStream_t st) {
     int rc = ensure_side(pl);
     if (rc) return rc;
     cudaStream_t sd = pl->side;
+    if (pl->f.wpipe && pl->f.sweep) {
+        // Pipelined winds: the step kernel reads the records made during the previous step (or
+        // just before this one, run_step), while the side stream ticks the clock (kind 1) and
+        // makes the next step's records in the other buffer.
+        //   main: step kernel (records cur) ............................ | join
+        //   side: [clock tick] wind records for the next step (records 1-cur) |
+        CSADV_CUDA(cudaEventRecord(pl->sev[0], st));
+        CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[0], 0));
+        const int cur = pl->cur;
+        rc = fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, cur, st);  // none with inline ghost cells
+        if (!rc)
+            rc = fused_kernel(pl->opt, pl->grid, pl->dt, pl->T, pl->f, pl->cur, st, pl->prof ? pl->pev[0] : nullptr,
+                              pl->prof ? pl->pev[1] : nullptr);
+        if (!rc && kind == 1) rc = do_update_winds(pl, true, 0, 0.0, sd);
+        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, 1 - cur, sd);
+        if (rc) return rc;
+        CSADV_CUDA(cudaEventRecord(pl->sev[3], sd));
+        CSADV_CUDA(cudaStreamWaitEvent(st, pl->sev[3], 0));
+        return CSADV_OK;
+    }
     CSADV_CUDA(cudaEventRecord(pl->sev[0], st));
     CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[0], 0));
     rc = fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, pl->cur, sd);
@@ -160,7 +184,7 @@ int fused_step_work(csadv_plan *pl, int kind, cudaStream_t st) {
     const bool td = wind_time_dependent(pl->opt);
     if (td) {
         if (!pl->w.nbasis) rc = wind_halo(pl->opt, pl->grid, pl->w, st);  // the basis includes the halo
-        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
+        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, pl->cur, st);
         if (rc) return rc;
     }
     CSADV_CUDA(cudaEventRecord(pl->sev[1], sd));
@@ -223,6 +247,11 @@ int count_kernel_nodes(cudaGraph_t g) {
 
 // one step (kind 0: time step; kind 1: time step + wind update), replayed from a graph
 int run_step(csadv_plan *pl, int kind, cudaStream_t st) {
+    if (pl->f.on && pl->f.sweep && pl->f.wpipe && !pl->f.rec_ready) {  // this step's records first
+        int rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, pl->cur, st);
+        if (rc) return rc;
+        pl->f.rec_ready = true;
+    }
     const int par = pl->cur;
     const bool use_graph = pl->graphs && !pl->prof;  // profiled steps launch directly (events on the stream)
     if (use_graph && !pl->gexec[kind][par]) {
@@ -301,7 +330,7 @@ int plan_pre_step(csadv_plan *pl, cudaStream_t st, bool ghosts) {
     int rc = ghosts ? fused_ghosts(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st) : CSADV_OK;
     if (!rc && wind_time_dependent(pl->opt)) {
         if (!pl->w.nbasis) rc = wind_halo(pl->opt, pl->grid, pl->w, st);
-        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
+        if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, pl->cur, st);
     }
     return rc;
 }
@@ -405,6 +434,7 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     // departure-point winds, CFL
     rc = wind_setup(o, pl->grid, pl->w, pl->mem, dt, st);
     if (!rc && fused) rc = wind_basis_setup(o, pl->grid, pl->w, pl->mem, st);
+    if (!rc && fused) rc = fused_wind_pipeline(o, pl->grid, pl->w, pl->mem, pl->f, st);  // before the descriptors
     if (!rc) rc = wind_initial(o, pl->grid, pl->w, st);
     if (!rc) rc = wind_halo(o, pl->grid, pl->w, st);
     if (!rc) rc = copy_d2d(pl->w.u_old, pl->w.u_pu, (size_t)F * pl->w.esize, st);
@@ -423,7 +453,8 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
         rc = fused_set_tile(o, pl->grid, ntracers, dt, pl->f, o.tile > 0 ? o.tile - 1 : default_tile(o, N, ntracers), st);
     if (!rc) rc = wind_average(o, pl->grid, pl->w, dt, st);
     if (!rc) rc = wind_cfl(o, pl->grid, pl->w, dt, pl->tmp, pl->cfl, st);
-    if (!rc && fused) rc = fused_prep_winds(o, pl->grid, pl->w, dt, pl->f, st);
+    if (!rc && fused) rc = fused_prep_winds(o, pl->grid, pl->w, dt, pl->f, pl->cur, st);
+    pl->f.rec_ready = true;
     if (rc) {
         delete pl;
         return rc;
@@ -528,6 +559,7 @@ int csadv_time_step(csadv_plan *pl, int k, void *stream) {
 
 int csadv_update_winds(csadv_plan *pl, double t, void *stream) {
     if (!pl) return CSADV_ERR_ARG;
+    pl->f.rec_ready = false;  // pipelined winds: the next step's records follow the new clock
     return do_update_winds(pl, false, pl->k, t, S(stream));
 }
 

@@ -211,6 +211,7 @@ int batch_run_step(csadv_batch *b, int kind, cudaStream_t st) {
         pl->cur = 1 - pl->cur;
         pl->k += 1;
         pl->f.settled = false;
+        pl->f.rec_ready = false;  // a batch step makes no records for the plan's next step
         pl->stats.steps += 1;
     }
     b->phase ^= 1;
@@ -383,7 +384,7 @@ int csadv_tune(csadv_plan *pl, int reps, void *stream, int *tile_out) {
         for (int c = 0; c < SWEEP_NTILE_CFG && !rc; ++c) {
             const int tile = FUSED_NTILE_CFG + c;
             rc = fused_set_tile(pl->opt, pl->grid, pl->T, pl->dt, pl->f, tile, st);
-            if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
+            if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, pl->cur, st);
             // the kernel reads Qbuf[cur] and writes the other buffer: the state does not change
             for (int r = 0; r < reps + 1 && !rc; ++r) {
                 if (r == 1) {
@@ -410,8 +411,9 @@ int csadv_tune(csadv_plan *pl, int reps, void *stream, int *tile_out) {
         g_tune[key] = best;
     }
     int rc = fused_set_tile(pl->opt, pl->grid, pl->T, pl->dt, pl->f, best, st);
-    if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, st);
+    if (!rc) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, pl->cur, st);
     if (rc) return rc;
+    pl->f.rec_ready = true;
     pl->drop_graphs();
     batch_touch(pl);
     if (tile_out) *tile_out = best + 1;

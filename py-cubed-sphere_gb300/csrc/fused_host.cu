@@ -172,13 +172,27 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     return CSADV_OK;
 }
 
-int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, cudaStream_t st) {
+int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceArena &mem, FusedState &f,
+                        cudaStream_t st) {
+    if (o.precision != 32 || !w.nbasis) return CSADV_OK;
+    const size_t bytes = 2 * (size_t)g.d.field * sizeof(float);
+    f.erx1 = mem.alloc<char>(bytes);
+    f.ery1 = mem.alloc<char>(bytes);
+    if (!mem.ok()) return CSADV_ERR_OOM;
+    CSADV_CUDA(cudaMemsetAsync(f.erx1, 0, bytes, st));
+    CSADV_CUDA(cudaMemsetAsync(f.ery1, 0, bytes, st));
+    f.wpipe = true;
+    return CSADV_OK;
+}
+
+int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, int buf,
+                     cudaStream_t st) {
     if (f.sweep && w.nbasis) {
         if (o.precision == 64)
             return wind_step<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT, (double2 *)f.erx,
                                      (double2 *)f.ery, st);
-        return wind_step<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.erx,
-                                (float2 *)f.ery, st);
+        return wind_step<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.rec_x(buf),
+                                (float2 *)f.rec_y(buf), st);
     }
     if (w.nbasis) {  // per-edge tile kernel on a basis wind: current and previous winds first
         int rc = wind_sync(o, g, w, st);
@@ -232,8 +246,8 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.corr_out = pr ? f.corr[1 - b] : nullptr;
         s.partials = f.partials;
         s.counter = f.counter;
-        s.erx = f.erx;
-        s.ery = f.ery;
+        s.erx = f.rec_x(b);
+        s.ery = f.rec_y(b);
         s.crx = f.crx;
         s.cry = f.cry;
         s.gpc = f.g_pc;

@@ -138,6 +138,15 @@ struct FusedState {
     bool sweep = false;
     int scfg = 0;               // SWEEP_TILES index
     void *erx = nullptr, *ery = nullptr;  // edge records {wind, +-g} (x natural, y transposed)
+    // Pipelined winds (FP32 step kernel with a time-dependent wind): a second record buffer; the
+    // step that reads Qbuf[b] reads records b, and while it runs the records of the next step are
+    // computed into the other buffer on a second stream.  rec_ready: the records of the step that
+    // reads Qbuf[cur] are in place (host record; false after a clock change or a batch step).
+    void *erx1 = nullptr, *ery1 = nullptr;
+    bool wpipe = false;
+    bool rec_ready = false;
+    void *rec_x(int b) const { return wpipe && b == 1 ? erx1 : erx; }
+    void *rec_y(int b) const { return wpipe && b == 1 ? ery1 : ery; }
     void *crx = nullptr, *cry = nullptr;  // cell records {g, 1/g} (natural, transposed)
     const void *gpvT = nullptr;           // y-edge metric transposed
     SweepSolve *dsolve = nullptr;  // [2]
@@ -150,7 +159,12 @@ struct FusedState {
 
 int fused_supported(const Options &o);
 int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedState &f, cudaStream_t st);
-int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, cudaStream_t st);
+// departure-point winds of the step that reads Qbuf[buf] (edge records buffer buf when pipelined)
+int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, int buf,
+                     cudaStream_t st);
+// FP32 step kernel with a time-dependent (basis) wind: allocate the second record buffer
+int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceArena &mem, FusedState &f,
+                        cudaStream_t st);
 // ghost cells of every tracer of Qbuf[cur] (with the pending correction applied)
 int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
 // the fused kernel Qbuf[cur] -> Qbuf[1-cur]; cur flips

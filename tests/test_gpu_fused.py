@@ -229,3 +229,42 @@ def test_fp32_ghost_cells_equal_fp64_interpolation_rounded():
     assert ulp[ghost & ~side].max() <= 4  # corner blocks: weights up to ~2 on inputs one rounding apart
     assert ulp[side].max() <= 1
     assert np.count_nonzero(ulp[side]) <= max(2, ulp[side].size // 1000)
+
+
+def test_pipelined_wind_records_follow_every_call_pattern():
+    """FP32 with a time-dependent wind computes the next step's edge records while the step
+    runs.  Whatever the order of calls -- advance, the reference's time_step + update_winds
+    loop, steps taken in a batch, graphs on or off, profiled steps -- a plan gives the same bits
+    as one advanced straight through."""
+    from csadv import Batch, Plan
+    N, dt, nsteps = 40, 0.004, 9
+    kw = dict(recon=2, dp=2, opsplit=1, et=3, mt=1, mf=3, vf=2, ntracers=2, precision=32)
+
+    def make():
+        pl = Plan(N, dt, **kw)
+        pl.init_tracer(2, tracer=0)
+        pl.init_tracer(101, ic_param=(0.5, 0.2, 5.0, 0.0), tracer=1)
+        return pl
+
+    with make() as a:
+        a.advance(nsteps)
+        ref = [a.get_tracer(t) for t in range(2)]
+    with make() as b:
+        b.advance(2)
+        for k in (3, 4):  # adv_sphere's loop: time step k, then the wind at k dt
+            b.time_step(k)
+            b.update_winds(k * dt)
+        with Batch(4) as bt:
+            bt.add(b)
+            bt.advance(2)
+            bt.remove(b)
+        b.set_graphs(False)
+        b.advance(1)
+        b.set_graphs(True)
+        b.set_profiling(True)
+        b.advance(1)
+        b.set_profiling(False)
+        b.advance(1)
+        assert b.step == nsteps
+        for t in range(2):
+            np.testing.assert_array_equal(b.get_tracer(t), ref[t])
