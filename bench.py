@@ -57,15 +57,17 @@ def dt_for_cfl(make_plan):
     return 1e-3 * CFL / c
 
 
-def profiled_traffic(key):
-    """DRAM bytes (read + write) of one launch of the step kernel on this workload, from the
-    committed ncu summary (a `key = value` line); None when absent."""
-    path = os.path.join(ROOT, "profiles", "k_sweep_N384_T2.md")
+PROFILE = os.path.join(ROOT, "profiles", "k_sweep2_N384_T2.md")
+
+
+def profiled(key):
+    """A figure of one launch of the step kernel on this workload from the committed ncu summary
+    (its `key = value` line, commas allowed); None when absent."""
     try:
-        for ln in open(path):
+        for ln in open(PROFILE):
             if ln.strip().startswith(key + " ="):
-                return int(ln.split("=")[1])
-    except OSError:
+                return float(ln.split("=")[1].split()[0].replace(",", ""))
+    except (OSError, ValueError):
         pass
     return None
 
@@ -419,11 +421,25 @@ def bench_gpu(args):
     alg = 6 * N_CELLS * N_CELLS * (NTRACERS * 2 * s_q + 3 * 4)
     kms = f32["kernel_ms"]
     achieved = alg / (kms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_sweep<float, PPM-CW84, AVLT>", "achieved": round(achieved, 1),
-            "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+    roof = {"bound": "hbm", "kernel": "k_sweep2<PPM-CW84, AVLT> (paired-tracer FP32 step kernel)",
+            "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
             "traffic": None, "kernel_ms": round(kms, 5), "alg_bytes_per_launch": alg,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
-    roof["traffic"] = profiled_traffic("dram_bytes_per_launch")
+    tr = profiled("dram_bytes_per_launch")
+    roof["traffic"] = int(tr) if tr else None
+    # The kernel is bound by instruction issue (DRAM a few percent busy): its warp instructions per
+    # launch (ncu, committed summary) over the launch time, against 4 per SM per cycle at the
+    # clock sampled during the timed steps.
+    inst = profiled("smsp__inst_executed.sum")
+    clk_s = clk.summary()
+    mhz = clk_s.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    if inst:
+        peak_issue = 152 * 4 * mhz * 1e6
+        issue = {"bound": "issue", "achieved": round(inst / (kms * 1e-3) / 1e12, 4), "peak": round(peak_issue / 1e12, 4),
+                 "unit": "T warp-inst/s", "frac": round(inst / (kms * 1e-3) / peak_issue, 4),
+                 "inst_per_launch": int(inst), "source": "profiles/k_sweep2_N384_T2.md"}
+    else:
+        issue = None
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "tracer cell-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
@@ -437,7 +453,8 @@ def bench_gpu(args):
         "gpu_launches": int(f32["stats"]["kernel_launches"]),
         "kernels_per_step": int(f32["stats"]["kernels_per_step"]),
         "roofline": roof,
-        "clocks": clk.summary(),
+        "issue_roofline": issue,
+        "clocks": clk_s,
         "errors_fp32_linf_l1_l2_vs_exact": [float("%.4e" % e) for e in f32["errors_linf_l1_l2"]],
     }
     if not args.no_batched:
