@@ -136,6 +136,21 @@ int csadv_get_step(const csadv_plan *plan, int *k);
  * current state, written as an interior (N, N, 6) array; the state is not advanced. */
 int csadv_divergence(csadv_plan *plan, int tracer, double *host_div, void *stream);
 
+/* ---------------------------------------------------------------- lat-lon output (headless plots) */
+/* ll2cs (interpolation.py:38-140), equiangular grid of N cells per panel edge: for n points
+ * (X, Y, Z) on the unit sphere (a lat-lon grid's sph2cart coordinates, sphgeo.py:18-22), the
+ * panel (Lauritzen et al. 2015: the largest |coordinate|, later panels winning ties as the
+ * reference's masks do) and the interior cell indices (i, j) in [0, N) of the cell holding each
+ * point (inverse gnomonic map, cs_transform.py:101-126, binned as floor((x + pi/4) / dx)).
+ * Host arrays; page-locked ones are used in place.  Returns when the outputs are written. */
+int csadv_ll2cs(int N, const double *X, const double *Y, const double *Z, long long n, uint32_t *i, uint32_t *j,
+                uint32_t *panel, void *stream);
+/* nearest_neighbour (interpolation.py:145-150): out[t] = Q[i0 + i[t], j0 + j[t], panel[t]] of one tracer
+ * of the plan (its current state, float64).  CSADV_ERR_ARG if an index is out of range (those
+ * outputs are NaN).  Returns when out is written. */
+int csadv_nearest_neighbour(csadv_plan *plan, int tracer, const uint32_t *i, const uint32_t *j,
+                            const uint32_t *panel, long long n, double *out, void *stream);
+
 /* ---------------------------------------------------------------- execution control and statistics */
 /* Steps run as CUDA graphs by default: one graph per step kind and buffer parity is
  * captured on first use and replayed on the caller's stream.  enable = 0 launches the

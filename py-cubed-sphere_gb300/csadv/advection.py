@@ -10,6 +10,7 @@ Same names, arguments and error behaviour as the reference:
 * ``adv_sphere(cs_grid, ll_grid, simulation, map_projection, plot, divtest_flag)`` -- advection_sphere.py:13
 * ``mass_computation(Q, cs_grid, total_mass0)``                -- diagnostics.py:14
 * ``compute_errors(Q, Qref)``                                  -- errors.py:99
+* ``latlon_grid``, ``ll2cs``, ``nearest_neighbour`` (re-exported from ``csadv.latlon``)
 
 The grid geometry, winds and tracer live on the GPU; ``simulation.Q`` reads return a
 float64 copy in the reference layout (N+8, N+8, 6) and assignments upload one.  Plots
@@ -18,7 +19,11 @@ float64 copy in the reference layout (N+8, N+8, 6) and assignments upload one.  
 import numpy as np
 
 from . import _lib as L
+from .latlon import latlon_grid, ll2cs, nearest_neighbour  # noqa: F401
 from .plan import Plan
+
+# where adv_sphere(plot=True) writes the lat-lon fields (the reference's graph directory)
+output_dir = "graphs"
 
 _RECON = {1: "PPM-0", 2: "PPM-CW84", 3: "PPM-PL07", 4: "PPM-L04"}
 _DP = {1: "RK1", 2: "RK2"}
@@ -203,6 +208,14 @@ def output_adv(cs_grid, ll_grid, simulation, plot, k, t, Nsteps, plotstep, map_p
     s.total_mass, s.mass_change = mass_computation(s, cs_grid, s.total_mass0)
     if k > 0 and not divtest_flag:
         print_diagnostics_adv(linf, l1, l2, s.mass_change, k, Nsteps)
+    # the reference's lat-lon plots (output.py:56-110), headless: Q on the lat-lon grid as .npy
+    if plot and ll_grid is not None and not divtest_flag and (k % max(plotstep, 1) == 0 or k == 0 or k == Nsteps):
+        import os
+        from .latlon import save_latlon
+        os.makedirs(output_dir, exist_ok=True)
+        name = "adv_Q_ic%d_vf%d_%s_%s_%s_%s_%s_interp%d_t%d" % (s.ic, s.vf, s.opsplit_name, s.recon_name, s.dp_name,
+                                                                s.et_name, s.mt_name, s.degree, k)
+        save_latlon(os.path.join(output_dir, name + ".npy"), s, cs_grid, ll_grid)
 
 
 def adv_sphere(cs_grid, ll_grid, simulation, map_projection, plot, divtest_flag):

@@ -40,6 +40,7 @@ UNITS = {
     "sweep_f32.cu": True,
     "sweep_f64.cu": True,
     "noalloc.cu": False,
+    "latlon.cu": False,
 }
 
 

@@ -341,6 +341,8 @@ int plan_post_step(csadv_plan *pl, int kind, cudaStream_t st) {
 
 int plan_select_device(csadv_plan *pl) { return select_device(pl); }
 
+int plan_settle(csadv_plan *pl, cudaStream_t st) { return settle(pl, st); }
+
 int graph_kernel_nodes(cudaGraph_t g) { return count_kernel_nodes(g); }
 
 }  // namespace csadv

@@ -85,6 +85,8 @@ namespace csadv {
 int plan_pre_step(csadv_plan *pl, cudaStream_t st, bool ghosts = true);
 int plan_post_step(csadv_plan *pl, int kind, cudaStream_t st);
 int plan_select_device(csadv_plan *pl);
+// apply a pending MF-PR correction: the stored state becomes the true state
+int plan_settle(csadv_plan *pl, cudaStream_t st);
 int graph_kernel_nodes(cudaGraph_t g);
 // batch.cu: tile chosen by csadv_tune for plans of this shape (-1: none); detach a plan from
 // its batch; mark the plan's batch for a rebuild (its descriptors changed)

@@ -21,6 +21,9 @@ uninstalled numexpr / netCDF4 / matplotlib, see that file) and records:
                          mass; and 30 steps of PPM-CW84/RK2/vf=2.
 * ``cases_N12.npz``   -- qexact_adv for ic 1-4 x vf 1-4 and velocity_adv for vf 1-4.
 * ``par.npz``         -- the reference's parse of its own par/*.par files.
+* ``latlon.npz``      -- ll2cs (panel and cell indices of lat-lon points) and
+                         nearest_neighbour for three (N, Nlat, Nlon), with the lat-lon
+                         points' X, Y, Z (``--only latlon`` writes just this file).
 """
 import argparse
 import itertools
@@ -53,11 +56,15 @@ def invalid_combos():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=None)
+    ap.add_argument("--only", default=None, choices=("latlon",))
     args = ap.parse_args()
     if args.ref:
         os.environ["CSADV_REFERENCE_SRC"] = args.ref
     sys.path.insert(0, HERE)
     import refharness as rh
+    if args.only == "latlon":
+        latlon_fixtures(rh.modules())
+        return
 
     m = rh.modules()
     interior = lambda g: (slice(g.i0, g.iend), slice(g.j0, g.jend), slice(None))  # noqa: E731
@@ -194,7 +201,27 @@ def main():
     np.savez_compressed(os.path.join(HERE, "par.npz"),
                         configuration=np.array([str(x) for x in conf]),
                         advection=np.array([repr(x) for x in adv]))
+    latlon_fixtures(m)
     print("golden fixtures written to", HERE)
+
+
+def latlon_fixtures(m):
+    """ll2cs and nearest_neighbour of the reference (interpolation.py:38-150)."""
+    out = {}
+    # (lat-lon sizes for which no point lies on a panel edge: the reference indexes past the
+    # panel there, interpolation.py:148)
+    for N, nlat, nlon in ((16, 46, 91), (48, 90, 180), (25, 31, 63)):
+        grid = m.cs_datastruct.cubed_sphere(N, "gnomonic_equiangular", False, False)
+        ll = m.cs_datastruct.latlon_grid(nlat, nlon)
+        i, j, p = m.interpolation.ll2cs(grid, ll)
+        ll.ix, ll.jy, ll.mask = i, j, p
+        f = np.arange(N * N * 6, dtype=np.float64).reshape(N, N, 6) * 0.5 - 7.0
+        q = m.interpolation.nearest_neighbour(type("F", (), {"f": f})(), grid, ll)
+        key = "N%d_%dx%d" % (N, nlat, nlon)
+        out[key + "_X"], out[key + "_Y"], out[key + "_Z"] = ll.X, ll.Y, ll.Z
+        out[key + "_i"], out[key + "_j"], out[key + "_panel"] = i, j, p
+        out[key + "_nn"] = q
+    np.savez_compressed(os.path.join(HERE, "latlon.npz"), **out)
 
 
 if __name__ == "__main__":

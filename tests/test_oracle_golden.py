@@ -158,3 +158,19 @@ def test_long_run_errors_and_mass(golden_dir, name):
         np.testing.assert_allclose(m, z[name + "_mass"][k - 1][0], rtol=1e-12)
         solver.update_adv(s, t)
     assert_close(s.Q[it], z[name + "_Q"])
+
+
+def test_latlon_oracle_matches_reference(golden_dir):
+    """ll2cs / nearest_neighbour restated (oracle/latlon.py) against the reference's own output."""
+    from oracle import latlon
+    z = np.load(os.path.join(golden_dir, "latlon.npz"))
+    keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
+    assert len(keys) == 3
+    for key in keys:
+        N = int(key.split("_")[0][1:])
+        i, j, p = latlon.ll2cs(N, z[key + "_X"], z[key + "_Y"], z[key + "_Z"])
+        np.testing.assert_array_equal(i, z[key + "_i"])
+        np.testing.assert_array_equal(j, z[key + "_j"])
+        np.testing.assert_array_equal(p, z[key + "_panel"])
+        f = np.arange(N * N * 6, dtype=np.float64).reshape(N, N, 6) * 0.5 - 7.0
+        np.testing.assert_array_equal(latlon.nearest_neighbour(f, i, j, p), z[key + "_nn"])
