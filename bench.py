@@ -129,8 +129,37 @@ class ClockSampler:
         return {"sm_mhz": sms[len(sms) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
 
 
+# ----------------------------------------------------------------------------- replicas (N > 1)
+def replica_barrier(world, device=None):
+    """Barrier across the replicas (N > 1) and a device synchronisation: brackets every timed
+    region, so every rank starts and ends its timed steps together."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    if device == "cuda":
+        import torch
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(values, world, device="cuda"):
+    """Each value maximised over the ranks (the job ends with its slowest replica); unchanged
+    on one rank.  device: where the collective's tensor lives ("cuda" for NCCL, "cpu" for gloo)."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_rate(units_per_step, world, ms_per_step):
+    """Whole-job rate: the units all ranks processed per step over the slowest rank's step time."""
+    return world * units_per_step / (ms_per_step * 1e-3)
+
+
 # ----------------------------------------------------------------------------- GPU arm
-def run_form(torch, precision, steps, warmup, flush, stream):
+def run_form(torch, precision, steps, warmup, flush, stream, world=1):
     """Throughput loop (graphs, no host syncs), then a kernel-timing loop (events around the
     main kernel, recorded inside the graph) over the same number of steps."""
     from csadv import Plan
@@ -144,15 +173,15 @@ def run_form(torch, precision, steps, warmup, flush, stream):
     for t, ic in enumerate(ICS):
         pl.init_tracer(ic, tracer=t)
     pl.advance(warmup)
-    torch.cuda.synchronize()
     pl.reset_stats()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    replica_barrier(world, "cuda")
     for k in range(steps):
         flush.fill_(k)
         ev[k][0].record(stream)
         pl.advance(1)
         ev[k][1].record(stream)
-    torch.cuda.synchronize()
+    replica_barrier(world, "cuda")
     ms = [a.elapsed_time(b) for a, b in ev]
     st = pl.stats()
     pl.set_profiling(True)
@@ -171,7 +200,7 @@ def run_form(torch, precision, steps, warmup, flush, stream):
     return res
 
 
-def run_e2e(torch, precision, steps, stream):
+def run_e2e(torch, precision, steps, stream, world=1):
     """Through the C ABI with host buffers: per step, upload both tracers from pinned host
     memory (reference layout, full arrays), advance, download both tracers."""
     import ctypes
@@ -208,11 +237,11 @@ def run_e2e(torch, precision, steps, stream):
 
     for _ in range(3):
         one_step()
-    torch.cuda.synchronize()
+    replica_barrier(world, "cuda")
     t0 = time.perf_counter()
     for _ in range(steps):
         one_step()
-    torch.cuda.synchronize()
+    replica_barrier(world, "cuda")
     sec = (time.perf_counter() - t0) / steps
     for pin, pout in bufs:
         L.csadv_host_free(pin)
@@ -395,19 +424,13 @@ def bench_gpu(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2 (129 MB)
 
     with ClockSampler(local) as clk:
-        f32 = run_form(torch, 32, args.steps, args.warmup, flush, stream)
-    f64 = run_form(torch, 64, max(3, args.steps // 5), args.warmup, flush, stream)
-    e2e_sec, h2d, d2h = run_e2e(torch, 32, max(3, args.steps // 2), stream)
+        f32 = run_form(torch, 32, args.steps, args.warmup, flush, stream, world)
+    f64 = run_form(torch, 64, max(3, args.steps // 5), args.warmup, flush, stream, world)
+    e2e_sec, h2d, d2h = run_e2e(torch, 32, max(3, args.steps // 2), stream, world)
 
-    ms = f32["ms_per_step"]
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms, e2e_sec], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_sec = float(t[0]), float(t[1])
-        dist.barrier()
+    ms, ms64, e2e_sec = max_over_ranks([f32["ms_per_step"], f64["ms_per_step"], e2e_sec], world)
     cells = NTRACERS * 6 * N_CELLS * N_CELLS
-    value = world * cells / (ms * 1e-3)
+    value = job_rate(cells, world, ms)
     if rank != 0:
         return
     peaks = {}
@@ -445,10 +468,10 @@ def bench_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (analytic ICs and winds)",
         "config": dict(workload_config(), parallelism="replicas" if world > 1 else "single GPU"),
-        "fp64": {"value": round(world * cells / (f64["ms_per_step"] * 1e-3), 1), "ms_per_step": round(f64["ms_per_step"], 5),
+        "fp64": {"value": round(job_rate(cells, world, ms64), 1), "ms_per_step": round(ms64, 5),
                  "kernel_ms": round(f64["kernel_ms"], 5), "dtype": "f64"},
-        "fp32_over_fp64": round(f64["ms_per_step"] / ms, 2),
-        "e2e": {"value": round(world * cells / e2e_sec, 1), "unit": "tracer cell-steps/s",
+        "fp32_over_fp64": round(ms64 / ms, 2),
+        "e2e": {"value": round(job_rate(cells, world, e2e_sec * 1e3), 1), "unit": "tracer cell-steps/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(f32["stats"]["kernel_launches"]),
         "kernels_per_step": int(f32["stats"]["kernels_per_step"]),

@@ -70,3 +70,43 @@ def test_compute_errors_host():
     assert linf == 5.0
     assert l1 == pytest.approx((95 * 2 + 5) / 96)
     assert l2 == pytest.approx(np.sqrt((95 * 4 + 25) / 96))
+
+
+def _replica_rank(rank, world, port, out_dir):
+    import json
+    import os
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    try:
+        bench.replica_barrier(world)
+        # rank r took (1 + r) ms per step and (5 - r) s end to end: the job takes the slowest
+        ms, e2e = bench.max_over_ranks([1.0 + rank, 5.0 - rank], world, device="cpu")
+        rate = bench.job_rate(100, world, ms)
+        bench.replica_barrier(world)
+    finally:
+        dist.destroy_process_group()
+    with open(os.path.join(out_dir, "rank%d.json" % rank), "w") as f:
+        json.dump({"ms": ms, "e2e": e2e, "rate": rate}, f)
+
+
+def test_bench_replicas_take_the_slowest_rank(tmp_path):
+    """bench.py --gpus N runs N independent replicas (the solve does not shard): every timed
+    region is bracketed by a barrier, times are maximised over the ranks, and the whole-job
+    rate counts the units of all ranks.  Checked with two gloo ranks on the CPU."""
+    import json
+    import socket
+
+    import torch.multiprocessing as mp
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    mp.start_processes(_replica_rank, args=(2, port, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
+    for r in range(2):
+        got = json.load(open(tmp_path / ("rank%d.json" % r)))
+        assert got["ms"] == 2.0 and got["e2e"] == 5.0
+        assert abs(got["rate"] - 2 * 100 / 2e-3) < 1e-6
