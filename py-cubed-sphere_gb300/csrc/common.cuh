@@ -105,9 +105,9 @@ struct Grid {
     // Lagrange ghost-cell weights [depth][k][m] and stencil starts [depth][k] (lagrange.py:28-163)
     const double *lag_w;
     const int *lag_k;
-    // the same weights split into two FP32 words, hi = (float)w, lo = (float)(w - hi) (the FP32
-    // form's ghost cells, evaluated in double-float arithmetic: halo.cuh)
-    const float2 *lag_wf;
+    // the FP32 form's ghost-cell stencils, flattened per ghost cell (halo.cuh, built by grid.cu):
+    // side-strip rows [panel][side][depth][k] of 4 terms, corner-block rows of 16
+    const struct GhostTerm *gside, *gcorner;
     double a2;  // sum over the interior of g_pc^2, all panels (MF-PR denominator)
 };
 

@@ -259,8 +259,8 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.lag_k = f.inline_ghosts ? g.lag_k : nullptr;
         s.hlag_w = g.lag_w;
         s.hlag_k = g.lag_k;
-        s.lag_wf = f.inline_ghosts ? g.lag_wf : nullptr;
-        s.hlag_wf = g.lag_wf;
+        s.gside = g.gside;
+        s.gcorner = g.gcorner;
     }
     f.nitems = NFACE * h[0].ntiles;
     f.smem = o.precision == 64 ? sweep_smem_bytes<double>(f.scfg) : sweep_smem_bytes<float>(f.scfg);

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "halo.cuh"
 #include "internal.h"
 
 namespace csadv {
@@ -199,6 +200,81 @@ int lagrange_tables(int N, const std::vector<double> &xc, double dx, std::vector
 }
 
 // Build every FP64 geometry array of resolution N into `mem` (device) and fill `grid`.
+// ---------------------------------------------------------------- FP32 ghost-cell stencil tables
+__device__ GhostTerm ghost_term(const Dims &d, int q, int i, int j, double w) {
+    GhostTerm t;
+    t.o = (int)at(d, q, i, j);
+    t.o2 = (int)at2(d, i, j);
+    const float hi = (float)w;
+    t.w = make_float2(hi, (float)(w - (double)hi));
+    return t;
+}
+
+// the 4 terms of the side-strip ghost cell at depth dep outside side s of panel p, along-edge
+// index k, every weight times `scale` (the index rules of side_ghost, halo.cuh)
+__device__ void side_terms(const Dims &d, const double *__restrict__ W, const int *__restrict__ K, int p, int s,
+                           int dep, int k, double scale, GhostTerm *out) {
+    const Conn c = c_conn[p][s];
+    const int n = d.n;
+    const int k0 = K[dep * n + k];
+    const double *w = W + ((long long)dep * n + k) * 4;
+    for (int m = 0; m < 4; ++m) {
+        const int kk = k0 + m, along = c.rev ? n - 1 - kk : kk;
+        int i, j;
+        inside_ij(d, c.qs, dep, along, i, j);
+        out[m] = ghost_term(d, c.q, i, j, scale * w[m]);
+    }
+}
+
+// One thread per table row: side rows [p][s][dep][k - i0] (4 terms), then corner rows
+// [p][corner][di][dj] (16 terms: for each of the 4 outer points of the E/W interpolation
+// (ghost_value, halo.cuh), the neighbour's cell itself or its side-strip stencil, weights
+// multiplied in FP64; unused slots have weight 0)
+__global__ void k_ghost_tables(Dims d, const double *__restrict__ W, const int *__restrict__ K, GhostTerm *side,
+                               GhostTerm *corner) {
+    const int N = d.N, n = d.n;
+    const long long nside = (long long)NFACE * 4 * NG * N;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < nside) {
+        const int kk = (int)(t % N), dep = (int)((t / N) % NG), s = (int)((t / ((long long)N * NG)) % 4);
+        const int p = (int)(t / ((long long)N * NG * 4));
+        side_terms(d, W, K, p, s, dep, d.i0 + kk, 1.0, side + 4 * t);
+        return;
+    }
+    const long long r = t - nside;
+    if (r >= (long long)NFACE * 4 * NG * NG) return;
+    const int dj = (int)(r % NG), di = (int)((r / NG) % NG), cc = (int)((r / (NG * NG)) % 4);
+    const int p = (int)(r / (NG * NG * 4));
+    const int gj = (cc & 1) ? d.iend + dj : d.i0 - 1 - dj;
+    const int s = (cc & 2) ? SIDE_E : SIDE_W, dep = di;
+    const Conn c = c_conn[p][s];
+    const int k0 = K[dep * n + gj];
+    const double *w = W + ((long long)dep * n + gj) * 4;
+    GhostTerm *out = corner + GHOST_CORNER_TERMS * r;
+    for (int m = 0; m < 4; ++m) {
+        const int kk = k0 + m, along = c.rev ? n - 1 - kk : kk;
+        int qi, qj;
+        inside_ij(d, c.qs, dep, along, qi, qj);
+        // the cell (qi, qj) of panel c.q: interior, or in a side strip (cell_or_side_ghost, halo.cuh)
+        int s2 = -1, dep2 = 0, k2 = 0;
+        if (qi >= d.iend) {
+            s2 = SIDE_E; dep2 = qi - d.iend; k2 = qj;
+        } else if (qi < d.i0) {
+            s2 = SIDE_W; dep2 = d.i0 - 1 - qi; k2 = qj;
+        } else if (qj >= d.iend) {
+            s2 = SIDE_N; dep2 = qj - d.iend; k2 = qi;
+        } else if (qj < d.i0) {
+            s2 = SIDE_S; dep2 = d.i0 - 1 - qj; k2 = qi;
+        }
+        if (s2 < 0) {
+            out[4 * m] = ghost_term(d, c.q, qi, qj, w[m]);
+            for (int e = 1; e < 4; ++e) out[4 * m + e] = ghost_term(d, c.q, qi, qj, 0.0);
+        } else {
+            side_terms(d, W, K, c.q, s2, dep2, k2, w[m], out + 4 * m);
+        }
+    }
+}
+
 int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     Dims d = make_dims(N);
     grid.d = d;
@@ -222,19 +298,16 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     if (rc != CSADV_OK) return rc;
     double *lag_w = mem.alloc<double>(lw.size());
     int *lag_k = mem.alloc<int>(lk.size());
-    float2 *lag_wf = mem.alloc<float2>(lw.size());
-    std::vector<float2> lwf(lw.size());
-    for (size_t e = 0; e < lw.size(); ++e) {
-        const float hi = (float)lw[e];
-        lwf[e] = make_float2(hi, (float)(lw[e] - (double)hi));
-    }
+    const long long nside = (long long)NFACE * 4 * NG * N, ncorner = (long long)NFACE * 4 * NG * NG;
+    GhostTerm *gside = mem.alloc<GhostTerm>(4 * nside);
+    GhostTerm *gcorner = mem.alloc<GhostTerm>(GHOST_CORNER_TERMS * ncorner);
     if (!mem.ok()) return CSADV_ERR_OOM;
     for (double *g : {g_pc, g_pu, g_pv}) CSADV_CUDA(cudaMemsetAsync(g, 0, P1 * sizeof(double), st));
     CSADV_CUDA(cudaMemcpyAsync(xs_dev, xc.data(), xc.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(xs_dev + xc.size(), xe.data(), xe.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(lag_w, lw.data(), lw.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(lag_k, lk.data(), lk.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    CSADV_CUDA(cudaMemcpyAsync(lag_wf, lwf.data(), lwf.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+    k_ghost_tables<<<ceil_div(nside + ncorner, 128), 128, 0, st>>>(d, lag_w, lag_k, gside, gcorner);
     const double *xcd = xs_dev, *xed = xs_dev + xc.size();
     const int n = d.n;
     PointOut o;
@@ -263,7 +336,8 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     for (int c = 0; c < 4; ++c) grid.cc[c] = cc[c];
     grid.lag_w = lag_w;
     grid.lag_k = lag_k;
-    grid.lag_wf = lag_wf;
+    grid.gside = gside;
+    grid.gcorner = gcorner;
     grid.a2 = a2h;
     return CSADV_OK;
 }

@@ -25,7 +25,8 @@ namespace csadv {
 // blockIdx.y = tracer (fields `fstride` elements apart); corr[tracer] optional
 template <class real>
 __global__ void k_halo_dg(real *F0, long long fstride, Dims d, const double *__restrict__ W,
-                          const float2 *__restrict__ Wf, const int *__restrict__ K, const double *__restrict__ corr,
+                          const int *__restrict__ K, const GhostTerm *__restrict__ gside,
+                          const GhostTerm *__restrict__ gcorner, const double *__restrict__ corr,
                           const real *__restrict__ g) {
     const int n = d.n;
     int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -38,12 +39,8 @@ __global__ void k_halo_dg(real *F0, long long fstride, Dims d, const double *__r
     int p = tid / (n * NG * 4);
     int gi, gj;
     ghost_ij(d, s, dep, k, gi, gj);
-    if (is_interior(d, k)) {
-        F[at(d, p, gi, gj)] = side_cell(S, d, W, Wf, K, p, s, dep, k);
-        return;
-    }
-    if (s == SIDE_N || s == SIDE_S) return;  // corner blocks are filled from the E/W sides
-    F[at(d, p, gi, gj)] = ghost_cell(S, d, W, Wf, K, p, gi, gj);
+    if (!is_interior(d, k) && (s == SIDE_N || s == SIDE_S)) return;  // corner blocks: from the E/W sides
+    F[at(d, p, gi, gj)] = ghost_cell(S, d, W, K, gside, gcorner, p, gi, gj);
 }
 
 // ghost cells of many solves in one launch: item (s, b) of the work table is block b % nb of
@@ -65,10 +62,8 @@ __global__ void k_halo_batch(const SweepSolve *__restrict__ solves, const int2 *
         const int k = tid % n, dep = (tid / n) % NG, s = (tid / (n * NG)) % 4, p = tid / (n * NG * 4);
         int gi, gj;
         ghost_ij(d, s, dep, k, gi, gj);
-        if (is_interior(d, k)) {
-            F[at(d, p, gi, gj)] = side_cell(src, d, S.hlag_w, S.hlag_wf, S.hlag_k, p, s, dep, k);
-        } else if (s == SIDE_E || s == SIDE_W) {  // corner blocks, from the E/W sides
-            F[at(d, p, gi, gj)] = ghost_cell(src, d, S.hlag_w, S.hlag_wf, S.hlag_k, p, gi, gj);
+        if (is_interior(d, k) || s == SIDE_E || s == SIDE_W) {  // corner blocks, from the E/W sides
+            F[at(d, p, gi, gj)] = ghost_cell(src, d, S.hlag_w, S.hlag_k, S.gside, S.gcorner, p, gi, gj);
         }
     }
 }
@@ -105,7 +100,8 @@ __global__ void k_halo_adjacent(real *Qx, real *Qy, Dims d) {
 template <class real>
 int launch_halo_dg(real *F, const Grid &g, cudaStream_t st) {
     int tot = NFACE * 4 * NG * g.d.n;
-    k_halo_dg<real><<<ceil_div(tot, 128), 128, 0, st>>>(F, 0, g.d, g.lag_w, g.lag_wf, g.lag_k, nullptr, nullptr);
+    k_halo_dg<real><<<ceil_div(tot, 128), 128, 0, st>>>(F, 0, g.d, g.lag_w, g.lag_k, g.gside, g.gcorner, nullptr,
+                                                        nullptr);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -114,7 +110,7 @@ template <class real>
 int launch_halo_dg_tracers(real *F, int T, const Grid &g, const double *corr, const real *greal, cudaStream_t st) {
     int tot = NFACE * 4 * NG * g.d.n;
     dim3 grid(ceil_div(tot, 128), T);
-    k_halo_dg<real><<<grid, 128, 0, st>>>(F, g.d.field, g.d, g.lag_w, g.lag_wf, g.lag_k, corr, greal);
+    k_halo_dg<real><<<grid, 128, 0, st>>>(F, g.d.field, g.d, g.lag_w, g.lag_k, g.gside, g.gcorner, corr, greal);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }

@@ -112,15 +112,24 @@ __device__ __forceinline__ double ghost_value(const Src<real> &S, const Dims &d,
     return side_ghost(S, d, W, K, p, s, dep, i);
 }
 
-// ---------------------------------------------------------------- FP32 form: double-float sums
+// ---------------------------------------------------------------- FP32 form: stencil tables
 // The FP32 form keeps the Lagrange weights at FP64 accuracy but evaluates the interpolation on
 // the FP32 pipe: GB300 runs FP64 at 1/64 of the FP32 rate, with long latency, and the ghost cells
-// are on the critical path of every step.  A weight is carried as hi + lo (two FP32 words, about
-// 48 significant bits), each product q w as an unevaluated sum p + e (the FMA gives the rounding
-// error of q hi exactly, Dekker's product), and the four products are summed with Knuth's
-// two-sum; the result is rounded once to FP32.  It equals the FP64 evaluation rounded to FP32
-// except when that value lies within ~2^-47 of a rounding boundary.  The order of the terms
-// and the two-level corner rule are those of the FP64 functions above.
+// are on the critical path of every step.  Each ghost cell's interpolation is flattened, once per
+// grid, into a list of terms {source cell, weight}: 4 for a side-strip cell, 16 for a corner-block
+// cell (the outer weights times the inner stencils of the neighbour's side strip, formed in FP64,
+// instead of the reference's two levels).  A weight is stored as hi + lo (two FP32 words, about
+// 48 significant bits); each product q w is carried as an unevaluated sum (the FMA gives the
+// rounding error of q hi exactly: Dekker's product) and the terms are summed with Knuth's
+// two-sum, then rounded once to FP32.  Every evaluation is one level of table loads and one of
+// source loads, without branches on the panel connectivity.
+struct __align__(16) GhostTerm {
+    int o;      // source cell: offset in one tracer's field (panel plane, row, column)
+    int o2;     // the same cell in the single metric plane
+    float2 w;   // weight: hi + lo
+};
+constexpr int GHOST_CORNER_TERMS = 16;
+
 struct DFloat {
     float hi, lo;
 };
@@ -138,109 +147,62 @@ __device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
 }
 __device__ __forceinline__ float df_round(DFloat a) { return __fadd_rn(a.hi, a.lo); }
 
-// side_ghost for the FP32 form (weights as hi + lo pairs)
-__device__ __forceinline__ float side_ghost_f(const Src<float> &S, const Dims &d, const float2 *__restrict__ W,
-                                              const int *__restrict__ K, int p, int s, int dep, int k) {
-    const Conn c = c_conn[p][s];
-    const int n = d.n;
-    const int k0 = K[dep * n + k];
-    const float2 *w = W + ((long long)dep * n + k) * 4;
-    DFloat prod[4];
+// sum of NT terms: all table loads, then all source loads, then the arithmetic
+template <int NT>
+__device__ __forceinline__ float ghost_terms_f(const Src<float> &S, const GhostTerm *__restrict__ t) {
+    GhostTerm x[NT];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        int kk = k0 + m;
-        int along = c.rev ? n - 1 - kk : kk;
-        int i, j;
-        inside_ij(d, c.qs, dep, along, i, j);
-        prod[m] = df_prod(S.value(d, c.q, i, j), w[m]);
-    }
-    return df_round(df_add(df_add(df_add(prod[0], prod[1]), prod[2]), prod[3]));
+    for (int m = 0; m < NT; ++m) x[m] = t[m];
+    float v[NT];
+#pragma unroll
+    for (int m = 0; m < NT; ++m) v[m] = S.has_corr ? corrected(S.F[x[m].o], S.g[x[m].o2], S.corr) : S.F[x[m].o];
+    DFloat acc = df_prod(v[0], x[0].w);
+#pragma unroll
+    for (int m = 1; m < NT; ++m) acc = df_add(acc, df_prod(v[m], x[m].w));
+    return df_round(acc);
 }
 
-__device__ __forceinline__ float cell_or_side_ghost_f(const Src<float> &S, const Dims &d, const float2 *__restrict__ W,
-                                                      const int *__restrict__ K, int q, int i, int j) {
-    int s = -1, dep = 0, k = 0;
-    if (i >= d.iend) {
-        s = SIDE_E;
-        dep = i - d.iend;
+// the ghost cell (i, j) of panel p (not interior; both within the 4 ghost layers) for the FP32
+// form, from the stencil tables (side rows [p][s][dep][k - i0] x 4, corner rows
+// [p][corner][di][dj] x 16)
+__device__ __forceinline__ float ghost_table_f(const Src<float> &S, const Dims &d, const GhostTerm *__restrict__ side,
+                                               const GhostTerm *__restrict__ corner, int p, int i, int j) {
+    const bool io = i < d.i0 || i >= d.iend, jo = j < d.i0 || j >= d.iend;
+    if (io && jo) {
+        const int cc = (i >= d.iend ? 2 : 0) + (j >= d.iend ? 1 : 0);
+        const int di = i >= d.iend ? i - d.iend : d.i0 - 1 - i, dj = j >= d.iend ? j - d.iend : d.i0 - 1 - j;
+        return ghost_terms_f<GHOST_CORNER_TERMS>(S, corner + (((p * 4 + cc) * NG + di) * NG + dj) * GHOST_CORNER_TERMS);
+    }
+    int s, dep, k;
+    if (io) {
+        s = i >= d.iend ? SIDE_E : SIDE_W;
+        dep = s == SIDE_E ? i - d.iend : d.i0 - 1 - i;
         k = j;
-    } else if (i < d.i0) {
-        s = SIDE_W;
-        dep = d.i0 - 1 - i;
-        k = j;
-    } else if (j >= d.iend) {
-        s = SIDE_N;
-        dep = j - d.iend;
-        k = i;
-    } else if (j < d.i0) {
-        s = SIDE_S;
-        dep = d.i0 - 1 - j;
+    } else {
+        s = j >= d.iend ? SIDE_N : SIDE_S;
+        dep = s == SIDE_N ? j - d.iend : d.i0 - 1 - j;
         k = i;
     }
-    if (s < 0) return S.value(d, q, i, j);
-    return side_ghost_f(S, d, W, K, q, s, dep, k);
+    return ghost_terms_f<4>(S, side + ((((p * 4 + s) * NG + dep) * d.N) + (k - d.i0)) * 4);
 }
 
-// ghost_value for the FP32 form
-__device__ __forceinline__ float ghost_value_f(const Src<float> &S, const Dims &d, const float2 *__restrict__ W,
-                                               const int *__restrict__ K, int p, int i, int j) {
-    if (i < d.i0 || i >= d.iend) {
-        const int s = i >= d.iend ? SIDE_E : SIDE_W;
-        const int dep = s == SIDE_E ? i - d.iend : d.i0 - 1 - i;
-        if (is_interior(d, j)) return side_ghost_f(S, d, W, K, p, s, dep, j);
-        const Conn c = c_conn[p][s];
-        const int n = d.n;
-        const int k0 = K[dep * n + j];
-        const float2 *w = W + ((long long)dep * n + j) * 4;
-        DFloat prod[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            int kk = k0 + m;
-            int along = c.rev ? n - 1 - kk : kk;
-            int qi, qj;
-            inside_ij(d, c.qs, dep, along, qi, qj);
-            prod[m] = df_prod(cell_or_side_ghost_f(S, d, W, K, c.q, qi, qj), w[m]);
-        }
-        return df_round(df_add(df_add(df_add(prod[0], prod[1]), prod[2]), prod[3]));
-    }
-    const int s = j >= d.iend ? SIDE_N : SIDE_S;
-    const int dep = s == SIDE_N ? j - d.iend : d.i0 - 1 - j;
-    return side_ghost_f(S, d, W, K, p, s, dep, i);
-}
-
-// The ghost-cell value in the state's precision: FP64 sums for FP64 state, double-float sums
-// (weights Wf) for FP32 state
+// The ghost-cell value in the state's precision: FP64 sums in the reference's order for FP64
+// state, the stencil tables for FP32 state
 template <class real>
 __device__ __forceinline__ real ghost_cell(const Src<real> &S, const Dims &d, const double *__restrict__ W,
-                                           const float2 *__restrict__ Wf, const int *__restrict__ K, int p, int i,
-                                           int j);
+                                           const int *__restrict__ K, const GhostTerm *__restrict__ side,
+                                           const GhostTerm *__restrict__ corner, int p, int i, int j);
 template <>
 __device__ __forceinline__ double ghost_cell<double>(const Src<double> &S, const Dims &d, const double *__restrict__ W,
-                                                     const float2 *__restrict__, const int *__restrict__ K, int p,
-                                                     int i, int j) {
+                                                     const int *__restrict__ K, const GhostTerm *__restrict__,
+                                                     const GhostTerm *__restrict__, int p, int i, int j) {
     return ghost_value(S, d, W, K, p, i, j);
 }
 template <>
 __device__ __forceinline__ float ghost_cell<float>(const Src<float> &S, const Dims &d, const double *__restrict__,
-                                                   const float2 *__restrict__ Wf, const int *__restrict__ K, int p,
-                                                   int i, int j) {
-    return ghost_value_f(S, d, Wf, K, p, i, j);
-}
-template <class real>
-__device__ __forceinline__ real side_cell(const Src<real> &S, const Dims &d, const double *__restrict__ W,
-                                          const float2 *__restrict__ Wf, const int *__restrict__ K, int p, int s,
-                                          int dep, int k);
-template <>
-__device__ __forceinline__ double side_cell<double>(const Src<double> &S, const Dims &d, const double *__restrict__ W,
-                                                    const float2 *__restrict__, const int *__restrict__ K, int p,
-                                                    int s, int dep, int k) {
-    return side_ghost(S, d, W, K, p, s, dep, k);
-}
-template <>
-__device__ __forceinline__ float side_cell<float>(const Src<float> &S, const Dims &d, const double *__restrict__,
-                                                  const float2 *__restrict__ Wf, const int *__restrict__ K, int p,
-                                                  int s, int dep, int k) {
-    return side_ghost_f(S, d, Wf, K, p, s, dep, k);
+                                                   const int *__restrict__, const GhostTerm *__restrict__ side,
+                                                   const GhostTerm *__restrict__ corner, int p, int i, int j) {
+    return ghost_table_f(S, d, side, corner, p, i, j);
 }
 
 }  // namespace csadv

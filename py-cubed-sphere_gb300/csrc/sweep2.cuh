@@ -511,7 +511,7 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
 #pragma unroll
                 for (int l = 0; l < NL; ++l) {
                     const Src<float> src{(const float *)S.Qin + (long long)(tr + l) * d.field, gpc, corr[l], hc};
-                    set_lane(v, l, ghost_value_f(src, d, S.lag_wf, S.lag_k, p, I0 + r, J0 + c));
+                    set_lane(v, l, ghost_table_f(src, d, S.gside, S.gcorner, p, I0 + r, J0 + c));
                 }
                 sQ[(r + 3) * QJP + c + 3] = v;
             }

@@ -74,8 +74,7 @@ struct SweepSolve {
     const int *lag_k;       // evaluates the ghost cells of its tiles itself; else it reads them
     const double *hlag_w;   // the same tables for the batched ghost-cell kernel (always set)
     const int *hlag_k;
-    const float2 *lag_wf;   // the weights as FP32 hi + lo pairs (FP32 form), with lag_w / hlag_w
-    const float2 *hlag_wf;
+    const struct GhostTerm *gside, *gcorner;  // the FP32 form's flattened ghost-cell stencils
 };
 
 // blocks of the batched ghost-cell kernel per tracer of a solve (128 ghost-cell columns each)
