@@ -1,14 +1,16 @@
 """``python -m csadv [pardir]``: the advection test case of the reference's main.py:78-95.
 
 Reads par/configuration.par and par/advection.par (or those in `pardir`); test case 5 runs
-one advection simulation (advection test case 1: adv_sphere) or the convergence study
-(advection test case 2: error_analysis_adv) on the GPU.  Other test cases (grid generation,
-grid quality, interpolation, divergence) are outside this library.
+one advection simulation (advection test case 1: adv_sphere, with the lat-lon fields written
+as .npy where the reference plots them) or the convergence study (advection test case 2:
+error_analysis_adv) on the GPU.  Other test cases (grid generation, grid quality,
+interpolation, divergence) are outside this library.
 """
 import sys
 
 from .advection import adv_simulation_par, adv_sphere, cubed_sphere, error_analysis_adv
 from .configuration import PARDIR, get_advection_parameters, get_parameters
+from .latlon import NLAT, NLON, latlon_grid, ll2cs
 
 
 def main(argv=None):
@@ -23,7 +25,10 @@ def main(argv=None):
     dt, Tf, tc, ic, vf, recon, dp, opsplit, et, mt, mf = get_advection_parameters(pardir)
     simulation = adv_simulation_par(cs_grid, dt, Tf, ic, vf, tc, recon, dp, opsplit, et, mt, mf)
     if simulation.tc == 1:
-        return adv_sphere(cs_grid, None, simulation, map_projection, False, False)
+        # the lat-lon grid of the plots (main.py:58-60)
+        ll_grid = latlon_grid(NLAT, NLON)
+        ll_grid.ix, ll_grid.jy, ll_grid.mask = ll2cs(cs_grid, ll_grid)
+        return adv_sphere(cs_grid, ll_grid, simulation, map_projection, True, False)
     return error_analysis_adv(simulation, map_projection, False, transformation, showonscreen, gridload, pardir=pardir)
 
 

@@ -18,6 +18,9 @@ import numpy as np
 
 from . import _lib as L
 
+NLAT = 720        # lat-lon grid of the reference's plots (constants.py:36-37)
+NLON = 2 * NLAT
+
 
 class latlon_grid:
     """Regular lon-lat grid; X, Y, Z on the unit sphere (cs_datastruct.py:569-582)."""

@@ -53,8 +53,13 @@ def test_convergence_study_matches_oracle_and_converges(tmp_path):
 
 def test_module_entry_point_runs_the_par_files(tmp_path):
     from csadv import __main__ as entry
+    from csadv import advection
     pardir = write_par(tmp_path, N=16, tc=1, dt=0.05, Tf=0.5)
+    advection.output_dir = str(tmp_path / "graphs")
     linf, l1, l2 = entry.main([pardir])
+    # the reference plots Q on its 720 x 1440 lat-lon grid at steps 0, 2, ..., 10: written as .npy
+    outs = sorted(os.listdir(advection.output_dir))
+    assert len(outs) == 6 and np.load(os.path.join(advection.output_dir, outs[0])).shape == (1440, 720)
     g = CubedSphere(16)
     ref = solver.adv_sphere(solver.Simulation(g, 0.05, 0.5, 2, 1, 3, 1, 3, 3, 2, 3))
     for a, b in zip((linf, l1, l2), ref):
