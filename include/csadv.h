@@ -136,6 +136,17 @@ int csadv_get_step(const csadv_plan *plan, int *k);
  * current state, written as an interior (N, N, 6) array; the state is not advanced. */
 int csadv_divergence(csadv_plan *plan, int tracer, double *host_div, void *stream);
 
+/* ---------------------------------------------------------------- checkpoint / resume (no counterpart
+ * in the reference, which keeps no state between runs) */
+/* Sets the step counter to k and the wind clock to time k dt with previous time (k-1) dt (the
+ * current and previous winds of per-edge winds likewise): the state k steps of csadv_advance
+ * leave.  With the tracers restored by csadv_set_tracer, a saved run continues with the same bits. */
+int csadv_set_step(csadv_plan *plan, int k, void *stream);
+/* The FP32 form's mass-fixer target of a tracer (the sum of Q g that its MF-PR correction
+ * restores, recorded when the tracer was set): read into *get and/or replaced by *set (either
+ * may be NULL).  CSADV_ERR_UNSUPPORTED for plans without one (FP64, or no MF-PR). */
+int csadv_mass_target(csadv_plan *plan, int tracer, double *get, const double *set, void *stream);
+
 /* ---------------------------------------------------------------- lat-lon output (headless plots) */
 /* ll2cs (interpolation.py:38-140), equiangular grid of N cells per panel edge: for n points
  * (X, Y, Z) on the unit sphere (a lat-lon grid's sph2cart coordinates, sphgeo.py:18-22), the

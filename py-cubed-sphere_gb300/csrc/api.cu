@@ -670,6 +670,36 @@ int csadv_get_stats(csadv_plan *pl, csadv_stats *out) {
     return CSADV_OK;
 }
 
+int csadv_set_step(csadv_plan *pl, int k, void *stream) {
+    if (!pl || k < 0) return CSADV_ERR_ARG;
+    cudaStream_t st = S(stream);
+    int rc = select_device(pl);
+    // the clock (and, for per-edge winds, the current and previous winds) at (k-1) dt, then at
+    // k dt: what k steps of csadv_advance leave
+    pl->k = k > 0 ? k - 1 : 0;
+    if (!rc) rc = do_update_winds(pl, false, pl->k, pl->k * pl->dt, st);
+    pl->k = k;
+    if (!rc) rc = do_update_winds(pl, false, pl->k, pl->k * pl->dt, st);
+    pl->f.rec_ready = false;
+    if (!rc) CSADV_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+int csadv_mass_target(csadv_plan *pl, int tracer, double *get, const double *set, void *stream) {
+    if (!pl || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
+    if (!pl->f.on || !pl->f.mass_target) return CSADV_ERR_UNSUPPORTED;
+    cudaStream_t st = S(stream);
+    if (get) {
+        CSADV_CUDA(cudaMemcpyAsync(get, pl->f.mass_target + tracer, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CSADV_CUDA(cudaStreamSynchronize(st));
+    }
+    if (set) {
+        CSADV_CUDA(cudaMemcpyAsync(pl->f.mass_target + tracer, set, sizeof(double), cudaMemcpyHostToDevice, st));
+        CSADV_CUDA(cudaStreamSynchronize(st));
+    }
+    return CSADV_OK;
+}
+
 int csadv_reset_stats(csadv_plan *pl) {
     if (!pl) return CSADV_ERR_ARG;
     pl->stats = csadv_stats{};
