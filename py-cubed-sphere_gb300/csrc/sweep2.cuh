@@ -433,6 +433,17 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
             asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
         }
     }
+    {   // the Q and metric rows that the tile load reads in its second round (rows 32..)
+        const int r0 = 4 * (SWEEP_THREADS / 32), R = ni + 6, nrow = R > r0 ? R - r0 : 0;
+        const int narr = Lanes<V>::n + (hc ? 1 : 0);
+        for (int k = tid; k < nrow * narr * 3; k += SWEEP_THREADS) {
+            const int l = k % 3, ra = k / 3, a = ra / nrow, r = r0 + ra % nrow;
+            const float *base = (a < Lanes<V>::n ? (const float *)S.Qin + (long long)(tr + a) * d.field + pofs : gpc) +
+                                (long long)(I0 - 3 + r) * P + (J0 - 3);
+            const char *ad = (const char *)base + 128 * l;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(ad));
+        }
+    }
     __syncthreads();
 
     // P0: Q on the tile + 3 halo cells; interior cells with the pending MF-PR correction.  Warp w
