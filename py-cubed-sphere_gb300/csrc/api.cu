@@ -347,6 +347,40 @@ int graph_kernel_nodes(cudaGraph_t g) { return count_kernel_nodes(g); }
 
 }  // namespace csadv
 
+namespace {
+
+// Tracer upload and read-out on the fused engine with MF-PR, without materialising the pending
+// correction of the other tracers: the upload clears this tracer's correction (the new field
+// replaces the corrected one) and, in FP32, records its mass target in the same pass; the
+// read-out forms Q* + g corr as it reads.  Both give the bits of materialise-then-copy.
+template <class real>
+static int tracer_upload(csadv_plan *pl, int tracer, double *src, int layout, cudaStream_t st) {
+    FusedState &f = pl->f;
+    IoLazy<real> x;
+    if (f.on && pl->opt.mf == MF_PR) {
+        x.corr = f.corr[pl->cur] + tracer;
+        if (f.mass_target) {
+            x.g = (const real *)f.g_pc;
+            x.part = f.anchor_part;
+            x.count = f.anchor_count;
+            x.mass = f.mass_target + tracer;
+        }
+    }
+    return tracer_io<real>(pl->grid, (real *)pl->tracer(tracer), src, layout, true, st, &x);
+}
+template <class real>
+static int tracer_download(csadv_plan *pl, int tracer, double *dst, int layout, cudaStream_t st) {
+    FusedState &f = pl->f;
+    IoLazy<real> x;
+    if (f.on && pl->opt.mf == MF_PR && !f.settled) {
+        x.g = (const real *)f.g_pc;
+        x.corr = f.corr[pl->cur] + tracer;
+    }
+    return tracer_io<real>(pl->grid, (real *)pl->tracer(tracer), dst, layout, false, st, &x);
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *csadv_version(void) { return "csadv 0.1 (sm_103a)"; }
@@ -513,17 +547,13 @@ int csadv_set_tracer(csadv_plan *pl, int tracer, const double *host, int layout,
     const Dims d = pl->grid.d;
     const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
     cudaStream_t st = S(stream);
-    int rc = settle(pl, st);
-    if (rc) return rc;
     double *src = mapped_host(host);
     if (!src) {
         CSADV_CUDA(cudaMemcpyAsync(pl->stage, host, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyHostToDevice, st));
         src = pl->stage;
     }
-    rc = pl->opt.precision == 64 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), src, layout, true, st)
-                                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), src, layout, true, st);
-    if (!rc && pl->f.on) rc = fused_anchor_mass(pl->opt, pl->grid, pl->f, pl->cur, tracer, st);
-    return rc;
+    return pl->opt.precision == 64 ? tracer_upload<double>(pl, tracer, src, layout, st)
+                                   : tracer_upload<float>(pl, tracer, src, layout, st);
 }
 
 int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void *stream) {
@@ -532,18 +562,15 @@ int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void 
     const Dims d = pl->grid.d;
     const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
     cudaStream_t st = S(stream);
-    int rc = settle(pl, st);
-    if (rc) return rc;
     // the full array carries the ghost cells filled at the start of the last step, as the
     // reference's Q does; the fused engine keeps them in its other buffer
     if (layout == CSADV_LAYOUT_FULL && pl->f.on && pl->k > 0) {
-        rc = fused_ghosts_to_current(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
+        int rc = fused_ghosts_to_current(pl->opt, pl->grid, pl->T, pl->f, pl->cur, st);
         if (rc) return rc;
     }
     double *dst = mapped_host(host);
-    rc = pl->opt.precision == 64
-                 ? tracer_io<double>(pl->grid, (double *)pl->tracer(tracer), dst ? dst : pl->stage, layout, false, st)
-                 : tracer_io<float>(pl->grid, (float *)pl->tracer(tracer), dst ? dst : pl->stage, layout, false, st);
+    int rc = pl->opt.precision == 64 ? tracer_download<double>(pl, tracer, dst ? dst : pl->stage, layout, st)
+                                     : tracer_download<float>(pl, tracer, dst ? dst : pl->stage, layout, st);
     if (rc) return rc;
     if (!dst)
         CSADV_CUDA(cudaMemcpyAsync(host, pl->stage, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyDeviceToHost, st));

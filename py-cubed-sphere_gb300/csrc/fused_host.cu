@@ -6,6 +6,8 @@
 
 namespace csadv {
 
+constexpr int ANCHOR_BLOCKS = 512;  // blocks of k_anchor_mass
+
 int fused_supported(const Options &o) { return o.et == ET_DG && o.mf != MF_AF; }
 
 __global__ void k_plane_to_float(const double *__restrict__ src, float *dst, long long n) {
@@ -142,7 +144,9 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     f.dsolve = mem.alloc<SweepSolve>(2);
     if (o.precision == 32 && o.mf == MF_PR) {
         f.mass_target = mem.alloc<double>(T);
-        f.anchor_part = mem.alloc<double>(512);
+        const long long io_blocks = ceil_div((long long)d.n * d.n, IO_B);  // the full layout's upload
+        f.anchor_part = mem.alloc<double>(io_blocks > ANCHOR_BLOCKS ? io_blocks : ANCHOR_BLOCKS);
+        f.anchor_count = mem.alloc<unsigned int>(1);
     }
     if (!mem.ok()) return CSADV_ERR_OOM;
     {
@@ -165,6 +169,7 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     CSADV_CUDA(cudaMemsetAsync(f.erx, 0, 2 * (size_t)d.field * es, st));
     CSADV_CUDA(cudaMemsetAsync(f.ery, 0, 2 * (size_t)d.field * es, st));
     if (f.mass_target) CSADV_CUDA(cudaMemsetAsync(f.mass_target, 0, T * sizeof(double), st));
+    if (f.anchor_count) CSADV_CUDA(cudaMemsetAsync(f.anchor_count, 0, sizeof(unsigned int), st));
     CSADV_CUDA(cudaMemsetAsync(f.Qbuf[1], 0, (size_t)T * d.field * es, st));
     for (int b = 0; b < 2; ++b) CSADV_CUDA(cudaMemsetAsync(f.corr[b], 0, T * sizeof(double), st));
     CSADV_CUDA(cudaMemsetAsync(f.counter, 0, sizeof(unsigned int), st));
@@ -327,7 +332,6 @@ int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &
 
 // sum over the interior of Q g (metric in the state's precision): per-block partials over a
 // grid-stride range, then one block sums them in a fixed order -> *out
-constexpr int ANCHOR_BLOCKS = 512;
 template <class real>
 __global__ void k_anchor_mass(const real *__restrict__ Q, const real *__restrict__ g, Dims d, double *part) {
     __shared__ double red[256];

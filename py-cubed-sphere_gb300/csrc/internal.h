@@ -153,7 +153,8 @@ struct FusedState {
     int nitems = 0;             // work items of one sweep launch (6 x tiles)
     bool inline_ghosts = false; // k_sweep evaluates the ET-DG ghost cells of its tiles (no ghost kernel)
     double *mass_target = nullptr;  // [T] FP32 + MF-PR: sum(Q g) of each tracer when it was set
-    double *anchor_part = nullptr;  // [512] block partials of that sum
+    double *anchor_part = nullptr;  // block partials of that sum (k_anchor_mass or the tracer upload)
+    unsigned int *anchor_count = nullptr;  // blocks of the tracer upload that have written theirs
     size_t smem = 0;
 };
 
@@ -198,8 +199,24 @@ template <class real> int fused_launch(const struct FusedArgs &a, int recon, int
 int diag_partials(const Grid &g);
 template <class real>
 int init_tracer(const Grid &g, int ic, int vf, const IcParams &prm, real *Q, cudaStream_t st);
+// Optional work of the layout conversion on the fused engine's state (null pointers: none).
+//  to the device -- *corr = 0: the tracer's pending MF-PR correction belongs to the field the
+//                   upload replaces; with `mass`, sum(Q g) over the interior of the uploaded field
+//                   (FP64 products of the stored values), one partial per block in `part`, summed
+//                   in block order by the block that finishes last (`count` back to 0)
+//  to the host   -- with `corr`, each interior value read out is the true state Q* + g corr
+constexpr int IO_B = 128;  // cells per block of the layout conversion
 template <class real>
-int tracer_io(const Grid &g, real *Q, double *dev_stage, int layout, bool to_native, cudaStream_t st);
+struct IoLazy {
+    const real *g = nullptr;  // metric plane in the state's precision
+    double *corr = nullptr;   // this tracer's pending correction
+    double *part = nullptr;   // [blocks of the conversion]
+    unsigned int *count = nullptr;
+    double *mass = nullptr;
+};
+template <class real>
+int tracer_io(const Grid &g, real *Q, double *dev_stage, int layout, bool to_native, cudaStream_t st,
+              const IoLazy<real> *lazy = nullptr);
 template <class real>
 int diag_mass(const Grid &g, const real *Q, double *dev_tmp, double &mass, cudaStream_t st);
 template <class real>

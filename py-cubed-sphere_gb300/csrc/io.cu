@@ -10,6 +10,7 @@
 
 #include "cases.cuh"
 #include "common.cuh"
+#include "halo.cuh"
 #include "internal.h"
 
 namespace csadv {
@@ -33,16 +34,31 @@ __device__ __forceinline__ long long host_index(const Dims &d, int layout, int p
     return ((long long)(i - d.i0) * d.N + (j - d.i0)) * NFACE + p;
 }
 
-// Reference layout A[i][j][p] (p fastest) <-> native planes, 128 cells per block: the block's
-// 768 host values form one contiguous range, copied between the host array and shared memory
+// Reference layout A[i][j][p] (p fastest) <-> native planes, IO_B cells per block: the block's
+// 6 IO_B host values form one contiguous range, copied between the host array and shared memory
 // with consecutive lanes on consecutive addresses (16 bytes per lane when the host array is
 // 16-byte aligned), so the interconnect sees whole lines; each thread then moves the six panel
 // values of one cell, consecutive threads on consecutive columns of each plane.  `host` may be a
-// device buffer or page-locked host memory mapped into the device.
-constexpr int IO_B = 128;
+// device buffer or page-locked host memory mapped into the device.  `x` adds the work on the
+// fused engine's state (the pending correction, the mass record) to the same pass.
+__device__ __forceinline__ double block_sum(double v, double *ws) {
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, s));
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int w = 0; w < IO_B / 32; ++w) t = __dadd_rn(t, ws[w]);
+    __syncthreads();
+    return t;  // thread 0
+}
+
 template <class real, bool VEC>
-__global__ void k_io(Dims d, real *Q, double *host, int layout, int to_native) {
+__global__ void __launch_bounds__(IO_B) k_io(Dims d, real *Q, double *host, int layout, int to_native, IoLazy<real> x) {
     __shared__ __align__(16) double s[IO_B * NFACE];
+    __shared__ double ws[IO_B / 32];
+    __shared__ int last;
     const int m = layout == CSADV_LAYOUT_FULL ? d.n : d.N;
     const int off = layout == CSADV_LAYOUT_FULL ? 0 : d.i0;
     const long long cell0 = (long long)blockIdx.x * IO_B, ncell = (long long)m * m;
@@ -50,20 +66,54 @@ __global__ void k_io(Dims d, real *Q, double *host, int layout, int to_native) {
     double *h = host + cell0 * NFACE;
     const int tid = threadIdx.x;
     const long long cell = cell0 + tid;
-    const long long o = (long long)(off + cell / m) * d.pitch + off + cell % m;
+    const int i = off + (int)(cell / m), j = off + (int)(cell % m);
+    const long long o = at2(d, i, j);
+    const bool inner = tid < nc && i >= d.i0 && i < d.iend && j >= d.i0 && j < d.iend;
     if (to_native) {
         if (VEC)
             for (int e = tid; e < nc * NFACE / 2; e += IO_B) ((double2 *)s)[e] = ((const double2 *)h)[e];
         else
             for (int e = tid; e < nc * NFACE; e += IO_B) s[e] = h[e];
         __syncthreads();
+        double mp = 0.0;
+        const double gw = x.mass && inner ? (double)x.g[o] : 0.0;
         if (tid < nc)
 #pragma unroll
-            for (int p = 0; p < NFACE; ++p) Q[p * d.plane + o] = (real)s[tid * NFACE + p];
+            for (int p = 0; p < NFACE; ++p) {
+                const real v = (real)s[tid * NFACE + p];
+                Q[p * d.plane + o] = v;
+                if (x.mass && inner) mp = __dadd_rn(mp, __dmul_rn((double)v, gw));
+            }
+        if (x.corr && blockIdx.x == 0 && tid == 0) *x.corr = 0.0;
+        if (x.mass) {  // the same for every block
+            mp = block_sum(mp, ws);
+            if (tid == 0) {
+                x.part[blockIdx.x] = mp;
+                __threadfence();
+                last = atomicAdd(x.count, 1u) == gridDim.x - 1;
+            }
+            __syncthreads();
+            if (last) {
+                __threadfence();
+                double a = 0.0;
+                for (int b = tid; b < (int)gridDim.x; b += IO_B) a = __dadd_rn(a, __ldcg(x.part + b));
+                a = block_sum(a, ws);
+                if (tid == 0) {
+                    *x.mass = a;
+                    *x.count = 0u;
+                }
+            }
+        }
     } else {
-        if (tid < nc)
+        if (tid < nc) {
+            const bool fix = x.corr && inner;
+            const real c = fix ? (real)*x.corr : real(0), gc = fix ? x.g[o] : real(0);
 #pragma unroll
-            for (int p = 0; p < NFACE; ++p) s[tid * NFACE + p] = (double)Q[p * d.plane + o];
+            for (int p = 0; p < NFACE; ++p) {
+                const real v = Q[p * d.plane + o];
+                s[tid * NFACE + p] = (double)(fix ? corrected(v, gc, c) : v);
+            }
+        }
         __syncthreads();
         if (VEC)
             for (int e = tid; e < nc * NFACE / 2; e += IO_B) ((double2 *)h)[e] = ((const double2 *)s)[e];
@@ -167,13 +217,15 @@ int init_tracer(const Grid &g, int ic, int vf, const IcParams &prm, real *Q, cud
 }
 
 template <class real>
-int tracer_io(const Grid &g, real *Q, double *dev_stage, int layout, bool to_native, cudaStream_t st) {
+int tracer_io(const Grid &g, real *Q, double *dev_stage, int layout, bool to_native, cudaStream_t st,
+              const IoLazy<real> *lazy) {
     const int m = layout == CSADV_LAYOUT_FULL ? g.d.n : g.d.N;
     const long long tot = (long long)m * m;
+    const IoLazy<real> x = lazy ? *lazy : IoLazy<real>{};
     if (((uintptr_t)dev_stage & 15) == 0)
-        k_io<real, true><<<ceil_div(tot, IO_B), IO_B, 0, st>>>(g.d, Q, dev_stage, layout, to_native ? 1 : 0);
+        k_io<real, true><<<ceil_div(tot, IO_B), IO_B, 0, st>>>(g.d, Q, dev_stage, layout, to_native ? 1 : 0, x);
     else
-        k_io<real, false><<<ceil_div(tot, IO_B), IO_B, 0, st>>>(g.d, Q, dev_stage, layout, to_native ? 1 : 0);
+        k_io<real, false><<<ceil_div(tot, IO_B), IO_B, 0, st>>>(g.d, Q, dev_stage, layout, to_native ? 1 : 0, x);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -210,7 +262,7 @@ int diag_errors(const Grid &g, const real *Q, int ic, int vf, const IcParams &pr
 
 #define INST(real)                                                                                       \
     template int init_tracer<real>(const Grid &, int, int, const IcParams &, real *, cudaStream_t);     \
-    template int tracer_io<real>(const Grid &, real *, double *, int, bool, cudaStream_t);              \
+    template int tracer_io<real>(const Grid &, real *, double *, int, bool, cudaStream_t, const IoLazy<real> *); \
     template int diag_mass<real>(const Grid &, const real *, double *, double &, cudaStream_t);         \
     template int diag_errors<real>(const Grid &, const real *, int, int, const IcParams &, double, double *, \
                                    double *, cudaStream_t);

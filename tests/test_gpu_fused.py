@@ -140,6 +140,53 @@ def test_fused_set_get_between_steps_keeps_state():
         assert rel(b.get_tracer(), a.get_tracer()) <= RTOL
 
 
+@pytest.mark.parametrize("prec", [64, 32])
+def test_upload_of_one_tracer_leaves_the_others_pending(prec):
+    # set_tracer / get_tracer with a pending MF-PR correction on the other tracers give the bits
+    # of materialise-then-copy (here forced by a mass diagnostic before the upload)
+    c, vf, dt, N = (2, 2, 1, 3, 1, 3), 2, 0.004, 32
+    rng = np.random.default_rng(11)
+    q = 1.0 + 0.1 * rng.standard_normal((N + 8, N + 8, 6))
+    with plan(N, dt, c, vf, engine=FUSED, ntracers=3, precision=prec) as a, \
+            plan(N, dt, c, vf, engine=FUSED, ntracers=3, precision=prec) as b:
+        for pl in (a, b):
+            for t, ic in enumerate((2, 3, 4)):
+                pl.init_tracer(ic, tracer=t)
+            pl.advance(3)
+        lazy = [b.get_tracer(t, full=True) for t in range(3)]
+        a.mass(0)  # materialises the correction of every tracer
+        for t in range(3):
+            np.testing.assert_array_equal(lazy[t], a.get_tracer(t, full=True))
+        for pl in (a, b):
+            pl.set_tracer(q, tracer=1)
+            pl.advance(3)
+        for t in range(3):
+            np.testing.assert_array_equal(b.get_tracer(t), a.get_tracer(t))
+
+
+@pytest.mark.parametrize("full", [True, False])
+def test_fp32_upload_records_the_mass_target(full):
+    # the FP32 upload records sum(Q g) over the interior (FP64 products of the stored FP32
+    # values and the FP32 metric) as the tracer's mass target, in the same pass; 1e-9 relative
+    # allows an ulp of difference between the oracle's metric and the device's in a few cells
+    import ctypes
+    from csadv import _lib
+    N, dt = 40, 0.004
+    rng = np.random.default_rng(5)
+    q = 1.0 + 0.1 * rng.standard_normal((N + 8, N + 8, 6) if full else (N, N, 6))
+    g32 = CubedSphere(N).metric_tensor_pc[4:N + 4, 4:N + 4].astype(np.float32).astype(np.float64)
+    with plan(N, dt, (2, 2, 1, 3, 1, 3), 2, engine=FUSED, ntracers=2, precision=32) as pl:
+        pl.init_tracer(2, tracer=0)
+        pl.advance(2)
+        pl.set_tracer(q, tracer=1)
+        m = ctypes.c_double()
+        _lib.check(_lib.lib().csadv_mass_target(pl._h, 1, ctypes.byref(m), None, pl.stream))
+        qi = (q[4:N + 4, 4:N + 4] if full else q).astype(np.float32).astype(np.float64)
+        want = float(np.sum(qi * g32))
+        assert abs(m.value - want) <= 1e-9 * abs(want)
+        np.testing.assert_array_equal(pl.get_tracer(1), qi)
+
+
 @pytest.mark.parametrize("c", [(2, 2, 1, 3, 1, 3), (3, 1, 1, 3, 1, 3)])
 def test_fp32_form_accuracy_and_mass(c):
     N, dt, nsteps, ic, vf = 96, 0.002, 80, 3, 2
