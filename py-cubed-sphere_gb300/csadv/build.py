@@ -38,6 +38,8 @@ UNITS = {
     "fused_f32.cu": True,
     "fused_f64.cu": True,
     "sweep_f32.cu": True,
+    "sweep_f32_pairs.cu": True,
+    "sweep_f32_one.cu": True,
     "sweep_f64.cu": True,
     "noalloc.cu": False,
     "latlon.cu": False,

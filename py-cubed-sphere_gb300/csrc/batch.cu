@@ -35,6 +35,7 @@ struct csadv_batch {
     int nwork = 0, nhwork = 0;
     size_t smem = 0;
     int precision = 0, recon = 0, split = 0;
+    int tgroup = 0;                  // tracer grouping of the FP32 step kernel (SWEEP_TG_*)
     int phase = 0;                   // steps since the tables were built, mod 2
     bool dirty = true;
     bool graphs = true;
@@ -140,6 +141,9 @@ int batch_rebuild(csadv_batch *b, cudaStream_t st) {
     b->precision = b->plans.front()->opt.precision;
     b->recon = b->plans.front()->opt.recon;
     b->split = b->plans.front()->opt.opsplit;
+    b->tgroup = sweep_tgroup(b->plans.front()->T);
+    for (csadv_plan *pl : b->plans)
+        if (sweep_tgroup(pl->T) != b->tgroup) b->tgroup = SWEEP_TG_ANY;
     b->dirty = false;
     return CSADV_OK;
 }
@@ -164,8 +168,10 @@ int batch_step_work(csadv_batch *b, int kind, cudaStream_t st) {
     }
     if (b->prof) CSADV_CUDA(cudaEventRecord(b->pev[0], st));
     int rc = b->precision == 64
-                 ? sweep_launch<double>(b->recon, b->split, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st)
-                 : sweep_launch<float>(b->recon, b->split, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st);
+                 ? sweep_launch<double>(b->recon, b->split, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st,
+                                        b->tgroup)
+                 : sweep_launch<float>(b->recon, b->split, b->dsolves, b->dwork[b->phase], b->nwork, b->nwork, b->smem, st,
+                                       b->tgroup);
     if (rc) return rc;
     if (b->prof) CSADV_CUDA(cudaEventRecord(b->pev[1], st));
     for (csadv_plan *pl : b->plans) {

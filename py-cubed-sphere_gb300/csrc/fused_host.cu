@@ -217,8 +217,8 @@ int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt,
 
 int fused_prepare(const Options &o, int tile) {
     if (tile >= FUSED_NTILE_CFG)
-        return o.precision == 64 ? sweep_launch<double>(o.recon, o.opsplit, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1)
-                                 : sweep_launch<float>(o.recon, o.opsplit, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1);
+        return o.precision == 64 ? sweep_launch<double>(o.recon, o.opsplit, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1, 0)
+                                 : sweep_launch<float>(o.recon, o.opsplit, nullptr, nullptr, 0, 0, 0, (cudaStream_t)-1, 0);
     FusedArgs a{};
     return o.precision == 64 ? fused_launch<double>(a, o.recon, tile, (cudaStream_t)-1)
                              : fused_launch<float>(a, o.recon, tile, (cudaStream_t)-1);
@@ -291,8 +291,9 @@ int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &
     if (f.sweep) {
         if (ev0) CSADV_CUDA(cudaEventRecord(ev0, st));
         int rc = o.precision == 64
-                     ? sweep_launch<double>(o.recon, o.opsplit, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st)
-                     : sweep_launch<float>(o.recon, o.opsplit, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st);
+                     ? sweep_launch<double>(o.recon, o.opsplit, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st, 0)
+                     : sweep_launch<float>(o.recon, o.opsplit, f.dsolve + cur, nullptr, f.nitems, f.nitems, f.smem, st,
+                                           sweep_tgroup(T));
         if (rc) return rc;
         if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
         cur = 1 - cur;

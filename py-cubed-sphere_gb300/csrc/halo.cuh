@@ -162,16 +162,17 @@ __device__ __forceinline__ float ghost_terms_f(const Src<float> &S, const GhostT
     return df_round(acc);
 }
 
-// the ghost cell (i, j) of panel p (not interior; both within the 4 ghost layers) for the FP32
-// form, from the stencil tables (side rows [p][s][dep][k - i0] x 4, corner rows
-// [p][corner][di][dj] x 16)
-__device__ __forceinline__ float ghost_table_f(const Src<float> &S, const Dims &d, const GhostTerm *__restrict__ side,
-                                               const GhostTerm *__restrict__ corner, int p, int i, int j) {
+// the stencil-table row of the ghost cell (i, j) of panel p (not interior; both within the 4 ghost
+// layers): side rows [p][s][dep][k - i0] x 4 terms, corner rows [p][corner][di][dj] x 16
+__device__ __forceinline__ const GhostTerm *ghost_row(const Dims &d, const GhostTerm *__restrict__ side,
+                                                      const GhostTerm *__restrict__ corner, int p, int i, int j,
+                                                      bool &is_corner) {
     const bool io = i < d.i0 || i >= d.iend, jo = j < d.i0 || j >= d.iend;
-    if (io && jo) {
+    is_corner = io && jo;
+    if (is_corner) {
         const int cc = (i >= d.iend ? 2 : 0) + (j >= d.iend ? 1 : 0);
         const int di = i >= d.iend ? i - d.iend : d.i0 - 1 - i, dj = j >= d.iend ? j - d.iend : d.i0 - 1 - j;
-        return ghost_terms_f<GHOST_CORNER_TERMS>(S, corner + (((p * 4 + cc) * NG + di) * NG + dj) * GHOST_CORNER_TERMS);
+        return corner + (((p * 4 + cc) * NG + di) * NG + dj) * GHOST_CORNER_TERMS;
     }
     int s, dep, k;
     if (io) {
@@ -183,7 +184,64 @@ __device__ __forceinline__ float ghost_table_f(const Src<float> &S, const Dims &
         dep = s == SIDE_N ? j - d.iend : d.i0 - 1 - j;
         k = i;
     }
-    return ghost_terms_f<4>(S, side + ((((p * 4 + s) * NG + dep) * d.N) + (k - d.i0)) * 4);
+    return side + ((((p * 4 + s) * NG + dep) * d.N) + (k - d.i0)) * 4;
+}
+
+// the ghost cell (i, j) of panel p for the FP32 form, from the stencil tables
+__device__ __forceinline__ float ghost_table_f(const Src<float> &S, const Dims &d, const GhostTerm *__restrict__ side,
+                                               const GhostTerm *__restrict__ corner, int p, int i, int j) {
+    bool cn;
+    const GhostTerm *t = ghost_row(d, side, corner, p, i, j, cn);
+    return cn ? ghost_terms_f<GHOST_CORNER_TERMS>(S, t) : ghost_terms_f<4>(S, t);
+}
+
+// Two fields at once (the two tracers of a pair in the FP32 step kernel; F1 = F0 + one field):
+// each table entry and metric value is loaded once for both.  Per field the arithmetic is
+// ghost_terms_f's, term by term, so each result has ghost_table_f's bits.  Terms are taken
+// 8 at a time (loads of a chunk, then its arithmetic) to bound the registers held.
+template <int NT>
+__device__ __forceinline__ float2 ghost_terms_f2(const float *__restrict__ F0, const float *__restrict__ F1,
+                                                 const float *__restrict__ g, float c0, float c1, bool has_corr,
+                                                 const GhostTerm *__restrict__ t) {
+    constexpr int CH = NT < 8 ? NT : 8;
+    DFloat a0{0.f, 0.f}, a1{0.f, 0.f};
+#pragma unroll
+    for (int m0 = 0; m0 < NT; m0 += CH) {
+        GhostTerm x[CH];
+#pragma unroll
+        for (int m = 0; m < CH; ++m) x[m] = t[m0 + m];
+        float v0[CH], v1[CH];
+#pragma unroll
+        for (int m = 0; m < CH; ++m) {
+            v0[m] = F0[x[m].o];
+            v1[m] = F1[x[m].o];
+            if (has_corr) {
+                const float gg = g[x[m].o2];
+                v0[m] = corrected(v0[m], gg, c0);
+                v1[m] = corrected(v1[m], gg, c1);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < CH; ++m) {
+            if (m0 + m == 0) {
+                a0 = df_prod(v0[0], x[0].w);
+                a1 = df_prod(v1[0], x[0].w);
+            } else {
+                a0 = df_add(a0, df_prod(v0[m], x[m].w));
+                a1 = df_add(a1, df_prod(v1[m], x[m].w));
+            }
+        }
+    }
+    return make_float2(df_round(a0), df_round(a1));
+}
+
+__device__ __forceinline__ float2 ghost_table_f2(const float *F0, const float *F1, const float *g, float c0, float c1,
+                                                 bool has_corr, const Dims &d, const GhostTerm *__restrict__ side,
+                                                 const GhostTerm *__restrict__ corner, int p, int i, int j) {
+    bool cn;
+    const GhostTerm *t = ghost_row(d, side, corner, p, i, j, cn);
+    return cn ? ghost_terms_f2<GHOST_CORNER_TERMS>(F0, F1, g, c0, c1, has_corr, t)
+              : ghost_terms_f2<4>(F0, F1, g, c0, c1, has_corr, t);
 }
 
 // The ghost-cell value in the state's precision: FP64 sums in the reference's order for FP64

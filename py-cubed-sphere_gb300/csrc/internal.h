@@ -176,13 +176,15 @@ int fused_prepare(const Options &o, int tile);
 // select the tile configuration of the fused engine (tile code as in csadv_options.tile,
 // zero-based); rewrites the sweep descriptors.  Outside stream capture.
 int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState &f, int tile, cudaStream_t st);
+// the line-marching step kernel over `nwork` items (stream -1: prepare the kernels' shared-memory
+// limits only); tgroup (SWEEP_TG_*) is how the FP32 form groups the tracers of the solves
 template <class real>
 int sweep_launch(int recon, int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
-                 cudaStream_t st);
+                 cudaStream_t st, int tgroup);
 // the FP32 form runs the paired-tracer kernel (sweep2.cuh)
 template <>
 int sweep_launch<float>(int recon, int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid,
-                        size_t smem, cudaStream_t st);
+                        size_t smem, cudaStream_t st, int tgroup);
 // edge records of the line-marching kernel from the reference-layout winds (static winds: once)
 template <class real, class V>
 int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT,

@@ -517,7 +517,7 @@ int sweep_split(int split, const SweepSolve *dsolves, const int2 *work, int nwor
 
 template <class real>
 int sweep_launch(int recon, int split, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
-                 cudaStream_t st) {
+                 cudaStream_t st, int) {
     switch (recon) {
         case REC_PPM0: return sweep_split<real, REC_PPM0>(split, dsolves, work, nwork, grid, smem, st);
         case REC_CW84: return sweep_split<real, REC_CW84>(split, dsolves, work, nwork, grid, smem, st);

@@ -519,10 +519,13 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
                     c = nj + (k - cw - ce - cs) % 3;
                 }
                 V v;
-#pragma unroll
-                for (int l = 0; l < NL; ++l) {
-                    const Src<float> src{(const float *)S.Qin + (long long)(tr + l) * d.field, gpc, corr[l], hc};
-                    set_lane(v, l, ghost_table_f(src, d, S.gside, S.gcorner, p, I0 + r, J0 + c));
+                if constexpr (Lanes<V>::n == 2) {  // one table load serves both tracers
+                    const float *F0 = (const float *)S.Qin + (long long)tr * d.field;
+                    v = ghost_table_f2(F0, F0 + d.field, gpc, corr[0], corr[1], hc, d, S.gside, S.gcorner, p, I0 + r,
+                                       J0 + c);
+                } else {
+                    const Src<float> src{(const float *)S.Qin + (long long)tr * d.field, gpc, corr[0], hc};
+                    set_lane(v, 0, ghost_table_f(src, d, S.gside, S.gcorner, p, I0 + r, J0 + c));
                 }
                 sQ[(r + 3) * QJP + c + 3] = v;
             }
@@ -638,7 +641,10 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
 }
 
 // SPL: the splitting (SP_AVLT, SP_L04 with MT-0; SP_PL07 with MT-PL07), fixed per kernel
-template <int REC, int SPL>
+// TG: how the launch groups the tracers of its solves (SWEEP_TG_*): pairs only (every T even),
+// one at a time (T = 1), or pairs and an odd last one (any T).  Each grouping is its own kernel so
+// that the pair and single paths do not share one register allocation.
+template <int REC, int SPL, int TG>
 __global__ void __launch_bounds__(SWEEP_THREADS, 2) k_sweep2(const SweepSolve *__restrict__ solves,
                                                            const int2 *__restrict__ work, int nwork) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -654,11 +660,17 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 2) k_sweep2(const SweepSolve *_
         int I0, ni, J0, nj;
         sweep_tile(S, tile, I0, ni, J0, nj);
         const int T = S.T;
-        for (int tr = 0; tr < T; tr += 2) {
-            if (tr + 1 < T)
-                tile_pass<REC, SPL, float2>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
-            else
-                tile_pass<REC, SPL, float>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
+        if (TG == SWEEP_TG_PAIRS) {
+            for (int tr = 0; tr + 1 < T; tr += 2) tile_pass<REC, SPL, float2>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
+        } else if (TG == SWEEP_TG_ONE) {
+            for (int tr = 0; tr < T; ++tr) tile_pass<REC, SPL, float>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
+        } else {
+            for (int tr = 0; tr < T; tr += 2) {
+                if (tr + 1 < T)
+                    tile_pass<REC, SPL, float2>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
+                else
+                    tile_pass<REC, SPL, float>(S, p, it.y, tr, I0, ni, J0, nj, smem_raw, red);
+            }
         }
         if (S.mfpr) {
             // the last item of the solve to finish sums its partials: corr = dt m0 / a2, or (FP32
@@ -692,40 +704,39 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 2) k_sweep2(const SweepSolve *_
     }
 }
 
-template <int REC, int SPL>
+template <int REC, int SPL, int TG>
 int go(const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem, cudaStream_t st) {
     if (st == (cudaStream_t)-1) {  // prepare only: allow the largest layout
         size_t mx = 0;
         for (int c = 0; c < SWEEP_NTILE_CFG; ++c) mx = mx > sweep_smem_bytes<float>(c) ? mx : sweep_smem_bytes<float>(c);
-        CSADV_CUDA(cudaFuncSetAttribute(k_sweep2<REC, SPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+        CSADV_CUDA(cudaFuncSetAttribute(k_sweep2<REC, SPL, TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
         return CSADV_OK;
     }
-    k_sweep2<REC, SPL><<<grid, SWEEP_THREADS, smem, st>>>(dsolves, work, nwork);
+    k_sweep2<REC, SPL, TG><<<grid, SWEEP_THREADS, smem, st>>>(dsolves, work, nwork);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
 
-template <int REC>
+template <int REC, int TG>
 int split(int spl, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem, cudaStream_t st) {
     switch (spl) {
-        case SP_AVLT: return go<REC, SP_AVLT>(dsolves, work, nwork, grid, smem, st);
-        case SP_L04: return go<REC, SP_L04>(dsolves, work, nwork, grid, smem, st);
-        default: return go<REC, SP_PL07>(dsolves, work, nwork, grid, smem, st);
+        case SP_AVLT: return go<REC, SP_AVLT, TG>(dsolves, work, nwork, grid, smem, st);
+        case SP_L04: return go<REC, SP_L04, TG>(dsolves, work, nwork, grid, smem, st);
+        default: return go<REC, SP_PL07, TG>(dsolves, work, nwork, grid, smem, st);
+    }
+}
+
+// the kernels of one tracer grouping (each grouping is instantiated in its own translation unit)
+template <int TG>
+int launch_group(int recon, int spl, const SweepSolve *dsolves, const int2 *work, int nwork, int grid, size_t smem,
+                 cudaStream_t st) {
+    switch (recon) {
+        case REC_PPM0: return split<REC_PPM0, TG>(spl, dsolves, work, nwork, grid, smem, st);
+        case REC_CW84: return split<REC_CW84, TG>(spl, dsolves, work, nwork, grid, smem, st);
+        case REC_PL07: return split<REC_PL07, TG>(spl, dsolves, work, nwork, grid, smem, st);
+        default: return split<REC_L04, TG>(spl, dsolves, work, nwork, grid, smem, st);
     }
 }
 
 }  // namespace pairk
-
-// the FP32 form's step kernel: tracers in pairs (k_sweep2)
-template <>
-int sweep_launch<float>(int recon, int spl, const SweepSolve *dsolves, const int2 *work, int nwork, int grid,
-                        size_t smem, cudaStream_t st) {
-    switch (recon) {
-        case REC_PPM0: return pairk::split<REC_PPM0>(spl, dsolves, work, nwork, grid, smem, st);
-        case REC_CW84: return pairk::split<REC_CW84>(spl, dsolves, work, nwork, grid, smem, st);
-        case REC_PL07: return pairk::split<REC_PL07>(spl, dsolves, work, nwork, grid, smem, st);
-        default: return pairk::split<REC_L04>(spl, dsolves, work, nwork, grid, smem, st);
-    }
-}
-
 }  // namespace csadv

@@ -3,5 +3,5 @@
 #include "sweep.cuh"
 
 namespace csadv {
-template int sweep_launch<double>(int, int, const SweepSolve *, const int2 *, int, int, size_t, cudaStream_t);
+template int sweep_launch<double>(int, int, const SweepSolve *, const int2 *, int, int, size_t, cudaStream_t, int);
 }

@@ -81,6 +81,10 @@ struct SweepSolve {
 __host__ __device__ inline int halo_blocks(const Dims &d) { return (NFACE * 4 * NG * d.n + 127) / 128; }
 
 constexpr int SWEEP_THREADS = 256;
+// tracer grouping of an FP32 step-kernel launch: tracers of every solve in pairs (all T even), one
+// at a time (T = 1), or pairs and an odd last one (any T)
+constexpr int SWEEP_TG_ANY = 0, SWEEP_TG_PAIRS = 1, SWEEP_TG_ONE = 2;
+inline int sweep_tgroup(int T) { return T == 1 ? SWEEP_TG_ONE : T % 2 == 0 ? SWEEP_TG_PAIRS : SWEEP_TG_ANY; }
 // largest tile shapes of the sweep kernels: {ti, tj}; the N cells of each direction are split into
 // nearly equal tiles no larger than these (sweep_tile)
 constexpr int SWEEP_TILES[][2] = {{55, 55}, {55, 26}, {26, 55}, {26, 26}};
