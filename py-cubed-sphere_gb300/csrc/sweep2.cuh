@@ -31,9 +31,25 @@ namespace pairk {
 typedef unsigned long long u64;
 
 #ifndef CSADV_PAIR_UNROLL
-#define CSADV_PAIR_UNROLL 2
+#define CSADV_PAIR_UNROLL 0
 #endif
-constexpr int PAIR_UNROLL = CSADV_PAIR_UNROLL;  // march loop unrolling
+#ifndef CSADV_UNROLL_LIGHT
+#define CSADV_UNROLL_LIGHT 3
+#endif
+// march loop unrolling: 3 for the lighter reconstructions (PPM-0, PL07), 2 for the limited ones,
+// whose longer bodies leave no registers for a third copy
+template <int REC>
+constexpr int pair_unroll() {
+    return CSADV_PAIR_UNROLL ? CSADV_PAIR_UNROLL : (REC == REC_PPM0 || REC == REC_PL07) ? CSADV_UNROLL_LIGHT : 2;
+}
+#ifndef CSADV_EDGE_AHEAD
+#define CSADV_EDGE_AHEAD 3
+#endif
+#ifndef CSADV_CELL_AHEAD
+#define CSADV_CELL_AHEAD 2
+#endif
+// how far ahead of its use the march loads edge (2 or 3) and cell (1 or 2) records
+constexpr int EDGE_AHEAD = CSADV_EDGE_AHEAD, CELL_AHEAD = CSADV_CELL_AHEAD;
 
 // ------------------------------------------------------------------ one- and two-lane arithmetic
 __device__ __forceinline__ float vadd(float a, float b) { return __fadd_rn(a, b); }
@@ -253,6 +269,7 @@ struct Marcher {
     V w[5];
     Recon<REC, V> rc;
     float2 eA, eB, cC, cP;  // edges m, m+1; cells m, m-1
+    float2 eC, cD;          // edge m+2, cell m+1 (deeper lookahead)
     V pL, pR, pQ, Fp;       // previous cell's (metric-weighted) parabola and mean; flux through edge m-1
     float cmp;              // g u dt/dx at edge m-1 (SP-L04, SP-PL07)
     V *out;
@@ -273,10 +290,12 @@ struct Marcher {
         const float2 *e = erec + (long long)(ma - 1) * P;
         eA = __ldg(e);
         eB = __ldg(e + P);
-        ef = e + 2 * (long long)P;
+        if (EDGE_AHEAD == 3) eC = __ldg(e + 2 * (long long)P);
+        ef = e + EDGE_AHEAD * (long long)P;
         const float2 *c = crec + (long long)(ma - 1) * P;
         cC = __ldg(c);
-        cf = c + P;
+        if (CELL_AHEAD == 2) cD = __ldg(c + P);
+        cf = c + CELL_AHEAD * (long long)P;
     }
 
     // iteration m: parabola of cell m; with FLUX the flux through edge m; with OUT the output of
@@ -367,8 +386,18 @@ struct Marcher {
         pQ = cQ;
         cP = cC;
         eA = eB;
-        eB = eN;
-        cC = cN;
+        if (EDGE_AHEAD == 3) {
+            eB = eC;
+            eC = eN;
+        } else {
+            eB = eN;
+        }
+        if (CELL_AHEAD == 2) {
+            cC = cD;
+            cD = cN;
+        } else {
+            cC = cN;
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) w[k] = w[k + 1];
         w[4] = wn;
@@ -379,7 +408,8 @@ struct Marcher {
     __device__ __forceinline__ void run(int ma, int mb) {
         step<false, false>();
         step<true, false>();
-#pragma unroll PAIR_UNROLL
+        constexpr int U = pair_unroll<REC>();
+#pragma unroll U
         for (int m = ma + 1; m <= mb; ++m) step<true, true>();
     }
 };
