@@ -147,6 +147,17 @@ int csadv_set_step(csadv_plan *plan, int k, void *stream);
  * may be NULL).  CSADV_ERR_UNSUPPORTED for plans without one (FP64, or no MF-PR). */
 int csadv_mass_target(csadv_plan *plan, int tracer, double *get, const double *set, void *stream);
 
+/* ---------------------------------------------------------------- grid file */
+/* The arrays of the reference's grid file (save_grid_netcdf4, plot.py:522-660; read back by
+ * cubed_sphere, cs_datastruct.py:45-195) for the equiangular grid of N cells per panel edge and
+ * 4 ghost layers, computed on the device: kind 0 po (cell corners, (N+9) x (N+9)), 1 pc (centres,
+ * (N+8) x (N+8)), 2 pu (x-edges, (N+9) x (N+8)), 3 pv (y-edges, (N+8) x (N+9)).  P[i][j][panel][5]
+ * = X, Y, Z, lon, lat (cs_datastruct.py:238-330 with cs_transform.py:41-96); EX, EY the tangent
+ * vectors in the same layout (cs_transform.py:245-397: X, Y, Z, then lon = lat = 0 as the
+ * reference leaves them).  Any of P, EX, EY may be NULL; host arrays, page-locked ones used in
+ * place.  Returns when the outputs are written. */
+int csadv_grid_points(int N, int kind, double *P, double *EX, double *EY, void *stream);
+
 /* ---------------------------------------------------------------- lat-lon output (headless plots) */
 /* ll2cs (interpolation.py:38-140), equiangular grid of N cells per panel edge: for n points
  * (X, Y, Z) on the unit sphere (a lat-lon grid's sph2cart coordinates, sphgeo.py:18-22), the

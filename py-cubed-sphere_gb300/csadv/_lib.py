@@ -93,6 +93,7 @@ _SIGS = {
     "csadv_tune": ([_vp, _c_int, _vp, ctypes.POINTER(_c_int)], _c_int),
     "csadv_mass_fixer_noalloc": ([_vp, _vp, _vp, _c_int, _vp], _c_int),
     "csadv_host_alloc": ([ctypes.POINTER(_vp), ctypes.c_size_t], _c_int),
+    "csadv_grid_points": ([_c_int, _c_int, _vp, _vp, _vp, _vp], _c_int),
     "csadv_ll2cs": ([_c_int, _vp, _vp, _vp, ctypes.c_longlong, _vp, _vp, _vp, _vp], _c_int),
     "csadv_set_step": ([_vp, _c_int, _vp], _c_int),
     "csadv_mass_target": ([_vp, _c_int, _dp, _dp, _vp], _c_int),

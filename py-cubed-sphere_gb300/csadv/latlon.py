@@ -39,10 +39,31 @@ class latlon_grid:
 
 def ll2cs(cs_grid, latlon_grid):
     """Panel and interior cell indices of every lat-lon point (interpolation.py:38-140), on the GPU.
-    Returns (i, j, panel), uint32 arrays shaped like the lat-lon grid."""
+    Returns (i, j, panel), uint32 arrays shaped like the lat-lon grid.
+
+    As the reference does, the indices are kept in ``griddir + cs_grid.name + "_ll2cs.nc"``: read
+    from there when that file exists (and matches the lat-lon grid's shape), else computed and
+    written there.  The file is used only when the grid directory exists (the reference's driver
+    creates it; ``python -m csadv`` does too), so library calls elsewhere leave no files."""
+    import os
+    from . import gridfile
     if getattr(cs_grid, "projection", "gnomonic_equiangular") != "gnomonic_equiangular":
         print("ERROR: invalid grid transformation.")
         raise SystemExit(1)
+    name = getattr(cs_grid, "name", None)
+    path = os.path.join(gridfile.griddir, name + "_ll2cs.nc") if name else None
+    use_file = path is not None and os.path.isdir(gridfile.griddir)
+    if use_file and os.path.isfile(path):
+        i, j, p = gridfile.load_ll2cs(path)
+        if i.shape == np.shape(latlon_grid.X):
+            return i, j, p
+    i, j, p = _ll2cs_gpu(cs_grid, latlon_grid)
+    if use_file:
+        gridfile.ll2cs_netcdf(i, j, p, cs_grid, path)
+    return i, j, p
+
+
+def _ll2cs_gpu(cs_grid, latlon_grid):
     X = np.ascontiguousarray(latlon_grid.X, dtype=np.float64)
     Y = np.ascontiguousarray(latlon_grid.Y, dtype=np.float64)
     Z = np.ascontiguousarray(latlon_grid.Z, dtype=np.float64)

@@ -122,6 +122,40 @@ __global__ void k_grid_points(Dims d, const double *__restrict__ xs, int nx, con
     }
 }
 
+// The arrays of the reference's grid file (plot.py:522-660, read back by cs_datastruct.py:45-195)
+// for one family of points over the axes (xs, ys): P[i][j][panel][5] = X, Y, Z, lon, lat of the
+// point (the arithmetic of k_grid_points), EX and EY its tangent vectors d/dx and d/dy in the same
+// layout (X, Y, Z; their lon, lat entries stay 0, as the reference leaves them).  Any output may
+// be null.
+__global__ void k_grid_file(const double *__restrict__ xs, int nx, const double *__restrict__ ys, int ny, double *P,
+                            double *EX, double *EY) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tid >= (long long)NFACE * nx * ny) return;
+    const int p = (int)(tid % NFACE);
+    const long long ij = tid / NFACE;
+    const double x = xs[ij / ny], y = ys[ij % ny];
+    const long long o = tid * 5;
+    if (P) {
+        const double tx = tan(x), ty = tan(y);
+        const double invD = 1.0 / sqrt(1.0 + tx * tx + ty * ty);
+        double X, Y, Z;
+        panel_xyz(p, invD, invD * tx, invD * ty, X, Y, Z);
+        P[o + 0] = X;
+        P[o + 1] = Y;
+        P[o + 2] = Z;
+        P[o + 3] = atan2(Y, X);
+        P[o + 4] = atan2(Z, hypot(X, Y));
+    }
+    if (EX || EY) {
+        double ex[3], ey[3];
+        tangents(p, x, y, ex, ey);
+        for (int c = 0; c < 5; ++c) {
+            if (EX) EX[o + c] = c < 3 ? ex[c] : 0.0;
+            if (EY) EY[o + c] = c < 3 ? ey[c] : 0.0;
+        }
+    }
+}
+
 // sum of g_pc^2 over the interior of all panels (discrete_operators.py:99), fixed order
 __global__ void k_sum_g2(Dims d, const double *__restrict__ g, double *out) {
     __shared__ double red[1024];
@@ -343,3 +377,36 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
 }
 
 }  // namespace csadv
+
+using namespace csadv;
+
+extern "C" int csadv_grid_points(int N, int kind, double *P, double *EX, double *EY, void *stream) {
+    if (N < 1 || kind < 0 || kind > 3 || (!P && !EX && !EY)) return CSADV_ERR_ARG;
+    std::vector<double> xc, xe;
+    double dx;
+    angular_axes(N, xc, xe, dx);
+    // po: (x edges, y edges), pc: (centres, centres), pu: (x edges, centres), pv: (centres, y edges)
+    const std::vector<double> &xs = kind == 0 || kind == 2 ? xe : xc;
+    const std::vector<double> &ys = kind == 0 || kind == 3 ? xe : xc;
+    const int nx = (int)xs.size(), ny = (int)ys.size();
+    const size_t bytes = (size_t)nx * ny * NFACE * 5 * sizeof(double);
+    cudaStream_t st = (cudaStream_t)stream;
+    DevArray ax, ay, op, oex, oey;
+    int rc = dev_in(xs.data(), nx * sizeof(double), st, ax);
+    if (!rc) rc = dev_in(ys.data(), ny * sizeof(double), st, ay);
+    if (!rc && P) rc = dev_out(P, bytes, st, op);
+    if (!rc && EX) rc = dev_out(EX, bytes, st, oex);
+    if (!rc && EY) rc = dev_out(EY, bytes, st, oey);
+    if (!rc) {
+        const long long tot = (long long)NFACE * nx * ny;
+        k_grid_file<<<ceil_div(tot, 128), 128, 0, st>>>((const double *)ax.dev, nx, (const double *)ay.dev, ny,
+                                                         (double *)op.dev, (double *)oex.dev, (double *)oey.dev);
+        if (cudaGetLastError() != cudaSuccess) rc = CSADV_ERR_CUDA;
+    }
+    if (!rc && P) rc = dev_back(P, bytes, st, op);
+    if (!rc && EX) rc = dev_back(EX, bytes, st, oex);
+    if (!rc && EY) rc = dev_back(EY, bytes, st, oey);
+    for (DevArray *a : {&ax, &ay, &op, &oex, &oey}) dev_free(*a, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = CSADV_ERR_CUDA;
+    return rc;
+}

@@ -225,4 +225,41 @@ template <class real>
 int diag_errors(const Grid &g, const real *Q, int ic, int vf, const IcParams &prm, double t, double *dev_tmp,
                 double out[3], cudaStream_t st);
 
+// device address of a host array: page-locked memory in place, else a stream-ordered copy
+struct DevArray {
+    void *dev = nullptr;
+    bool owned = false;
+};
+inline int dev_in(const void *host, size_t bytes, cudaStream_t st, DevArray &a) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+        a.dev = at.devicePointer;
+        return CSADV_OK;
+    }
+    (void)cudaGetLastError();
+    CSADV_CUDA(cudaMallocAsync(&a.dev, bytes, st));
+    a.owned = true;
+    CSADV_CUDA(cudaMemcpyAsync(a.dev, host, bytes, cudaMemcpyHostToDevice, st));
+    return CSADV_OK;
+}
+inline int dev_out(void *host, size_t bytes, cudaStream_t st, DevArray &a) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+        a.dev = at.devicePointer;
+        return CSADV_OK;
+    }
+    (void)cudaGetLastError();
+    CSADV_CUDA(cudaMallocAsync(&a.dev, bytes, st));
+    a.owned = true;
+    return CSADV_OK;
+}
+inline int dev_back(void *host, size_t bytes, cudaStream_t st, DevArray &a) {
+    if (a.owned) CSADV_CUDA(cudaMemcpyAsync(host, a.dev, bytes, cudaMemcpyDeviceToHost, st));
+    return CSADV_OK;
+}
+inline void dev_free(DevArray &a, cudaStream_t st) {
+    if (a.owned && a.dev) cudaFreeAsync(a.dev, st);
+    a.dev = nullptr;
+}
+
 }  // namespace csadv

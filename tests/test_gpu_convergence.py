@@ -51,15 +51,22 @@ def test_convergence_study_matches_oracle_and_converges(tmp_path):
     assert np.all(rates["l2"] > 1.0)
 
 
-def test_module_entry_point_runs_the_par_files(tmp_path):
+def test_module_entry_point_runs_the_par_files(tmp_path, monkeypatch):
     from csadv import __main__ as entry
-    from csadv import advection
+    from csadv import advection, gridfile
     pardir = write_par(tmp_path, N=16, tc=1, dt=0.05, Tf=0.5)
-    advection.output_dir = str(tmp_path / "graphs")
+    monkeypatch.setattr(advection, "output_dir", str(tmp_path / "graphs"))
+    monkeypatch.setattr(gridfile, "griddir", str(tmp_path / "grid"))
+    monkeypatch.setattr(gridfile, "datadir", str(tmp_path / "data"))
     linf, l1, l2 = entry.main([pardir])
     # the reference plots Q on its 720 x 1440 lat-lon grid at steps 0, 2, ..., 10: written as .npy
     outs = sorted(os.listdir(advection.output_dir))
     assert len(outs) == 6 and np.load(os.path.join(advection.output_dir, outs[0])).shape == (1440, 720)
+    # and, as main.py and ll2cs do, the grid file and the lat-lon index file (netCDF)
+    g16 = gridfile.load_grid(str(tmp_path / "grid" / "gnomonic_equiangular_cs_16.nc"))
+    assert g16.N == 16 and g16.pc.lon.shape == (24, 24, 6)
+    i, j, p = gridfile.load_ll2cs(str(tmp_path / "grid" / "gnomonic_equiangular_cs_16_ll2cs.nc"))
+    assert i.shape == (1440, 720) and int(p.max()) == 5 and int(i.max()) <= 15
     g = CubedSphere(16)
     ref = solver.adv_sphere(solver.Simulation(g, 0.05, 0.5, 2, 1, 3, 1, 3, 3, 2, 3))
     for a, b in zip((linf, l1, l2), ref):
