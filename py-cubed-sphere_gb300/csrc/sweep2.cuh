@@ -712,19 +712,40 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 2) k_sweep2(const SweepSolve *_
             }
             __syncthreads();
             if (last) {
+                // fixed order: each thread sums items tid, tid + 256, ...; a warp butterfly (the
+                // same bits in every lane); the 8 warp sums in warp order.  Tracers two at a time
+                // (their partials read together), up to 32 per barrier.
                 __threadfence();
-                for (int tr = 0; tr < T; ++tr) {
-                    double a = 0.0;
-                    const volatile double *pp = S.partials + (long long)tr * nitems;
-                    for (int b = tid; b < nitems; b += SWEEP_THREADS) a += pp[b];
-                    red[tid] = a;
-                    __syncthreads();
-                    for (int s = SWEEP_THREADS / 2; s > 0; s >>= 1) {
-                        if (tid < s) red[tid] += red[tid + s];
-                        __syncthreads();
+                constexpr int NW = SWEEP_THREADS / 32, TB = SWEEP_THREADS / NW;
+                const int lane_id = tid & 31, warp = tid >> 5;
+                for (int t0 = 0; t0 < T; t0 += TB) {
+                    const int nt = T - t0 < TB ? T - t0 : TB;
+                    for (int k = 0; k < nt; k += 2) {
+                        const bool two = k + 1 < nt;
+                        const double *p0 = S.partials + (long long)(t0 + k) * nitems, *p1 = p0 + nitems;
+                        double a0 = 0.0, a1 = 0.0;
+                        for (int b = tid; b < nitems; b += SWEEP_THREADS) {
+                            a0 = __dadd_rn(a0, __ldcg(p0 + b));
+                            if (two) a1 = __dadd_rn(a1, __ldcg(p1 + b));
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            a0 = __dadd_rn(a0, __shfl_xor_sync(0xffffffffu, a0, o));
+                            a1 = __dadd_rn(a1, __shfl_xor_sync(0xffffffffu, a1, o));
+                        }
+                        if (lane_id == 0) {
+                            red[k * NW + warp] = a0;
+                            if (two) red[(k + 1) * NW + warp] = a1;
+                        }
                     }
-                    if (tid == 0)
-                        S.corr_out[tr] = S.mass_target ? (S.mass_target[tr] - red[0]) / S.a2 : S.dt * red[0] / S.a2;
+                    __syncthreads();
+                    if (tid < nt) {
+                        double sum = 0.0;
+#pragma unroll
+                        for (int w = 0; w < NW; ++w) sum = __dadd_rn(sum, red[tid * NW + w]);
+                        const int tr = t0 + tid;
+                        S.corr_out[tr] = S.mass_target ? (S.mass_target[tr] - sum) / S.a2 : S.dt * sum / S.a2;
+                    }
                     __syncthreads();
                 }
                 if (tid == 0) *S.counter = 0u;
