@@ -286,10 +286,7 @@ int run_step(csadv_plan *pl, int kind, cudaStream_t st) {
         if (rc) return rc;
     }
     pl->stats.steps += 1;
-    if (pl->f.on) {
-        pl->f.settled = false;
-        if (pl->f.defer && pl->f.sweep) pl->f.defer_pending = true;
-    }
+    if (pl->f.on) pl->f.settled = false;
     if (pl->prof) {
         CSADV_CUDA(cudaEventSynchronize(pl->pev[1]));
         float ms = 0.f;
@@ -361,8 +358,6 @@ static int tracer_upload(csadv_plan *pl, int tracer, double *src, int layout, cu
     FusedState &f = pl->f;
     IoLazy<real> x;
     if (f.on && pl->opt.mf == MF_PR) {
-        const int rc = fused_finalize(pl->opt, f, pl->cur, st);  // the other tracers' corrections
-        if (rc) return rc;
         x.corr = f.corr[pl->cur] + tracer;
         if (f.mass_target) {
             x.g = (const real *)f.g_pc;
@@ -378,8 +373,6 @@ static int tracer_download(csadv_plan *pl, int tracer, double *dst, int layout, 
     FusedState &f = pl->f;
     IoLazy<real> x;
     if (f.on && pl->opt.mf == MF_PR && !f.settled) {
-        const int rc = fused_finalize(pl->opt, f, pl->cur, st);
-        if (rc) return rc;
         x.g = (const real *)f.g_pc;
         x.corr = f.corr[pl->cur] + tracer;
     }
@@ -723,8 +716,6 @@ int csadv_mass_target(csadv_plan *pl, int tracer, double *get, const double *set
     if (!pl || tracer < 0 || tracer >= pl->T) return CSADV_ERR_ARG;
     if (!pl->f.on || !pl->f.mass_target) return CSADV_ERR_UNSUPPORTED;
     cudaStream_t st = S(stream);
-    // pending sums use the target in force when the step ran
-    if (int rc = fused_finalize(pl->opt, pl->f, pl->cur, st)) return rc;
     if (get) {
         CSADV_CUDA(cudaMemcpyAsync(get, pl->f.mass_target + tracer, sizeof(double), cudaMemcpyDeviceToHost, st));
         CSADV_CUDA(cudaStreamSynchronize(st));

@@ -217,7 +217,6 @@ int batch_run_step(csadv_batch *b, int kind, cudaStream_t st) {
         pl->cur = 1 - pl->cur;
         pl->k += 1;
         pl->f.settled = false;
-        if (pl->f.defer) pl->f.defer_pending = true;
         pl->f.rec_ready = false;  // a batch step makes no records for the plan's next step
         pl->stats.steps += 1;
     }

@@ -79,9 +79,7 @@ int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &
     const Dims d = g.d;
     if (f.sweep && f.inline_ghosts) {  // the step kernel kept its ghost cells on chip: fill the input's
         const bool pr = o.mf == MF_PR;
-        int rc = fused_finalize(o, f, cur, st);  // corr[1 - cur], if its sums were deferred
-        if (rc) return rc;
-        rc = o.precision == 64
+        int rc = o.precision == 64
                      ? launch_halo_dg_tracers<double>((double *)f.Qbuf[1 - cur], T, g, pr ? f.corr[1 - cur] : nullptr,
                                                       (const double *)f.g_pc, st)
                      : launch_halo_dg_tracers<float>((float *)f.Qbuf[1 - cur], T, g, pr ? f.corr[1 - cur] : nullptr,
@@ -114,9 +112,6 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
         maxb = maxb > NFACE * tmp.ntiles ? maxb : NFACE * tmp.ntiles;
     }
     f.partials = mem.alloc<double>((long long)T * maxb);
-    f.part[0] = f.partials;
-    f.part[1] = mem.alloc<double>((long long)T * maxb);
-    f.pend = mem.alloc<int2>(2);
     f.counter = mem.alloc<unsigned int>(1);
     f.ua = mem.alloc<char>(d.field * es);
     f.va = mem.alloc<char>(d.field * es);
@@ -178,7 +173,6 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     CSADV_CUDA(cudaMemsetAsync(f.Qbuf[1], 0, (size_t)T * d.field * es, st));
     for (int b = 0; b < 2; ++b) CSADV_CUDA(cudaMemsetAsync(f.corr[b], 0, T * sizeof(double), st));
     CSADV_CUDA(cudaMemsetAsync(f.counter, 0, sizeof(unsigned int), st));
-    CSADV_CUDA(cudaMemsetAsync(f.pend, 0, 2 * sizeof(int2), st));
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -239,10 +233,6 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
     if (!f.sweep) return CSADV_OK;
     f.scfg = tile - FUSED_NTILE_CFG;
     const bool pr = o.mf == MF_PR;
-    // the FP32 step kernel leaves its MF-PR sums to the launch that reads its output (whose CTAs
-    // form them while their tile loads are in flight) when no ghost-cell kernel needs the
-    // correction in between
-    f.defer = o.precision == 32 && pr && f.inline_ghosts;
     SweepSolve h[2];
     for (int b = 0; b < 2; ++b) {
         SweepSolve &s = h[b];
@@ -259,12 +249,8 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.Qout = f.Qbuf[1 - b];
         s.corr_in = pr ? f.corr[b] : nullptr;
         s.corr_out = pr ? f.corr[1 - b] : nullptr;
-        s.partials = f.part[1 - b];
+        s.partials = f.partials;
         s.counter = f.counter;
-        s.part_in = f.part[b];
-        s.pend_in = f.pend + b;
-        s.pend_out = f.pend + (1 - b);
-        s.lazy = f.defer ? 1 : 0;
         s.erx = f.rec_x(b);
         s.ery = f.rec_y(b);
         s.crx = f.crx;
@@ -292,10 +278,6 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
 int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
     if (f.sweep && f.inline_ghosts) return CSADV_OK;  // the step kernel evaluates them itself
     const bool pr = o.mf == MF_PR;
-    if (pr) {
-        const int rc = fused_finalize(o, f, cur, st);
-        if (rc) return rc;
-    }
     if (o.precision == 64)
         return launch_halo_dg_tracers<double>((double *)f.Qbuf[cur], T, g, pr ? f.corr[cur] : nullptr,
                                               (const double *)f.g_pc, st);
@@ -315,12 +297,7 @@ int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &
         if (rc) return rc;
         if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
         cur = 1 - cur;
-        if (f.defer) f.defer_pending = true;
         return CSADV_OK;
-    }
-    {  // the tile kernel reads corr[cur] directly
-        const int rc = fused_finalize(o, f, cur, st);
-        if (rc) return rc;
     }
     FusedArgs a{};
     a.d = g.d;
@@ -399,24 +376,8 @@ int fused_anchor_mass(const Options &o, const Grid &g, FusedState &f, int cur, i
     return CSADV_OK;
 }
 
-int fused_finalize(const Options &o, FusedState &f, int cur, cudaStream_t st) {
-    if (!f.defer_pending || o.mf != MF_PR) return CSADV_OK;  // (the descriptors of the sweep remain valid)
-    // both fields: the other one's sums were used by the last step but stay pending in its
-    // record, and its ghost cells (full-layout read-out) need its correction too
-    for (int b : {cur, 1 - cur}) {
-        const int rc = sweep_finalize_launch(f.dsolve + b, st);
-        if (rc) return rc;
-    }
-    f.defer_pending = false;
-    return CSADV_OK;
-}
-
 int fused_materialize(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
     if (o.mf != MF_PR) return CSADV_OK;
-    {
-        const int rc = fused_finalize(o, f, cur, st);
-        if (rc) return rc;
-    }
     const Dims d = g.d;
     dim3 grid(ceil_div((long long)NFACE * d.N * d.N, 256), T);
     if (o.precision == 64)

@@ -127,11 +127,7 @@ struct FusedState {
     int tile = 1;               // 0-3: k_fused (FUSED_TILES), 4-7: k_sweep (SWEEP_TILES[tile - 4])
     void *Qbuf[2] = {nullptr, nullptr};
     double *corr[2] = {nullptr, nullptr};  // [T] pending MF-PR correction of Qbuf[b]
-    double *partials = nullptr; // [T][max blocks] (= part[0])
-    double *part[2] = {nullptr, nullptr};  // the FP32 step kernel's partials, by the parity of the field they sum
-    int2 *pend = nullptr;       // [2] deferred MF-PR sums of Qbuf[b]: {1, items} while pending
-    bool defer = false;         // the FP32 step kernel defers its MF-PR sums (inline ghosts, MF-PR)
-    bool defer_pending = false; // host record: a step that may have deferred its sums ran since the last finalize
+    double *partials = nullptr; // [T][max blocks]
     unsigned int *counter = nullptr;
     void *ua = nullptr, *va = nullptr;     // departure-point winds in the state's precision
     uint32_t *upos = nullptr, *vpos = nullptr;  // upwind flags (1 bit per edge)
@@ -198,10 +194,6 @@ int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &
 // FP32 form with MF-PR: record sum(Q g) of tracer t of Qbuf[cur] (no pending correction) as the
 // mass the step's correction restores
 int fused_anchor_mass(const Options &o, const Grid &g, FusedState &f, int cur, int t, cudaStream_t st);
-// form the deferred MF-PR corrections of both fields into corr[] (no-op when none are pending)
-int fused_finalize(const Options &o, FusedState &f, int cur, cudaStream_t st);
-// the finalize kernel (sweep_f32.cu): one block, the descriptor of the launch that reads the field
-int sweep_finalize_launch(const SweepSolve *dsolve, cudaStream_t st);
 // apply and clear the pending MF-PR correction of Qbuf[cur]
 int fused_materialize(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
 template <class real> int fused_launch(const struct FusedArgs &a, int recon, int tile, cudaStream_t st);

@@ -414,82 +414,6 @@ struct Marcher {
     }
 };
 
-// ------------------------------------------------------------------ MF-PR sums
-// The sum of the n partials of one tracer.  For n <= LAZY_ITEMS (the solves whose sums a launch may
-// leave to the next) one order is used by every consumer (the next step's CTAs, a launch's last
-// CTA, the finalize kernel), so that the correction has the same bits whichever forms it: one warp,
-// lane l adding items l, l + 32, ... in turn (all loaded at once), then a xor butterfly (the same
-// bits in every lane).  Larger solves are summed only by their launch's last CTA, with all of its
-// threads.
-constexpr int LAZY_ITEMS = 320;  // 10 items per lane
-__device__ __forceinline__ double psum_warp(const double *__restrict__ p, int n, int lane) {
-    constexpr int H = LAZY_ITEMS / 64;  // loads per round (two rounds: fewer registers held)
-    double a = 0.0;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        double v[H];
-#pragma unroll
-        for (int k = 0; k < H; ++k) {
-            const int b = lane + 32 * (h * H + k);
-            v[k] = b < n ? __ldcg(p + b) : 0.0;
-        }
-#pragma unroll
-        for (int k = 0; k < H; ++k) a = __dadd_rn(a, v[k]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a = __dadd_rn(a, __shfl_xor_sync(0xffffffffu, a, o));
-    return a;
-}
-// the correction from the sum: dt m0 / a2 (discrete_operators.py:98-101), or (FP32 mass anchor)
-// the one that restores the recorded mass
-__device__ __forceinline__ double psum_corr(const SweepSolve &S, int tr, double sum) {
-    return S.mass_target ? (S.mass_target[tr] - sum) / S.a2 : S.dt * sum / S.a2;
-}
-// every tracer's correction from partials[T][n] by one block of SWEEP_THREADS threads -> corr
-__device__ __forceinline__ void psum_all(const SweepSolve &S, const double *__restrict__ part, int n, double *corr,
-                                         double *red) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, T = S.T;
-    constexpr int NW = SWEEP_THREADS / 32, TB = SWEEP_THREADS / NW;
-    if (n <= LAZY_ITEMS) {  // a tracer per warp
-        for (int tr = warp; tr < T; tr += NW) {
-            const double a = psum_warp(part + (long long)tr * n, n, lane);
-            if (lane == 0) corr[tr] = psum_corr(S, tr, a);
-        }
-        return;
-    }
-    // each thread sums items tid, tid + 256, ...; a warp butterfly; the 8 warp sums in warp order;
-    // tracers two at a time (their partials read together), up to 32 per barrier
-    for (int t0 = 0; t0 < T; t0 += TB) {
-        const int nt = T - t0 < TB ? T - t0 : TB;
-        for (int k = 0; k < nt; k += 2) {
-            const bool two = k + 1 < nt;
-            const double *p0 = part + (long long)(t0 + k) * n, *p1 = p0 + n;
-            double a0 = 0.0, a1 = 0.0;
-            for (int b = tid; b < n; b += SWEEP_THREADS) {
-                a0 = __dadd_rn(a0, __ldcg(p0 + b));
-                if (two) a1 = __dadd_rn(a1, __ldcg(p1 + b));
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                a0 = __dadd_rn(a0, __shfl_xor_sync(0xffffffffu, a0, o));
-                a1 = __dadd_rn(a1, __shfl_xor_sync(0xffffffffu, a1, o));
-            }
-            if (lane == 0) {
-                red[k * NW + warp] = a0;
-                if (two) red[(k + 1) * NW + warp] = a1;
-            }
-        }
-        __syncthreads();
-        if (tid < nt) {
-            double sum = 0.0;
-#pragma unroll
-            for (int w = 0; w < NW; ++w) sum = __dadd_rn(sum, red[tid * NW + w]);
-            corr[t0 + tid] = psum_corr(S, t0 + tid, sum);
-        }
-        __syncthreads();
-    }
-}
-
 // ------------------------------------------------------------------ one tile, one or two tracers
 // Phases as in k_sweep: P0 Q (+ halo) -> shared; P1 first-pass x- and y-lines -> Qx, Qy;
 // P2 y-lines of Qx -> dY; P3 x-lines of Qy -> div, update, MF-PR partial(s).  Every phase has
@@ -515,9 +439,8 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
 
     // the pending MF-PR corrections of the pair, rounded to FP32 once per CTA (GB300 converts from
     // FP64 at the FP64 rate) and shared through shared memory
-    // (read, or with deferred sums formed by warps 0 and 1 from the previous launch's partials,
-    // while the first batch of the tile load is in flight; see P0)
     float *scorr = (float *)(red + SWEEP_THREADS - 2);
+    if (tid < NL) scorr[tid] = hc ? (float)S.corr_in[tr + tid] : 0.f;
     // The first-pass lines read the edge and cell records of the tile from global memory, one to
     // two cells ahead of their use; after the records have left L2 (the first pair of a step)
     // that is not far enough to hide a DRAM access, so every thread first asks L2 for a few
@@ -551,22 +474,23 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
             asm volatile("prefetch.global.L2 [%0];" ::"l"(ad));
         }
     }
-    // (shared memory is free: the previous pass ended with a barrier)
+    __syncthreads();
 
     // P0: Q on the tile + 3 halo cells; interior cells with the pending MF-PR correction.  Warp w
     // takes rows w, w + 8, ...; all loads of a thread are issued before its first store.
     {
         const float *Qt[2];
-        float corr[2] = {0.f, 0.f};
+        float corr[2];
 #pragma unroll
-        for (int l = 0; l < NL; ++l) Qt[l] = (const float *)S.Qin + (long long)(tr + l) * d.field + pofs;
+        for (int l = 0; l < NL; ++l) {
+            Qt[l] = (const float *)S.Qin + (long long)(tr + l) * d.field + pofs;
+            corr[l] = scorr[l];
+        }
         // interior cells, and ghost cells as the ghost-cell kernel filled them (or, with inline
-        // ghost cells, left for the evaluation below); the same number of batches in every warp
+        // ghost cells, left for the evaluation below)
         const bool inl = S.lag_w != nullptr;
         constexpr int RR = 4, CC = (SWEEP_TMAX + 6 + 31) / 32;  // cells per batch: RR x CC
-        const int nbatch = (ni + 6 + RR * NWARP - 1) / (RR * NWARP);
-        for (int it = 0; it < nbatch; ++it) {
-            const int r0 = warp + it * RR * NWARP;
+        for (int r0 = warp; r0 < ni + 6; r0 += RR * NWARP) {
             float q[RR][CC][NL], g[RR][CC];
 #pragma unroll
             for (int a = 0; a < RR; ++a) {
@@ -580,20 +504,6 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
                         g[a][b] = hc ? __ldg(gpc + (q0 - Qt[0]) + 32 * b) : 0.f;
                     }
                 }
-            }
-            if (it == 0) {  // the pair's corrections, while this batch's loads are in flight
-                const int2 pend = hc ? *S.pend_in : make_int2(0, 0);
-                if (pend.x) {  // deferred sums of the previous launch: a tracer per warp
-                    if (warp < NL) {
-                        const double a = psum_warp(S.part_in + (long long)(tr + warp) * pend.y, pend.y, lane_id);
-                        if (lane_id == 0) scorr[warp] = (float)psum_corr(S, tr + warp, a);
-                    }
-                } else if (tid < NL) {
-                    scorr[tid] = hc ? (float)S.corr_in[tr + tid] : 0.f;
-                }
-                __syncthreads();
-#pragma unroll
-                for (int l = 0; l < NL; ++l) corr[l] = scorr[l];
             }
 #pragma unroll
             for (int a = 0; a < RR; ++a) {
@@ -793,24 +703,54 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 2) k_sweep2(const SweepSolve *_
             }
         }
         if (S.mfpr) {
-            // Qout's correction: left to the launch that reads it (deferred), or formed here by the
-            // last item of the solve to finish
-            const bool lazy = S.lazy && nitems <= LAZY_ITEMS;  // the consumer sums with one warp
-            if (it.y == 0 && tid == 0) *S.pend_out = lazy ? make_int2(1, nitems) : make_int2(0, 0);
-            if (!lazy) {
-                if (tid == 0) {
-                    __threadfence();
-                    const unsigned int prev = atomicAdd(S.counter, 1u);
-                    last = prev == (unsigned int)nitems - 1u;
-                }
-                __syncthreads();
-                if (last) {
-                    __threadfence();
-                    psum_all(S, S.partials, nitems, S.corr_out, red);
-                    if (tid == 0) *S.counter = 0u;
-                }
-                __syncthreads();
+            // the last item of the solve to finish sums its partials: corr = dt m0 / a2, or (FP32
+            // mass anchor) the correction that restores the recorded mass
+            if (tid == 0) {
+                __threadfence();
+                const unsigned int prev = atomicAdd(S.counter, 1u);
+                last = prev == (unsigned int)nitems - 1u;
             }
+            __syncthreads();
+            if (last) {
+                // fixed order: each thread sums items tid, tid + 256, ...; a warp butterfly (the
+                // same bits in every lane); the 8 warp sums in warp order.  Tracers two at a time
+                // (their partials read together), up to 32 per barrier.
+                __threadfence();
+                constexpr int NW = SWEEP_THREADS / 32, TB = SWEEP_THREADS / NW;
+                const int lane_id = tid & 31, warp = tid >> 5;
+                for (int t0 = 0; t0 < T; t0 += TB) {
+                    const int nt = T - t0 < TB ? T - t0 : TB;
+                    for (int k = 0; k < nt; k += 2) {
+                        const bool two = k + 1 < nt;
+                        const double *p0 = S.partials + (long long)(t0 + k) * nitems, *p1 = p0 + nitems;
+                        double a0 = 0.0, a1 = 0.0;
+                        for (int b = tid; b < nitems; b += SWEEP_THREADS) {
+                            a0 = __dadd_rn(a0, __ldcg(p0 + b));
+                            if (two) a1 = __dadd_rn(a1, __ldcg(p1 + b));
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            a0 = __dadd_rn(a0, __shfl_xor_sync(0xffffffffu, a0, o));
+                            a1 = __dadd_rn(a1, __shfl_xor_sync(0xffffffffu, a1, o));
+                        }
+                        if (lane_id == 0) {
+                            red[k * NW + warp] = a0;
+                            if (two) red[(k + 1) * NW + warp] = a1;
+                        }
+                    }
+                    __syncthreads();
+                    if (tid < nt) {
+                        double sum = 0.0;
+#pragma unroll
+                        for (int w = 0; w < NW; ++w) sum = __dadd_rn(sum, red[tid * NW + w]);
+                        const int tr = t0 + tid;
+                        S.corr_out[tr] = S.mass_target ? (S.mass_target[tr] - sum) / S.a2 : S.dt * sum / S.a2;
+                    }
+                    __syncthreads();
+                }
+                if (tid == 0) *S.counter = 0u;
+            }
+            __syncthreads();
         }
     }
 }

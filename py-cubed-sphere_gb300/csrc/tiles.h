@@ -60,14 +60,6 @@ struct SweepSolve {
     double *corr_out;       // [T] correction of Qout (MF-PR)
     double *partials;       // [T][6 ntiles]
     unsigned int *counter;  // arrival counter (MF-PR)
-    // Deferred MF-PR sums (FP32 step kernel): a launch with `lazy` set leaves its partials in
-    // `partials` and marks Qout's correction as pending ({1, items} in *pend_out) instead of summing
-    // them in its last CTA; the launch that reads that field next (or a finalize kernel) forms the
-    // correction from them.  *pend_in describes Qin the same way; part_in holds its partials.
-    const double *part_in;
-    const int2 *pend_in;
-    int2 *pend_out;
-    int lazy;
     // edge records {departure-point wind, +-metric at the edge; the sign is the upwind flag,
     // + when the wind is >= 0}: x-edges natural (row i, column j), y-edges transposed (row j,
     // column i); per panel plane, element type vec2 of the state's precision
