@@ -17,6 +17,10 @@ namespace csadv {
 
 constexpr int RB = 256;  // reduction block
 
+// maximum that propagates NaN, as numpy.max does in the reference's compute_errors (fmax would
+// drop a NaN and report a finite Linf for a state that holds one)
+__device__ __forceinline__ double max_nan(double a, double b) { return (a > b || a != a) ? a : b; }
+
 template <class real>
 __global__ void k_init(Grid g, int ic, int vf, IcParams prm, real *Q) {
     const Dims d = g.d;
@@ -161,7 +165,7 @@ __global__ void k_err_part(Grid g, const real *__restrict__ Q, int ic, int vf, I
     __syncthreads();
     for (int s = RB / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) {
-            rmax[threadIdx.x] = fmax(rmax[threadIdx.x], rmax[threadIdx.x + s]);
+            rmax[threadIdx.x] = max_nan(rmax[threadIdx.x], rmax[threadIdx.x + s]);
             rs1[threadIdx.x] += rs1[threadIdx.x + s];
             rs2[threadIdx.x] += rs2[threadIdx.x + s];
         }
@@ -182,7 +186,7 @@ __global__ void k_reduce(const double *__restrict__ part, int np, int w, double 
         if (w == 1) {
             a += part[t];
         } else {
-            a = fmax(a, part[3 * t]);
+            a = max_nan(a, part[3 * t]);
             b += part[3 * t + 1];
             c += part[3 * t + 2];
         }
@@ -193,7 +197,7 @@ __global__ void k_reduce(const double *__restrict__ part, int np, int w, double 
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) {
-            r0[threadIdx.x] = w == 1 ? r0[threadIdx.x] + r0[threadIdx.x + s] : fmax(r0[threadIdx.x], r0[threadIdx.x + s]);
+            r0[threadIdx.x] = w == 1 ? r0[threadIdx.x] + r0[threadIdx.x + s] : max_nan(r0[threadIdx.x], r0[threadIdx.x + s]);
             r1[threadIdx.x] += r1[threadIdx.x + s];
             r2[threadIdx.x] += r2[threadIdx.x + s];
         }
