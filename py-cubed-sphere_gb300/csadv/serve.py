@@ -43,6 +43,7 @@ class Request:
     arrival: float = 0.0       # seconds after the start of the run
     alpha: float = 0.0         # solid-body rotation angle
     hills: tuple = ()          # per tracer: (lon, lat, width)
+    deadline: float = None     # most seconds it may wait for admission (None: no limit)
 
 
 @dataclasses.dataclass
@@ -58,6 +59,7 @@ class Result:
     mass_change: list          # per tracer, relative
     cell_steps: int
     state: list = None         # per tracer final interior field (keep_state=True)
+    error: str = None          # why the request failed (not admitted, or a failed solve); None if served
 
     @property
     def latency(self):
@@ -108,6 +110,8 @@ def finish(pl, req, mass0):
         errs.append(pl.errors(L.IC_HILL, t_end, ic_param=(lon, lat, w, 0.0), tracer=t) if req.wind == "solid"
                     else (float("nan"),) * 3)
         m = pl.mass(t)
+        if not (math.isfinite(m) and math.isfinite(mass0[t])):  # whatever the wind: no error norms for
+            raise L.CsadvError(L.ERR_NONFINITE, "mass")          # the deformational one
         dm.append(abs(m - mass0[t]) / abs(mass0[t]) if mass0[t] != 0 else abs(m))
     return errs, dm
 
@@ -118,7 +122,11 @@ def plane_elems(N):
 
 
 class Server:
-    """The request loop.  budget_bytes bounds the device memory of resident solves."""
+    """The request loop.  budget_bytes bounds the device memory of resident solves.
+
+    Failures stay with their request: a request whose plan cannot be made (bad size, no
+    memory), whose state turns non-finite, or that waits past its deadline gets a Result with
+    `error` set and no cell-steps; the loop carries on with the others."""
 
     def __init__(self, budget_bytes, precision=32, cfl=0.5, max_active=512, stream=None, clock=time.perf_counter,
                  keep_state=False, max_steps_per_tick=8):
@@ -164,11 +172,20 @@ class Server:
                     queue.append(pending.popleft())
                 while queue and len(active) < self.max_active:
                     req = queue[0]
+                    waited = now - (req.arrival if realtime else 0.0)
+                    if req.deadline is not None and waited > req.deadline:
+                        queue.popleft()
+                        results.append(self._failed(req, realtime, t0, "not admitted within %.3g s" % req.deadline))
+                        continue
                     need = self.estimate(req)
                     if used + need > self.budget and active:
                         break
                     queue.popleft()
-                    pl = make_plan(req, self.precision, self.cfl, self.stream)
+                    try:
+                        pl = make_plan(req, self.precision, self.cfl, self.stream)
+                    except L.CsadvError as e:
+                        results.append(self._failed(req, realtime, t0, str(e)))
+                        continue
                     nbytes = pl.stats()["device_bytes"]
                     mass0 = [pl.mass(t) for t in range(req.tracers)]
                     batch.add(pl)
@@ -193,10 +210,15 @@ class Server:
                 for key in done:
                     pl, req, _, admitted, mass0, nbytes = active.pop(key)
                     batch.remove(pl)
-                    errs, dm = finish(pl, req, mass0)  # synchronises the plan's stream
+                    try:
+                        errs, dm = finish(pl, req, mass0)  # synchronises the plan's stream
+                        failed = None
+                    except L.CsadvError as e:  # e.g. a non-finite state: this request only
+                        errs, dm, failed = [], [], str(e)
                     fin = self.clock() - t0
                     res = Result(req.rid, req.N, req.tracers, req.steps, req.arrival if realtime else 0.0, admitted,
-                                 fin, errs, dm, 6 * req.N * req.N * req.tracers * req.steps)
+                                 fin, errs, dm, 0 if failed else 6 * req.N * req.N * req.tracers * req.steps,
+                                 error=failed)
                     if self.keep_state:
                         res.state = [pl.get_tracer(t) for t in range(req.tracers)]
                     results.append(res)
@@ -207,11 +229,18 @@ class Server:
                 v[0].close()
             batch.close()
         wall = self.clock() - t0
-        lat = np.array([r.latency for r in results]) if results else np.zeros(1)
-        cs = sum(r.cell_steps for r in results)
-        summary = {"requests": len(results), "wall_s": wall, "tracer_cell_steps": cs,
+        served = [r for r in results if r.error is None]
+        lat = np.array([r.latency for r in served]) if served else np.zeros(1)
+        cs = sum(r.cell_steps for r in served)
+        summary = {"requests": len(served), "failed": len(results) - len(served), "wall_s": wall,
+                   "tracer_cell_steps": cs,
                    "throughput": cs / wall if wall > 0 else 0.0,
                    "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                    "batch_steps": steps, "peak_bytes": peak, "budget_bytes": self.budget,
-                   "max_mass_change": max((max(r.mass_change) for r in results), default=0.0)}
+                   "max_mass_change": max((max(r.mass_change) for r in served), default=0.0)}
         return results, summary
+
+    def _failed(self, req, realtime, t0, why):
+        now = self.clock() - t0
+        return Result(req.rid, req.N, req.tracers, req.steps, req.arrival if realtime else 0.0, now, now, [], [], 0,
+                      error=why)

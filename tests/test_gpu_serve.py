@@ -68,3 +68,30 @@ def test_realtime_arrivals_overlap():
     results, summary = srv.run(reqs, realtime=True, on_step=lambda s, n, used: seen.append(n))
     assert summary["requests"] == len(reqs)
     assert all(r.finished >= r.arrival for r in results)
+
+
+def test_failed_requests_stay_with_their_request():
+    # failures are injected on the host: a size the library refuses, a hill whose width is NaN
+    # (its state turns non-finite), and a deadline that cannot be met; the other requests are
+    # served with the bits they get alone
+    import dataclasses
+    import math
+    from csadv import serve
+    good = small_stream(n=6, seed=7)
+    bad_size = dataclasses.replace(good[0], rid=100, N=20000)
+    bad_nan = dataclasses.replace(good[1], rid=101, wind="solid", hills=((0.0, 0.0, math.nan),) * good[1].tracers)
+    late = dataclasses.replace(good[2], rid=102, deadline=0.0)
+    reqs = good[:3] + [bad_size, bad_nan] + good[3:] + [late]
+    srv = serve.Server(budget_bytes=1, precision=32, keep_state=True)  # one at a time: `late` must wait
+    results, summary = srv.run(reqs, realtime=False)
+    by_id = {r.rid: r for r in results}
+    assert set(by_id) == {r.rid for r in reqs}
+    assert summary["requests"] == len(good) and summary["failed"] == 3
+    assert "invalid argument" in by_id[100].error
+    assert "non-finite" in by_id[101].error and by_id[101].cell_steps == 0
+    assert "not admitted" in by_id[102].error
+    for req in good:
+        got = by_id[req.rid]
+        assert got.error is None
+        for a, b in zip(got.state, alone(req, 32)):
+            np.testing.assert_array_equal(a, b)
