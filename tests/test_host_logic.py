@@ -110,3 +110,89 @@ def test_bench_replicas_take_the_slowest_rank(tmp_path):
         got = json.load(open(tmp_path / ("rank%d.json" % r)))
         assert got["ms"] == 2.0 and got["e2e"] == 5.0
         assert abs(got["rate"] - 2 * 100 / 2e-3) < 1e-6
+
+
+class _FakePlan:
+    """Stands in for csadv.Plan in the serving loop's host logic: memory, mass and error norms
+    of a solve that takes no GPU; `nan` makes its state non-finite."""
+
+    def __init__(self, req, nan=False):
+        self.req, self.nan, self.step, self.dt, self.closed = req, nan, 0, 0.01, False
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def stats(self):
+        return {"device_bytes": 1000 * self.req.N}
+
+    def mass(self, t):
+        return float("nan") if self.nan and self.step else 1.0
+
+    def errors(self, ic, t, ic_param=None, tracer=0):
+        if self.nan:
+            raise csadv.CsadvError(csadv._lib.ERR_NONFINITE, "csadv_errors")
+        return (0.1, 0.01, 0.02)
+
+    def get_tracer(self, t):
+        return np.zeros(3)
+
+    def close(self):
+        self.closed = True
+
+
+class _FakeBatch:
+    def __init__(self, capacity):
+        self.members, self.max_members = [], 0
+
+    def add(self, pl):
+        self.members.append(pl)
+        self.max_members = max(self.max_members, len(self.members))
+
+    def remove(self, pl):
+        self.members.remove(pl)
+
+    def advance(self, k, stream=None):
+        for pl in self.members:
+            pl.step += k
+
+    def close(self):
+        pass
+
+
+def test_serving_loop_reports_failures_per_request(monkeypatch):
+    """The request loop's host logic with failures injected on the host (no GPU): a plan that
+    cannot be made, a solve whose state turns non-finite, a request that misses its admission
+    deadline.  Each failed request gets a result with `error` set; the others are served."""
+    from csadv import serve
+    made = []
+
+    def make_plan(req, precision=32, cfl=0.5, stream=None):
+        if req.N > 16384:
+            raise csadv.CsadvError(csadv._lib.ERR_ARG, "csadv_plan_create")
+        pl = _FakePlan(req, nan=req.rid == 3)
+        made.append(pl)
+        return pl
+
+    monkeypatch.setattr(serve, "make_plan", make_plan)
+    monkeypatch.setattr(serve, "Batch", _FakeBatch)
+    hill = ((0.0, 0.0, 5.0),)
+    reqs = [serve.Request(rid=i, N=16, steps=5 + i, tracers=1, wind="solid", hills=hill) for i in range(6)]
+    reqs[1].N = 20000           # refused by the library
+    reqs[5].deadline = 0.0      # cannot be admitted in time: four solves are ahead of it
+    ticks = iter(range(10 ** 6))
+    srv = serve.Server(budget_bytes=10 ** 9, precision=32, clock=lambda: float(next(ticks)), max_active=2)
+    results, summary = srv.run(reqs, realtime=False)
+    by_id = {r.rid: r for r in results}
+    assert set(by_id) == set(range(6))
+    # (without the library loaded the status has no text: check its number)
+    assert "csadv_plan_create" in by_id[1].error and "status %d" % csadv._lib.ERR_ARG in by_id[1].error
+    assert "status %d" % csadv._lib.ERR_NONFINITE in by_id[3].error and by_id[3].cell_steps == 0
+    assert "not admitted" in by_id[5].error
+    for i in (0, 2, 4):
+        assert by_id[i].error is None and by_id[i].steps == 5 + i
+        assert by_id[i].cell_steps == 6 * 16 * 16 * (5 + i)
+    assert summary["requests"] == 3 and summary["failed"] == 3
+    assert all(pl.closed for pl in made)  # every plan made (probes included) is released
