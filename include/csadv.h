@@ -109,7 +109,10 @@ int csadv_init_tracer(csadv_plan *plan, int tracer, int ic, const double *ic_par
  * cudaMallocHost, cudaHostRegister) is read or written by the device directly, in one pass over
  * the interconnect; pageable memory is staged through a device buffer.  csadv_set_tracer is
  * ordered on the stream: the array must stay unchanged until the stream has passed the call.
- * csadv_get_tracer returns when the array holds the field. */
+ * csadv_get_tracer returns when the array holds the field.  With the fused engine and MF-PR the
+ * read-out applies the tracer's pending mass-fixer correction as it reads, and the upload
+ * replaces it (and, in FP32, records the uploaded field's sum(Q g) as the mass the fixer keeps);
+ * neither touches the other tracers' pending corrections. */
 int csadv_set_tracer(csadv_plan *plan, int tracer, const double *host, int layout, void *stream);
 int csadv_get_tracer(csadv_plan *plan, int tracer, double *host, int layout, void *stream);
 
