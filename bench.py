@@ -377,7 +377,7 @@ def run_serving(torch, nreq, stream, budget_gb=120.0):
     srv = serve.Server(budget_bytes=budget_gb * 1e9, precision=32, stream=stream)
     _, summ = srv.run(reqs, realtime=True)
     offered = sum(6 * r.N * r.N * r.tracers * r.steps for r in reqs) / max(reqs[-1].arrival, 1e-9)
-    return {"requests": summ["requests"], "p50_latency_s": round(summ["p50_latency_s"], 3),
+    return {"requests": summ["requests"], "failed": summ["failed"], "p50_latency_s": round(summ["p50_latency_s"], 3),
             "p99_latency_s": round(summ["p99_latency_s"], 3), "value": round(summ["throughput"], 1),
             "unit": "tracer cell-steps/s", "wall_s": round(summ["wall_s"], 2),
             "offered_load": round(offered, 1), "peak_resident_gb": round(summ["peak_bytes"] / 1e9, 2),
