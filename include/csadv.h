@@ -73,9 +73,10 @@ typedef struct csadv_options {
     int precision; /* 64: state in float64 ("plain form"); 32: state/PPM/fluxes in float32 */
     int engine;    /* CSADV_ENGINE_* */
     int tile;      /* fused engine tile (rows x columns of cells).  Per-edge tile kernel: 1 = 16x58,
-                      2 = 32x58, 3 = 16x26, 4 = 32x26.  Line-marching kernel: 5 = 58x58, 6 = 58x26,
-                      7 = 26x58, 8 = 26x26.  0 = default: the tile csadv_tune chose for this shape,
-                      else 5 for N >= 116 and 8 below */
+                      2 = 32x58, 3 = 16x26, 4 = 32x26.  Line-marching kernel (largest tiles; the N
+                      cells of each direction are split into nearly equal tiles no larger):
+                      5 = 55x55, 6 = 55x26, 7 = 26x55, 8 = 26x26.  0 = default: the tile csadv_tune
+                      chose for this shape, else 5 for N >= 116 and 8 below */
     double wind_param[4];
 } csadv_options;
 
