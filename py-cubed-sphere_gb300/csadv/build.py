@@ -10,7 +10,9 @@ engine is compiled with contraction allowed.  Host code is compiled with
 """
 import argparse
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -43,6 +45,7 @@ UNITS = {
     "sweep_f64.cu": True,
     "noalloc.cu": False,
     "latlon.cu": False,
+    "peak.cu": True,
 }
 
 
@@ -53,19 +56,41 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
-def _sources_newer_than(target):
-    if not os.path.exists(target):
-        return True
-    t = os.path.getmtime(target)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "csadv.h"),
-                                                                 os.path.abspath(__file__)]
-    return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
+STAMP = LIB + ".sha256"
+
+
+def source_digest():
+    """SHA-256 over every source the library is built from (csrc/, the public header, this
+    script), the compiler flags, the nvcc in use and the host architecture: the library is
+    rebuilt whenever one of them differs from the build that wrote the stamp file."""
+    h = hashlib.sha256()
+    deps = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC))
+    deps += [os.path.join(ROOT, "include", "csadv.h"), os.path.abspath(__file__)]
+    for p in deps:
+        if os.path.isfile(p):
+            h.update(os.path.basename(p).encode() + b"\0")
+            with open(p, "rb") as f:
+                h.update(f.read())
+    h.update(repr((ARCH, COMMON, sorted(UNITS.items()), platform.machine())).encode())
+    try:
+        h.update(os.path.realpath(nvcc()).encode())
+    except RuntimeError:
+        pass
+    return h.hexdigest()
+
+
+def up_to_date():
+    if not (os.path.exists(LIB) and os.path.exists(STAMP)):
+        return False
+    with open(STAMP) as f:
+        return f.read().strip() == source_digest()
 
 
 def build(force=False, jobs=None, verbose=False):
     """Compile every unit and link libcsadv.so; returns the library path."""
-    if not force and not _sources_newer_than(LIB):
+    if not force and up_to_date():
         return LIB
+    digest = source_digest()
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
 
@@ -91,6 +116,8 @@ def build(force=False, jobs=None, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(digest + "\n")
     return LIB
 
 

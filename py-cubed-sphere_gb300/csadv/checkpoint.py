@@ -3,8 +3,10 @@
 ``save(plan, path)`` writes the plan's options, grid size, time step, step count, tracers
 (float64, the reference's full (N+8, N+8, 6) layout) and, for the FP32 form with the mass
 fixer, each tracer's mass target; ``load(path)`` builds a new plan from them.  The resumed
-plan continues with the same bits as the saved one would have (the tile shape, which fixes
-the order of the mass-fixer sums, is saved too).  The reference keeps no state between runs;
+plan continues with the same bits as the saved one would have: the tile shape, which fixes
+the order of the mass-fixer sums, is saved too, and so is a ghost-cell choice made with
+``Plan.set_inline_ghosts`` (the step kernel's own ghost cells and the separate ghost-cell
+launch can differ in the last bits of FP32 corner cells).  The reference keeps no state between runs;
 its grid cache (NetCDF) has no counterpart here because the grid is rebuilt on the GPU.
 """
 import ctypes
@@ -24,7 +26,8 @@ def save(plan, path):
     opts["tile"] = int(st["tile"])  # the shape in use
     data = {"options": np.array([opts[n] for n in _OPTS], dtype=np.int64),
             "wind_param": np.array(list(o.wind_param), dtype=np.float64),
-            "N": plan.N, "dt": plan.dt, "ntracers": plan.ntracers, "step": plan.step}
+            "N": plan.N, "dt": plan.dt, "ntracers": plan.ntracers, "step": plan.step,
+            "inline_ghosts": -1 if plan.inline_ghosts is None else int(plan.inline_ghosts)}
     for t in range(plan.ntracers):
         data["Q%d" % t] = plan.get_tracer(t, full=True)
     targets = []
@@ -46,6 +49,8 @@ def load(path, stream=None):
     pl = Plan(int(z["N"]), float(z["dt"]), ntracers=int(z["ntracers"]), wind_param=tuple(z["wind_param"]),
               stream=stream, **opts)
     try:
+        if "inline_ghosts" in z.files and int(z["inline_ghosts"]) >= 0:
+            pl.set_inline_ghosts(bool(int(z["inline_ghosts"])))
         for t in range(pl.ntracers):
             pl.set_tracer(z["Q%d" % t], tracer=t)
         if "mass_target" in z.files:

@@ -27,6 +27,7 @@ class Plan:
         for c in range(4):
             o.wind_param[c] = float(wind_param[c]) if c < len(wind_param) else 0.0
         self._opts = o
+        self.inline_ghosts = None  # the form's default until set_inline_ghosts is called
         h = ctypes.c_void_p()
         L.check(L.lib().csadv_plan_create(self.N, self.dt, self.ntracers, ctypes.byref(o), self.stream,
                                           ctypes.byref(h)), "csadv_plan_create")
@@ -133,6 +134,7 @@ class Plan:
 
     def set_inline_ghosts(self, enable):
         L.check(L.lib().csadv_set_inline_ghosts(self._h, int(bool(enable))), "csadv_set_inline_ghosts")
+        self.inline_ghosts = bool(enable)
 
     def stats(self):
         st = L.Stats()

@@ -13,7 +13,9 @@
 // to a kernel (on the host it is only a stand-in for the device address); its device
 // address is looked up once per device with cudaGetSymbolAddress, with that device
 // current, by the first call made on the device.  That first call should therefore come
-// before any stream capture.  Every call uses the same scratch: calls whose work overlaps
+// before any stream capture.  The remembered address belongs to the device's primary
+// context: after cudaDeviceReset it is stale, and the entry point must not be called again
+// in that process.  Every call uses the same scratch: calls whose work overlaps
 // on the GPU (different streams without ordering) race and give wrong results.  Each call
 // writes every scratch slot it reads before reading it, so nothing carries over from the
 // previous call.

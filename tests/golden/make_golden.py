@@ -2,7 +2,7 @@
 
 Usage (only where the reference tree exists; the fixtures are committed):
 
-    python tests/golden/make_golden.py [--ref /path/to/py-cubed-sphere/src]
+    python tests/golden/make_golden.py --ref /path/to/py-cubed-sphere/src
 
 It imports the unmodified reference modules through ``refharness`` (stand-ins for the
 uninstalled numexpr / netCDF4 / matplotlib, see that file) and records:
@@ -55,11 +55,10 @@ def invalid_combos():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=None)
+    ap.add_argument("--ref", required=True, help="the reference's src/ directory")
     ap.add_argument("--only", default=None, choices=("latlon",))
     args = ap.parse_args()
-    if args.ref:
-        os.environ["CSADV_REFERENCE_SRC"] = args.ref
+    os.environ["CSADV_REFERENCE_SRC"] = os.path.abspath(args.ref)
     sys.path.insert(0, HERE)
     import refharness as rh
     if args.only == "latlon":

@@ -27,7 +27,8 @@ import types
 
 import numpy as np
 
-REF_SRC = os.environ.get("CSADV_REFERENCE_SRC", "/root/reference/src")
+# the reference's src/ directory: make_golden.py --ref sets it; there is no default location
+REF_SRC = os.environ.get("CSADV_REFERENCE_SRC", "")
 
 
 def _stub_module(name):
@@ -76,8 +77,9 @@ def install():
     global _installed
     if _installed:
         return
-    if not os.path.isdir(REF_SRC):
-        raise RuntimeError("reference sources not found at %s" % REF_SRC)
+    if not REF_SRC or not os.path.isdir(REF_SRC):
+        raise RuntimeError("set CSADV_REFERENCE_SRC (or make_golden.py --ref) to the reference's src/ "
+                           "directory; not found: %r" % REF_SRC)
     sys.modules["numexpr"] = _numexpr_module()
     sys.modules["netCDF4"] = _stub_module("netCDF4")
     mpl = _stub_module("matplotlib")

@@ -1,0 +1,172 @@
+"""GPU parity of the parameterised benchmark cases and of the benchmark workload itself.
+
+Winds 101 (solid body at angle alpha, speed u0), 102 (Nair-Lauritzen case 4 with free k and
+period T) and 103 (solid body plus a divergent perturbation) and initial conditions 101
+(Gaussian hill), 102 (cosine bells) and 103 (smooth bells) are parameterised members of the
+reference's families (advection_ic.py:208-313); the CPU oracle restates them in
+oracle/cases.py.  Every test drives libcsadv through its C ABI (csadv.Plan) in FP64 and
+compares with the oracle on the same inputs at |gpu - oracle| <= 1e-12 * max|oracle|, the
+parity bar of the plain form.  The FP32 form is compared with the same FP64 oracle at
+2e-5 of the field maximum (its state is rounded to float32 every step).
+
+The known-answer test pins the new cases to the reference itself: wind 101 with
+alpha = -pi/4, u0 = 2 pi/5 and hill 101 at (pi/4, pi/6), b0 = 10 are the reference's vf = 1
+and ic = 2 (advection_ic.py:221-246, :288-292), so they must reproduce the reference's own
+40-step default run (tests/golden/run_N16.npz).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import cases, solver
+from oracle.grid import CubedSphere
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+RTOL_F32 = 2e-5
+SCHEME = (2, 2, 1, 3, 1, 3)  # PPM-CW84, RK2, AVLT, ET-DG, MT-0, MF-PR
+WINDS = {101: (-0.3, 2.0 * math.pi / 5.0, 0.0, 0.0), 102: (0.48, 5.0, 0.0, 0.0),
+         103: (math.pi / 4.0, 2.0 * math.pi / 5.0, 0.3, 0.0)}
+ICS = {101: (0.7, -0.4, 6.0, 0.0), 102: None, 103: None}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__
+    __graft_entry__.build()
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def wind_spec(vf, p):
+    if vf == 101:
+        return cases.WindSpec("solid", alpha=p[0], u0=p[1])
+    if vf == 102:
+        return cases.WindSpec("deform", k=p[0], T=p[1])
+    return cases.WindSpec("solid_div", alpha=p[0], u0=p[1], eps=p[2])
+
+
+def ic_spec(ic, p):
+    if ic == 101:
+        return cases.ICSpec("hill", lon=p[0], lat=p[1], b0=p[2])
+    return cases.ICSpec("bells" if ic == 102 else "smooth_bells")
+
+
+def oracle_sim(g, dt, vf, ic, scheme=SCHEME):
+    w, q = wind_spec(vf, WINDS[vf]), ic_spec(ic, ICS[ic])
+    it = g.interior
+    return solver.Simulation(g, dt, 5.0, 0, 0, *scheme, ic_spec=q, wind=w, q0=q(g.pc.lon[it], g.pc.lat[it]))
+
+
+def gpu_plan(N, dt, vf, precision=64, ntracers=1, scheme=SCHEME):
+    from csadv import Plan
+    recon, dp, sp, et, mt, mf = scheme
+    return Plan(N, dt, recon=recon, dp=dp, opsplit=sp, et=et, mt=mt, mf=mf, vf=vf, ntracers=ntracers,
+                precision=precision, wind_param=WINDS[vf])
+
+
+@pytest.mark.parametrize("N", [16, 48])
+@pytest.mark.parametrize("vf", [101, 102, 103])
+def test_benchmark_winds_and_ics_vs_oracle(N, vf):
+    """All three ICs as three tracers of one plan, 12 steps at CFL 0.5 (time-dependent wind: the
+    clock runs through the steps), fields, CFL, mass and errors against the oracle."""
+    nsteps = 12
+    with gpu_plan(N, -0.5, vf, ntracers=3) as pl:
+        for t, ic in enumerate(ICS):
+            pl.init_tracer(ic, ic_param=ICS[ic], tracer=t)
+        dt = pl.dt
+        m0 = [pl.mass(t) for t in range(3)]
+        pl.advance(nsteps)
+        got = [pl.get_tracer(t) for t in range(3)]
+        errs = [pl.errors(ic, nsteps * dt, ic_param=ICS[ic], tracer=t) for t, ic in enumerate(ICS)]
+        mass = [pl.mass(t) for t in range(3)]
+        cfl = pl.cfl
+    g = CubedSphere(N)
+    it = g.interior
+    for t, ic in enumerate(ICS):
+        s = oracle_sim(g, dt, vf, ic)
+        assert s.CFL == pytest.approx(cfl, rel=1e-12)
+        om0, _ = solver.mass_computation(s.Q, g, 1.0)
+        solver.run_steps(s, nsteps)
+        assert rel(got[t], s.Q[it]) <= RTOL, (vf, ic, rel(got[t], s.Q[it]))
+        qex = s.qexact(g.pc.lon[it], g.pc.lat[it], nsteps * dt)
+        np.testing.assert_allclose(errs[t], solver.compute_errors(s.Q[it], qex), rtol=1e-9)
+        om, _ = solver.mass_computation(s.Q, g, 1.0)
+        assert m0[t] == pytest.approx(om0, rel=1e-12)
+        assert mass[t] == pytest.approx(om, rel=1e-12)
+
+
+@pytest.mark.parametrize("vf", [101, 102, 103])
+def test_benchmark_cases_fp32_vs_fp64_oracle(vf):
+    """The FP32 form on the same cases: its state within 2e-5 of the FP64 oracle's field maximum,
+    and its errors against the analytic solution stated beside the oracle's."""
+    N, nsteps = 48, 12
+    with gpu_plan(N, -0.5, vf, precision=32, ntracers=3) as pl:
+        for t, ic in enumerate(ICS):
+            pl.init_tracer(ic, ic_param=ICS[ic], tracer=t)
+        dt = pl.dt
+        pl.advance(nsteps)
+        got = [pl.get_tracer(t) for t in range(3)]
+        errs = [pl.errors(ic, nsteps * dt, ic_param=ICS[ic], tracer=t) for t, ic in enumerate(ICS)]
+    g = CubedSphere(N)
+    it = g.interior
+    for t, ic in enumerate(ICS):
+        s = oracle_sim(g, dt, vf, ic)
+        solver.run_steps(s, nsteps)
+        d = rel(got[t], s.Q[it])
+        qex = s.qexact(g.pc.lon[it], g.pc.lat[it], nsteps * dt)
+        ref = solver.compute_errors(s.Q[it], qex)
+        print("vf=%d ic=%d FP32 vs FP64 oracle %.2e; L2 vs exact FP32 %.6e FP64 %.6e" % (vf, ic, d, errs[t][2], ref[2]))
+        assert d <= RTOL_F32, (vf, ic, d)
+        assert abs(errs[t][2] - ref[2]) <= 0.01 * ref[2] + 1e-7
+
+
+def test_parameterised_cases_reproduce_the_reference_default_run(golden_dir):
+    """Wind 101 (alpha = -pi/4, u0 = 2 pi/5) and hill 101 at (pi/4, pi/6), b0 = 10 on the GPU
+    reproduce the reference's default run (PPM-PL07, RK1, AVLT, ET-DG, MT-0, MF-PR; vf = 1,
+    ic = 2): per-step errors against the exact rotated hill, mass, CFL and final field."""
+    from csadv import Plan
+    z = np.load(os.path.join(golden_dir, "run_N16.npz"))
+    cfg = z["default_cfg"]
+    dt = float(cfg[0])
+    recon, dp, sp, et, mt, mf = (int(x) for x in cfg[3:9])
+    nsteps = int(cfg[9])
+    wp = (-math.pi / 4.0, 2.0 * math.pi / 5.0, 0.0, 0.0)
+    ip = (math.pi / 4.0, math.pi / 6.0, 10.0, 0.0)
+    with Plan(int(z["N"]), dt, recon=recon, dp=dp, opsplit=sp, et=et, mt=mt, mf=mf, vf=101, wind_param=wp) as pl:
+        pl.init_tracer(101, ic_param=ip)
+        assert pl.cfl == pytest.approx(float(z["default_CFL"]), rel=1e-12)
+        for k in range(1, nsteps + 1):
+            pl.time_step(k)
+            np.testing.assert_allclose(pl.errors(101, k * dt, ic_param=ip), z["default_errors"][k - 1], rtol=1e-10)
+            np.testing.assert_allclose(pl.mass(), z["default_mass"][k - 1][0], rtol=1e-12)
+            pl.update_winds(k * dt)
+        assert rel(pl.get_tracer(), z["default_Q"]) <= RTOL
+
+
+def test_bench_workload_vs_oracle():
+    """The benchmark workload exactly: N = 384, deformational wind 102 with k = 0.48, T = 5,
+    cosine bells (102) and smooth bells (103) as two tracers, PPM-CW84 RK2 AVLT ET-DG MT-0
+    MF-PR, dt from CFL 0.5; three steps in FP64 (1e-12) and in FP32 (2e-5) against the oracle."""
+    N, nsteps, vf = 384, 3, 102
+    out = {}
+    for prec in (64, 32):
+        with gpu_plan(N, -0.5, vf, precision=prec, ntracers=2) as pl:
+            pl.init_tracer(102, tracer=0)
+            pl.init_tracer(103, tracer=1)
+            dt, cfl = pl.dt, pl.cfl
+            pl.advance(nsteps)
+            out[prec] = [pl.get_tracer(t) for t in range(2)]
+    g = CubedSphere(N)
+    it = g.interior
+    for t, ic in enumerate((102, 103)):
+        s = oracle_sim(g, dt, vf, ic)
+        assert s.CFL == pytest.approx(cfl, rel=1e-12)
+        solver.run_steps(s, nsteps)
+        assert rel(out[64][t], s.Q[it]) <= RTOL, (ic, rel(out[64][t], s.Q[it]))
+        assert rel(out[32][t], s.Q[it]) <= RTOL_F32, (ic, rel(out[32][t], s.Q[it]))

@@ -317,13 +317,19 @@ def test_pipelined_wind_records_follow_every_call_pattern():
             np.testing.assert_array_equal(b.get_tracer(t), ref[t])
 
 
-@pytest.mark.parametrize("prec,vf,wp", [(64, 2, (0, 0, 0, 0)), (32, 102, (0.48, 5.0, 0, 0)), (32, 101, (0.7, 1.25, 0, 0))])
-def test_checkpoint_resume_gives_the_same_bits(tmp_path, prec, vf, wp):
+@pytest.mark.parametrize("prec,vf,wp,inline", [(64, 2, (0, 0, 0, 0), None), (32, 102, (0.48, 5.0, 0, 0), None),
+                                               (32, 101, (0.7, 1.25, 0, 0), None), (32, 102, (0.48, 5.0, 0, 0), False),
+                                               (64, 102, (0.48, 5.0, 0, 0), True)])
+def test_checkpoint_resume_gives_the_same_bits(tmp_path, prec, vf, wp, inline):
     """A run saved after k steps and resumed in a new plan continues with the same bits as the
-    run that was not interrupted (time-dependent and static winds, FP64 and FP32 forms)."""
+    run that was not interrupted (time-dependent and static winds, FP64 and FP32 forms, and
+    ghost cells evaluated inside the step kernel or by the separate launch when that is not the
+    form's default: the choice is saved with the plan)."""
     from csadv import Plan, checkpoint
     kw = dict(recon=2, dp=2, opsplit=1, et=3, mt=1, mf=3, vf=vf, wind_param=wp, ntracers=3, precision=prec)
     with Plan(48, -0.5, **kw) as a:
+        if inline is not None:
+            a.set_inline_ghosts(inline)
         for t in range(3):
             a.init_tracer(101 + t, ic_param=(0.3, 0.2, 5.0, 0.0) if t == 0 else None, tracer=t)
         a.advance(5)

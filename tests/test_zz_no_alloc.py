@@ -1,5 +1,5 @@
 """The allocation-free mass-fixer entry point (csadv_mass_fixer_noalloc) against the plan-based
-path, through the C ABI, on two calls in a row.
+path, through the C ABI, on two calls in a row and a third in place.
 
 Callers that cannot call cudaMalloc (a service whose device memory is fully committed to
 resident solves, or a program whose device memory belongs to another runtime's pool) use
@@ -61,6 +61,13 @@ def test_no_alloc_mass_fixer_matches_plan_divergence_twice():
             out = d_out.cpu().numpy()
             assert rel(out[4:N + 4, 4:N + 4], div_ref) <= RTOL
             np.testing.assert_array_equal(out[:4], full[:4])  # non-interior cells copied
+        # in place (div_out == div_in), on the last state
+        rc = L.csadv_mass_fixer_noalloc(d_in.data_ptr(), metric.data_ptr(), d_in.data_ptr(), N, None)
+        assert rc == _lib.OK, _lib.status_string(rc)
+        torch.cuda.synchronize()
+        inplace = d_in.cpu().numpy()
+        assert rel(inplace[4:N + 4, 4:N + 4], div_ref) <= RTOL
+        np.testing.assert_array_equal(inplace[:4], full[:4])
 
 
 def test_no_alloc_rejects_bad_sizes():
