@@ -247,9 +247,19 @@ int csadv_tune(csadv_plan *plan, int reps, void *stream, int *tile_out);
  * pool): it needs no plan and allocates nothing; its reduction scratch is a fixed 98 KB
  * device array inside the library, held by every GPU that loads it until exit.
  * Limit: N <= 2048 (CSADV_ERR_TOO_LARGE beyond).  The first call on a device looks up the
- * scratch's device address; make it before any stream capture.  Calls that overlap on the
- * GPU share the scratch and race; order them on one stream. */
+ * scratch's device address; make it before any stream capture.  That address is remembered
+ * for the life of the process: it does not survive cudaDeviceReset (or any other teardown
+ * of the device's primary context), after which this entry point must not be called again
+ * in the process.  Calls that overlap on the GPU share the scratch and race; order them on
+ * one stream. */
 int csadv_mass_fixer_noalloc(const double *div_in, const double *metric, double *div_out, int N, void *stream);
+
+/* ---------------------------------------------------------------- measurement */
+/* No counterpart in the reference.  The FP64 fused multiply-add rate of the current device in
+ * flop/s (2 per DFMA): independent dependency chains on every SM, `iters` DFMA per chain, best
+ * of three CUDA-event-timed launches on `stream`.  The FP64 step kernel is bound by this pipe
+ * on GB300, so its roofline is stated against it.  Synchronises the stream. */
+int csadv_fp64_rate(int iters, double *flops_per_s, void *stream);
 
 /* ---------------------------------------------------------------- pinned host memory */
 int csadv_host_alloc(void **ptr, size_t bytes);

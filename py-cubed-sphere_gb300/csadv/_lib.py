@@ -99,6 +99,7 @@ _SIGS = {
     "csadv_mass_target": ([_vp, _c_int, _dp, _dp, _vp], _c_int),
     "csadv_nearest_neighbour": ([_vp, _c_int, _vp, _vp, _vp, ctypes.c_longlong, _vp, _vp], _c_int),
     "csadv_host_free": ([_vp], _c_int),
+    "csadv_fp64_rate": ([_c_int, _dp, _vp], _c_int),
 }
 
 
