@@ -83,8 +83,13 @@ def test_one_revolution_N48_fp64_and_fp32():
 
 def test_deformational_flow_N384_to_T_fp64_and_fp32():
     """N = 384, cosine bells and smooth bells in the deformational wind (k = 0.48, T = 5), to
-    t = T where the exact solution is the initial field.  FP32 L2 within 1 % of FP64's for both
-    tracers, mass within 1e-6 (FP32) and 1e-12 (FP64)."""
+    t = T where the exact solution is the initial field; mass within 1e-6 (FP32) and 1e-12 (FP64).
+
+    The cosine bells' FP32 L2 error is within 1 % of FP64's.  The smooth bells (0.95 + 0.05 h)
+    have an FP64 L2 error of about 2e-6 at this resolution, some 35 float32 ulps of their values
+    (~1): the FP32 state is rounded to 2^-24 relative at every one of the ~4800 steps, so its
+    error is bounded by FP64's plus that rounding's random walk, sqrt(steps) 2^-24 max|q|, and
+    not by 1 % of FP64's."""
     N, vf, wp = 384, 102, (0.48, 5.0, 0.0, 0.0)
     ics = [(102, None), (103, None)]
     nsteps, dt = steps_to(N, vf, wp, 5.0)
@@ -95,7 +100,10 @@ def test_deformational_flow_N384_to_T_fp64_and_fp32():
         q32, e32, dm32 = r32[t]
         print("N=384 deformational to t=T (%d steps), tracer %d: FP64 %s FP32 %s; FP32 vs FP64 %.2e; "
               "mass change FP64 %.2e FP32 %.2e" % (nsteps, t, e64, e32, rel(q32, q64), dm64, dm32))
-        assert abs(e32[2] - e64[2]) <= 0.01 * e64[2]
+        if t == 0:
+            assert abs(e32[2] - e64[2]) <= 0.01 * e64[2]
+        walk = math.sqrt(nsteps) * 2.0 ** -24 * np.max(np.abs(q64))
+        assert e32[2] <= 1.01 * e64[2] + walk
         assert dm64 < 1e-12
         assert dm32 < 1e-6
         assert rel(q32, q64) < 1e-3
