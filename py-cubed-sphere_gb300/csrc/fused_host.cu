@@ -136,8 +136,11 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     if (!mem.ok()) return CSADV_ERR_OOM;
     // line-marching kernel data: edge records (filled by the wind preparation), cell records
     // {g, 1/g} natural and transposed, the y-edge metric transposed (for the y-edge records)
-    f.erx = mem.alloc<char>(2 * d.field * es);
-    f.ery = mem.alloc<char>(2 * d.field * es);
+    // edge records {u, +-g}; FP64: with the flux coefficients in two more vec2 planes behind them
+    // (record_coef_offset)
+    const size_t rec_bytes = (o.precision == 64 ? 6 : 2) * (size_t)d.field * es;
+    f.erx = mem.alloc<char>(rec_bytes);
+    f.ery = mem.alloc<char>(rec_bytes);
     f.crx = mem.alloc<char>(2 * d.plane * es);
     f.cry = mem.alloc<char>(2 * d.plane * es);
     void *gpvT = mem.alloc<char>(d.plane * es);
@@ -166,8 +169,8 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
         CSADV_CUDA(cudaGetLastError());
     }
     f.gpvT = gpvT;
-    CSADV_CUDA(cudaMemsetAsync(f.erx, 0, 2 * (size_t)d.field * es, st));
-    CSADV_CUDA(cudaMemsetAsync(f.ery, 0, 2 * (size_t)d.field * es, st));
+    CSADV_CUDA(cudaMemsetAsync(f.erx, 0, rec_bytes, st));
+    CSADV_CUDA(cudaMemsetAsync(f.ery, 0, rec_bytes, st));
     if (f.mass_target) CSADV_CUDA(cudaMemsetAsync(f.mass_target, 0, T * sizeof(double), st));
     if (f.anchor_count) CSADV_CUDA(cudaMemsetAsync(f.anchor_count, 0, sizeof(unsigned int), st));
     CSADV_CUDA(cudaMemsetAsync(f.Qbuf[1], 0, (size_t)T * d.field * es, st));
@@ -195,9 +198,9 @@ int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt,
     if (f.sweep && w.nbasis) {
         if (o.precision == 64)
             return wind_step<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT, (double2 *)f.erx,
-                                     (double2 *)f.ery, st);
+                                     (double2 *)f.ery, f.crx, f.cry, st);
         return wind_step<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.rec_x(buf),
-                                (float2 *)f.rec_y(buf), st);
+                                (float2 *)f.rec_y(buf), nullptr, nullptr, st);
     }
     if (w.nbasis) {  // per-edge tile kernel on a basis wind: current and previous winds first
         int rc = wind_sync(o, g, w, st);
@@ -206,9 +209,9 @@ int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt,
     if (f.sweep) {
         if (o.precision == 64)
             return wind_avgprep_t<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT,
-                                          (double2 *)f.erx, (double2 *)f.ery, st);
+                                          (double2 *)f.erx, (double2 *)f.ery, f.crx, f.cry, st);
         return wind_avgprep_t<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.erx,
-                                     (float2 *)f.ery, st);
+                                     (float2 *)f.ery, nullptr, nullptr, st);
     }
     if (o.precision == 64)
         return wind_avgprep<double>(o, g, w, dt, (double *)f.ua, (double *)f.va, f.upos, f.vpos, f.wpitch, st);
@@ -253,6 +256,7 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.counter = f.counter;
         s.erx = f.rec_x(b);
         s.ery = f.rec_y(b);
+        s.ecofs = o.precision == 64 ? record_coef_offset<double>(g.d) : 0;
         s.crx = f.crx;
         s.cry = f.cry;
         s.gpc = f.g_pc;

@@ -104,10 +104,11 @@ int wind_set_dt(Winds &w, double dt, cudaStream_t st);
 // time-dependent wind of a fused plan as coefficient fields of a time basis, ghost edges
 // included (uses u_pu / v_pv as scratch: call before wind_initial)
 int wind_basis_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, cudaStream_t st);
-// departure-point winds + upwind flags of the step from the basis (line-marching layouts)
+// departure-point winds + upwind flags of the step from the basis (line-marching layouts); FP64:
+// with the edges' flux coefficients, from the cell records crx / cry
 template <class real, class V>
 int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
-              V *ery, cudaStream_t st);
+              V *ery, const void *crx, const void *cry, cudaStream_t st);
 // u_pu, v_pv, u_old, v_old <- the basis at the clock's times (before staged operators run)
 int wind_sync(const Options &o, const Grid &g, const Winds &w, cudaStream_t st);
 int wind_initial(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
@@ -188,7 +189,7 @@ int sweep_launch<float>(int recon, int split, const SweepSolve *dsolves, const i
 // edge records of the line-marching kernel from the reference-layout winds (static winds: once)
 template <class real, class V>
 int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT,
-                   V *erx, V *ery, cudaStream_t st);
+                   V *erx, V *ery, const void *crx, const void *cry, cudaStream_t st);
 // ghost cells of Qbuf[cur] <- those of Qbuf[1-cur] (the halo the last step used)
 int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
 // FP32 form with MF-PR: record sum(Q g) of tracer t of Qbuf[cur] (no pending correction) as the

@@ -71,6 +71,38 @@ struct Pred<double> {
     __device__ static __forceinline__ bool lt_neg(double p, double d) { return b(p) < 0 && (b(p) & MAG) > b(d); }
 };
 
+// FP64 helpers on the integer pipe.  GB300 issues FP64 arithmetic at 1/64 of the FP32 rate, so
+// the FP64 kernel moves every operation that needs no FP64 rounding off the FP64 pipe: absolute
+// values and sign transfers on the sign bit, exact scalings by powers of two on the exponent
+// field, orderings on the bit patterns.
+__device__ __forceinline__ double iabs(double x) {
+    return __hiloint2double(__double2hiint(x) & 0x7fffffff, __double2loint(x));
+}
+// |v| with the sign of a
+__device__ __forceinline__ double icopysign(double v, double a) {
+    return __hiloint2double((__double2hiint(v) & 0x7fffffff) | (__double2hiint(a) & (int)0x80000000),
+                            __double2loint(v));
+}
+// x 2^K, equal to the FP64 product whenever that is a normal number (every value of an advected
+// field); results below the normal range become a zero of x's sign, and x is returned unchanged
+// when it is infinite, NaN or so large (> 2^1022) that the product would overflow
+template <int K>
+__device__ __forceinline__ double pow2_scale(double x) {
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    const int e = (hi >> 20) & 0x7ff;
+    constexpr int EMIN = K < 0 ? 1 - K : 1, EMAX = K > 0 ? 0x7fe - K : 0x7fe;
+    const bool in = e >= EMIN && e <= EMAX;
+    const bool tiny = e < EMIN;
+    const int hi2 = in ? hi + K * (1 << 20) : (tiny ? (hi & (int)0x80000000) : hi);
+    return __hiloint2double(hi2, tiny ? 0 : lo);
+}
+// x as a signed integer key whose order is the floating-point order of finite values (+0 and -0
+// equal)
+__device__ __forceinline__ long long order_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b < 0 ? -(b & 0x7fffffffffffffffLL) : b;
+}
+
 // --------------------------------------------------------------------------- reconstructions
 // CW84 limited slope of the cell q0 between qm and qp (reconstruction_1d.py:64-100);
 // min(...) * sign(d0) written as copysign: equal for every finite input
@@ -139,8 +171,67 @@ __device__ __forceinline__ real ppm0_edge(real qam, real qa, real qb, real qbp) 
     return real(7.0 / 12.0) * (qb + qa) - Div<real>::by(qbp + qam, real(12.0), real(1.0 / 12.0));
 }
 
+// The FP64 CW84 reconstruction with its FP64 operations cut to the ones that round: the limited
+// slope from a = qp - qm, b = qp - q0, c = q0 - qm (reconstruction_1d.py:64-100) is
+// sign(a) min(|a|/2, 2 min(|b|, |c|)) when b c > 0, with the scalings exact on the exponent; the
+// edge value 0.5 (qa + qb) - (sb - sa)/6; the limiter (reconstruction_1d.py:102-153) with the
+// monotonicity test as an ordering of the bit patterns (R - qc and qc - L have the signs of
+// those comparisons) and the flattened case's DL = 0, mid = 0 selected.
+__device__ __forceinline__ double cw84_slope_d(double a, double b, double c) {
+    using B = Pred<double>;
+    const double m = B::min_nonneg(iabs(b), iabs(c));
+    const double v = B::min_nonneg(pow2_scale<-1>(iabs(a)), pow2_scale<1>(m));
+    return B::prod_pos(b, c) ? icopysign(v, a) : 0.0;
+}
+__device__ __forceinline__ double cw84_edge_d(double qa, double qb, double sa, double sb) {
+    return fma(-(sb - sa), 1.0 / 6.0, pow2_scale<-1>(qb + qa));
+}
+__device__ __forceinline__ void cw84_limit_d(double qc, double &L, double &R) {
+    using B = Pred<double>;
+    const double dq = R - L, RpL = R + L;
+    const double q3 = 3.0 * qc;
+    const double q6 = fma(-3.0, RpL, pow2_scale<1>(q3));
+    const long long kR = order_key(R), kq = order_key(qc), kL = order_key(L);
+    const bool flat = !((kR > kq && kq > kL) || (kR < kq && kq < kL));
+    const bool over = B::abs_lt(dq, q6);
+    const double DL = flat ? 0.0 : dq;
+    const double mid = flat ? 0.0 : fma(-0.5, RpL, qc);
+    const double d2 = DL * DL * (1.0 / 6.0);
+    const double prod = DL * mid;
+    const bool ml = over && B::gt_nonneg(prod, d2);
+    const bool mr = over && !ml && B::lt_neg(prod, d2);
+    const double Ln = fma(-2.0, R, q3), Rn = fma(-2.0, L, q3);
+    const double Lf = flat ? qc : L, Rf = flat ? qc : R;
+    L = ml ? Ln : Lf;
+    R = mr ? Rn : Rf;
+}
+
 // Marching reconstruction: init() with the window of the first cell, then cell() once per
 // cell (window w[0..4] = q[m-2..m+2]) gives the cell's (L, R) and advances.
+template <class real, int REC>
+struct March;
+template <>
+struct March<double, REC_CW84> {
+    double s, E, dd;  // slope of the current cell; edge value at its left edge; w[3] - w[2]
+    __device__ __forceinline__ void init(const double w[5]) {
+        const double d01 = w[1] - w[0], d12 = w[2] - w[1], d23 = w[3] - w[2];
+        const double sp = cw84_slope_d(w[2] - w[0], d12, d01);
+        s = cw84_slope_d(w[3] - w[1], d23, d12);
+        E = cw84_edge_d(w[1], w[2], sp, s);
+        dd = d23;
+    }
+    __device__ __forceinline__ void cell(const double w[5], double &L, double &R) {
+        const double b = w[4] - w[3];
+        const double sn = cw84_slope_d(w[4] - w[2], b, dd);
+        const double En = cw84_edge_d(w[2], w[3], s, sn);
+        L = E;
+        R = En;
+        cw84_limit_d(w[2], L, R);
+        s = sn;
+        E = En;
+        dd = b;
+    }
+};
 template <class real, int REC>
 struct March {
     real s, E;  // slope of the current cell; edge value at its left edge
@@ -197,6 +288,8 @@ struct Line {
     const real *s;
     int ss;
     const V *e, *c;
+    const V *f;     // flux coefficients of edge m: {alpha, beta} at f[m * P], {gamma, 0} at f[m * P + fo]
+    long long fo;   // (flux_coefs and put_record, wind.cu)
 };
 
 enum { MARCH_SPLIT = 0, MARCH_DIFF = 1, MARCH_UPDATE = 2 };
@@ -218,8 +311,8 @@ constexpr int SWEEP_UNROLL = CSADV_SWEEP_UNROLL;  // march loop unrolling (2: me
 //   MARCH_UPDATE: Q(k) - dt div(k) -> qout[k * P], with the y-flux differences dY[k * os]
 //                 and Q(k) at Qc[k * qs]; returns the line's sums of div * g and of the new
 //                 Q * g (MF-PR)
-// Loads run ahead of the arithmetic: edge records two iterations, cell records and the
-// shared-memory window one iteration, so the global (L1/L2) latency overlaps the work.
+// Loads run one iteration ahead of the arithmetic (edge records and flux coefficients, cell
+// records, the shared-memory window), so the global (L1/L2) latency overlaps the work.
 template <class real, int REC, int MODE>
 __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int ma, int mb, real dtdx, real irdx,
                                                 int mt, int split, bool mfpr, real *out, int os, const real *dY,
@@ -231,51 +324,45 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
     for (int k = 0; k < 5; ++k) w[k] = ln.s[(ma - 3 + k) * ln.ss];
     March<real, REC> rc;
     rc.init(w);
-    V eA = ln.e[(ma - 1) * P], eB = ln.e[ma * P], eN = eA;  // edges m, m+1 (m+2 loaded in the loop)
-    V cC = ln.c[(ma - 1) * P], cN = cC;                     // cell m
+    V eA = ln.e[(ma - 1) * P], eN = eA;                          // edge m (m+1 loaded in the loop)
+    V fA = ln.f[(ma - 1) * P], fN = fA;                          // its flux coefficients
+    real gA = ln.f[(ma - 1) * P + ln.fo].x, gN = gA;
+    V cC = ln.c[(ma - 1) * P], cN = cC;                          // cell m
     real nw4 = real(0);
-    real pL = real(0), pR = real(0), pQ = real(0);  // previous cell's parabola (metric-weighted for MT-0)
+    real pL = real(0), pR = real(0), pQ = real(0);  // previous cell's parabola
     real Fp = real(0), cp = real(0), gcp = real(0), igp = real(0), acc = real(0), accm = real(0);
 #pragma unroll SWEEP_UNROLL
     for (int m = ma - 1; m <= mb; ++m) {
         if (m < mb) {
             nw4 = ln.s[(m + 3) * ln.ss];
-            eN = ln.e[(m + 2) * P];
+            eN = ln.e[(m + 1) * P];
+            fN = ln.f[(m + 1) * P];
+            gN = ln.f[(m + 1) * P + ln.fo].x;
             cN = ln.c[(m + 1) * P];
         }
-        const real gl = O::ab(eA.y), gr = O::ab(eB.y), gcm = cC.x;
+        const real gl = O::ab(eA.y), gcm = cC.x;
         real L, R;
         rc.cell(w, L, R);
-        real cL = L, cR = R, cQ = w[2];
-        if (mt == MT_0) {  // flux.py:28-31
-            cL = L * gl;
-            cR = R * gr;
-            cQ = w[2] * gcm;
-        }
         if (m >= ma) {
-            // upwind PPM flux through edge m (flux.py:20-128): cell m-1 when the wind is >= 0
+            // upwind PPM flux through edge m (flux.py:20-128) from the parabola (q_L, q_R, mean) of
+            // the upwind cell (m-1 when the wind is >= 0): F = alpha q_R + beta q_L + gamma mean,
+            // the reference's u (e -+ c/2 (q6 -+ dq) - q6 c^2/3) with its metric weights
+            // (flux.py:28-31 for MT-0, the edge metric for MT-PL07) multiplied out per edge
+            // (flux_coefs, wind.cu)
             const real u = eA.x;
             const bool up = !signbit(eA.y);
             const real ig = igp;
-            const real c = u * dtdx;
-            const real eL = up ? pL : cL, eR = up ? pR : cR, eQ = up ? pQ : cQ;
-            const real dq = eR - eL;
-            const real q6 = real(6) * eQ - real(3) * (eR + eL);
-            const real e = up ? eR : eL;
-            const real hc = c * real(0.5);
-            const real t1 = up ? hc * (q6 - dq) : -(hc * (q6 + dq));
-            real F = e + t1 - Div<real>::by(q6 * c * c, real(3.0), real(1.0 / 3.0));
-            F = F * u;
-            if (mt == MT_PL07) F = F * gl;
-            const real cm = gl * c;  // g u dt/dx at edge m (SP-L04, SP-PL07)
+            const real eL = up ? pL : L, eR = up ? pR : R, eQ = up ? pQ : w[2];
+            const real F = fma(gA, eQ, fma(fA.y, eL, fA.x * eR));
+            const real cm = split == SP_AVLT ? real(0) : gl * (u * dtdx);  // g u dt/dx at edge m (SP-L04, SP-PL07)
             if (m > ma) {
                 const int k = m - 1;
                 if (MODE == MARCH_SPLIT) {
                     const real q = w[1];
                     const real dF = -(F - Fp) * dtdx;
                     real o;
-                    if (split == SP_AVLT)
-                        o = q + real(0.5) * dF * ig;
+                    if (split == SP_AVLT)  // q + dF / (2 g), dF = -(F - Fp) dt/dx
+                        o = fma(-(F - Fp), (real(0.5) * dtdx) * ig, q);
                     else if (split == SP_L04)
                         o = (q * gcp + real(0.5) * dF + real(0.5) * (cm - cp) * q) * ig;
                     else
@@ -285,24 +372,22 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
                     out[k * os] = F - Fp;
                 } else {
                     const real sdiv = (F - Fp) + dY[k * os];
-                    const real qn = Qc[k * qs] - sdiv * dtdx * ig;
+                    const real qn = fma(-sdiv, dtdx * ig, Qc[k * qs]);
                     qout[(long long)k * P] = qn;
-                    if (mfpr) {
-                        acc += sdiv * ig * irdx * gcp;
-                        accm += qn * gcp;
-                    }
+                    if (mfpr) acc += sdiv;  // sum(div g) = sum(sdiv) / dx: div = sdiv / (dx g)
                 }
             }
             Fp = F;
             cp = cm;
         }
-        pL = cL;
-        pR = cR;
-        pQ = cQ;
+        pL = L;
+        pR = R;
+        pQ = w[2];
         gcp = gcm;
         igp = cC.y;
-        eA = eB;
-        eB = eN;
+        eA = eN;
+        fA = fN;
+        gA = gN;
         cC = cN;
         w[0] = w[1];
         w[1] = w[2];
@@ -310,14 +395,15 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
         w[3] = w[4];
         w[4] = nw4;
     }
-    return LineSums<real>{acc, accm};
+    return LineSums<real>{acc * irdx, accm};
 }
 
-// CTAs per SM the register allocation is sized for: FP32 is latency-bound and gains from a
-// second resident CTA; FP64 is bound by the FP64 pipe and keeps the registers
+// CTAs per SM the register allocation is sized for: two, so that the FP64 pipe (on GB300 its
+// results arrive on the short scoreboard, long after issue) has twice the warps to choose from
+// (measured: 533 -> 517 us on the N=384 two-tracer step)
 #ifndef CSADV_SWEEP_MINB
 template <class real> struct SweepMinBlocks { static constexpr int value = 2; };
-template <> struct SweepMinBlocks<double> { static constexpr int value = 1; };
+template <> struct SweepMinBlocks<double> { static constexpr int value = 2; };
 #else
 template <class real> struct SweepMinBlocks { static constexpr int value = CSADV_SWEEP_MINB; };
 #endif
@@ -352,6 +438,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
         const bool mfpr = S.mfpr != 0;
         using V = typename Vec2<real>::type;
         const V *erx = (const V *)S.erx + pofs, *ery = (const V *)S.ery + pofs;
+        const V *efx = erx + S.ecofs, *efy = ery + S.ecofs;
         const V *crx = (const V *)S.crx, *cry = (const V *)S.cry;
         const real *gpc = (const real *)S.gpc;
 
@@ -386,66 +473,58 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
             // P1: first pass.  x-lines: columns c in [-3, nj+3), cells [0, ni) -> Qx;
             //                  y-lines: rows r in [-3, ni+3), cells [0, nj) -> Qy
             {
-                const int LX = round32(nj + 6), LY = round32(ni + 6);
+                // jobs packed densely (no idle lanes between lines); x- and y-lines share one code path
+                const int LX = nj + 6, LY = ni + 6;
                 const int jx = S.s1x * LX, jy = S.s1y * LY;
                 for (int job = tid; job < jx + jy; job += SWEEP_THREADS) {
-                    if (job < jx) {
-                        const int seg = job / LX, c = job - seg * LX - 3;
-                        const int ma = ni * seg / S.s1x, mb = ni * (seg + 1) / S.s1x;
-                        if (c >= nj + 3 || ma >= mb) continue;
-                        const long long g0 = (long long)I0 * P + J0 + c;
-                        Line<real> ln{sQ + 3 * L.QJp + c + 3, L.QJp, erx + g0, crx + g0};
-                        march<real, REC, MARCH_SPLIT>(ln, P, ma, mb, dtdx, irdx, mt, split, false, sQx + c + 3,
-                                                      L.QJp, nullptr, nullptr, 0, nullptr);
-                    } else {
-                        const int jj = job - jx;
-                        const int seg = jj / LY, r = jj - seg * LY - 3;
-                        const int ma = nj * seg / S.s1y, mb = nj * (seg + 1) / S.s1y;
-                        if (r >= ni + 3 || ma >= mb) continue;
-                        const long long g0 = (long long)J0 * P + I0 + r;
-                        Line<real> ln{sQ + (r + 3) * L.QJp + 3, 1, ery + g0, cry + g0};
-                        march<real, REC, MARCH_SPLIT>(ln, P, ma, mb, dtdx, irdx, mt, split, false,
-                                                      sQy + (r + 3) * L.TJp, 1, nullptr, nullptr, 0, nullptr);
-                    }
+                    const bool xl = job < jx;
+                    const int jj = xl ? job : job - jx, nl = xl ? LX : LY, ns = xl ? S.s1x : S.s1y, len = xl ? ni : nj;
+                    const int seg = jj / nl, o = jj - seg * nl - 3;  // o: column (x-lines) or row (y-lines)
+                    const int ma = len * seg / ns, mb = len * (seg + 1) / ns;
+                    if (ma >= mb) continue;
+                    const long long g0 = xl ? (long long)I0 * P + J0 + o : (long long)J0 * P + I0 + o;
+                    Line<real> ln{xl ? sQ + 3 * L.QJp + o + 3 : sQ + (o + 3) * L.QJp + 3, xl ? L.QJp : 1,
+                                  (xl ? erx : ery) + g0, (xl ? crx : cry) + g0, (xl ? efx : efy) + g0, S.ecofs};
+                    march<real, REC, MARCH_SPLIT>(ln, P, ma, mb, dtdx, irdx, mt, split, false,
+                                                  xl ? sQx + o + 3 : sQy + (o + 3) * L.TJp, xl ? L.QJp : 1, nullptr,
+                                                  nullptr, 0, nullptr);
                 }
             }
             __syncthreads();
             // P2: y-lines of Qx over rows [0, ni): y-flux differences -> sDy
             {
-                const int LY = round32(ni);
+                const int LY = ni;  // jobs packed densely
                 const int jy = S.s2y * LY;
                 for (int job = tid; job < jy; job += SWEEP_THREADS) {
                     const int seg = job / LY, r = job - seg * LY;
                     const int ma = nj * seg / S.s2y, mb = nj * (seg + 1) / S.s2y;
                     if (r >= ni || ma >= mb) continue;
                     const long long g0 = (long long)J0 * P + I0 + r;
-                    Line<real> ln{sQx + r * L.QJp + 3, 1, ery + g0, cry + g0};
+                    Line<real> ln{sQx + r * L.QJp + 3, 1, ery + g0, cry + g0, efy + g0, S.ecofs};
                     march<real, REC, MARCH_DIFF>(ln, P, ma, mb, dtdx, irdx, mt, split, false, sDy + r * L.TJp, 1,
                                                  nullptr, nullptr, 0, nullptr);
                 }
             }
             __syncthreads();
             // P3: x-lines of Qy over columns [0, nj): x fluxes, div, update, MF-PR partials
-            real acc = real(0), accm = real(0);
+            real acc = real(0);
             {
-                const int LX = round32(nj);
+                const int LX = nj;  // jobs packed densely
                 const int jx = S.s2x * LX;
                 for (int job = tid; job < jx; job += SWEEP_THREADS) {
                     const int seg = job / LX, c = job - seg * LX;
                     const int ma = ni * seg / S.s2x, mb = ni * (seg + 1) / S.s2x;
                     if (c >= nj || ma >= mb) continue;
                     const long long g0 = (long long)I0 * P + J0 + c;
-                    Line<real> ln{sQy + 3 * L.TJp + c, L.TJp, erx + g0, crx + g0};
+                    Line<real> ln{sQy + 3 * L.TJp + c, L.TJp, erx + g0, crx + g0, efx + g0, S.ecofs};
                     const LineSums<real> ls = march<real, REC, MARCH_UPDATE>(
                         ln, P, ma, mb, dtdx, irdx, mt, split, mfpr, nullptr, L.TJp, sDy + c, sQ + 3 * L.QJp + c + 3,
                         L.QJp, Qout + g0);
                     acc += ls.div;
-                    accm += ls.mass;
                 }
             }
             if (mfpr) {  // FP64 across threads, in a fixed order
-                const bool anchor = S.mass_target != nullptr;
-                double dacc = (double)(anchor ? accm : acc);
+                double dacc = (double)acc;  // the FP64 form has no mass target (the reference's projection)
                 for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
                 if (lane == 0) red[warp] = dacc;
                 __syncthreads();

@@ -566,7 +566,7 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
     //     y-lines over rows r in [-3, ni+3), cells [0, nj) -> Qy
     // (one code path for both directions: the line's strides and records are arguments)
     {
-        const int LX = round32(nj + 6), LY = round32(ni + 6);
+        const int LX = nj + 6, LY = ni + 6;  // jobs packed densely: no idle lanes between lines
         const int jx = S.s1x * LX, job = tid;
         bool go = false;
         const V *line = nullptr;
@@ -608,7 +608,7 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
     __syncthreads();
     // P2: y-lines of Qx over rows [0, ni): second-pass y-flux differences -> dY
     {
-        const int LY = round32(ni);
+        const int LY = ni;
         const int job = tid;
         if (job < S.s2y * LY) {
             const int seg = job / LY, r = job - seg * LY;
@@ -628,7 +628,7 @@ __device__ __forceinline__ void tile_pass(const SweepSolve &S, int p, int item, 
     // P3: x-lines of Qy over columns [0, nj): second-pass x fluxes, div, update, MF-PR partials
     V acc = bc<V>(0.f), accm = bc<V>(0.f);
     {
-        const int LX = round32(nj);
+        const int LX = nj;
         const int job = tid;
         if (job < S.s2x * LX) {
             const int seg = job / LX, c = job - seg * LX;

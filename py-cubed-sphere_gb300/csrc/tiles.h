@@ -62,8 +62,11 @@ struct SweepSolve {
     unsigned int *counter;  // arrival counter (MF-PR)
     // edge records {departure-point wind, +-metric at the edge; the sign is the upwind flag,
     // + when the wind is >= 0}: x-edges natural (row i, column j), y-edges transposed (row j,
-    // column i); per panel plane, element type vec2 of the state's precision
+    // column i); per panel plane, element type vec2 of the state's precision.  FP64: the edges'
+    // flux coefficients {alpha, beta} at erx + ecofs and {gamma, 0} at erx + 2 ecofs (units of
+    // double2; flux_coefs and put_record in wind.cu); ecofs 0 in the FP32 form, which has none
     const void *erx, *ery;
+    long long ecofs;
     // cell records {metric, 1 / metric}: natural and transposed (one plane)
     const void *crx, *cry;
     const void *gpc;        // metric at the centres (state precision), for the pending correction
@@ -76,6 +79,11 @@ struct SweepSolve {
     const int *hlag_k;
     const struct GhostTerm *gside, *gcorner;  // the FP32 form's flattened ghost-cell stencils
 };
+
+// offset (vec2 units) of the flux coefficients behind the edge records of one direction: the
+// FP64 line-marching kernel reads them, the FP32 one forms the same terms itself
+template <class real>
+__host__ __device__ inline long long record_coef_offset(const Dims &d) { return sizeof(real) == 8 ? d.field : 0; }
 
 // blocks of the batched ghost-cell kernel per tracer of a solve (128 ghost-cell columns each)
 __host__ __device__ inline int halo_blocks(const Dims &d) { return (NFACE * 4 * NG * d.n + 127) / 128; }
@@ -111,7 +119,9 @@ __host__ __device__ __forceinline__ SweepSmem sweep_smem(int ti, int tj) {
 }
 
 // tile configuration of a solve: shape and segments per line (about 256 threads per phase,
-// segments of at least ~10 cells)
+// segments of at least ~10 cells).  The step kernels number a phase's jobs densely (line l,
+// segment s at job s * lines + l), so lanes past the last line do not idle inside a warp; the
+// counts below, sized with lines rounded up to 32, stay within 256 jobs either way.
 inline void sweep_config(SweepSolve &s, int cfg) {
     s.ti = SWEEP_TILES[cfg][0];
     s.tj = SWEEP_TILES[cfg][1];

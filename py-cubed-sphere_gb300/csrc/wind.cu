@@ -38,6 +38,79 @@ __device__ __forceinline__ V edge_record(W wind, W g, bool up) {
     return r;
 }
 
+// Flux coefficients of an edge for the FP64 line-marching kernel.  The upwind PPM flux through an
+// edge (flux.py:20-128, with the metric weights of flux.py:28-31),
+//   u >= 0:  F = u (q_R + c/2 (q6 - dq) - q6 c^2/3),   u < 0:  F = u (q_L - c/2 (q6 + dq) - q6 c^2/3)
+// with dq = q_R - q_L, q6 = 6 mean - 3 (q_R + q_L) (each weighted by the metric at its point for
+// MT-0), c = u dt/dx and u the departure-point wind, is linear in the upwind cell's parabola:
+//   F = alpha q_R + beta q_L + gamma mean,
+//   u >= 0:  alpha = gR u (1-c)^2,  beta = -gL u c (1-c),  gamma = gC u c (3 - 2c)
+//   u <  0:  alpha = gR u c (1+c),  beta = gL u (1+c)^2,   gamma = -gC u c (3 + 2c)
+// (the weights gL, gR, gC of the upwind cell's left edge, right edge and centre for MT-0; the edge's
+// own metric for all three with MT-PL07, whose flux is F g).  Which cell is upwind follows the sign
+// of the current wind (flux.py:48-61); u above is the departure-point wind.  The coefficients
+// depend on the wind and the metric alone, so they are formed once per edge and step, here,
+// instead of once per tracer and pass in the step kernel, where every FP64 operation costs as much
+// as 64 FP32 ones on GB300.
+template <class W>
+struct UpwindMetric {
+    const W *ge;                          // edge metric along the line (x: g_pu natural; y: g_pv transposed)
+    const typename Vec2<W>::type *gc;     // cell records {g, 1/g} in the same orientation
+    int n;                                // rows of the orientation: edges 0..n, cells 0..n-1
+    int pl07;                             // MT-PL07: every weight is the edge's metric
+};
+
+// the upwind choice of an edge: wind >= 0 (flux.py:48-61), on the integer pipe for FP64 (-0 counts
+// as >= 0, as the comparison does)
+__device__ __forceinline__ bool wind_up(float u) { return u >= 0.f; }
+__device__ __forceinline__ bool wind_up(double u) {
+    const long long b = __double_as_longlong(u);
+    return b >= 0 || (b << 1) == 0;
+}
+
+template <class W>
+__device__ __forceinline__ void flux_coefs(W u, W g, bool up, W dtdx, const UpwindMetric<W> &um, const Dims &d, int m,
+                                           int col, W &al, W &be, W &ga) {
+    W gL = g, gR = g, gC = g;
+    if (!um.pl07) {  // the upwind cell: m - 1 (wind >= 0) or m, clamped to the plane
+        const int cm = up ? (m > 0 ? m - 1 : 0) : (m < um.n ? m : um.n - 1);
+        const int el = up ? (m > 0 ? m - 1 : 0) : m, er = up ? m : (m < um.n ? m + 1 : um.n);
+        gL = um.ge[at2(d, el, col)];
+        gR = um.ge[at2(d, er, col)];
+        gC = um.gc[at2(d, cm, col)].x;
+    }
+    // one branch-free form of both cases: s = 1 -+ c, P = u s^2, R = u c s;
+    // wind >= 0: (alpha, beta) = (gR P, -gL R), else (gR R, gL P); gamma = gC u c (+-3 - 2c)
+    const W c = u * dtdx;
+    const W uc = u * c;
+    const W sg = up ? W(1) : W(-1);
+    const W s = fma(-sg, c, W(1));
+    const W P = (u * s) * s, R = uc * s;
+    const W X = up ? P : R, Y = up ? -R : P;
+    al = gR * X;
+    be = gL * Y;
+    ga = gC * (uc * fma(W(-2), c, W(3) * sg));
+}
+
+// FP64 records: {u, +-g} (the sign carries the upwind choice) at rec[idx], the coefficients
+// {alpha, beta} at rec[idx + cofs] and {gamma, 0} at rec[idx + 2 cofs]; `coefs` false: zero
+// coefficients (an edge no flux goes through)
+__device__ __forceinline__ void put_record(double2 *rec, long long idx, long long cofs, double wind, double g, bool up,
+                                           double dtdx, const UpwindMetric<double> &um, const Dims &d, int m, int col,
+                                           bool coefs = true) {
+    rec[idx] = edge_record<double2>(wind, g, up);
+    double al = 0.0, be = 0.0, ga = 0.0;
+    if (coefs) flux_coefs(wind, g, up, dtdx, um, d, m, col, al, be, ga);
+    rec[idx + cofs] = make_double2(al, be);
+    rec[idx + 2 * cofs] = make_double2(ga, 0.0);
+}
+// FP32 records {u, +-g}: the paired kernel forms the flux terms of both tracers of a pair itself
+// (once per pair, in FP32), which measured faster than loading coefficient records
+__device__ __forceinline__ void put_record(float2 *rec, long long idx, long long, float wind, float g, bool up, float,
+                                           const UpwindMetric<float> &, const Dims &, int, int, bool = true) {
+    rec[idx] = edge_record<float2>(wind, g, up);
+}
+
 static dim3 plane_grid(const Dims &d, int bx) { return dim3(ceil_div(d.pitch, bx), d.n + 1, NFACE); }
 
 // analytic winds at interior edges at time t, converted to contravariant components
@@ -186,7 +259,7 @@ __global__ void k_clock_set(Clock *c, long long k, double t, WindParams wp, int 
 // on EVERY edge the step reads, ghost edges included: the reference's wind halo
 // (interpolation.py:347-532) is linear in the interior wind, so the ghost-edge coefficients
 // are the halo of each interior coefficient field, computed once.  A step then evaluates the
-// wind at the current and previous times directly (k_wind_step) instead of running the
+// wind at the current and previous times directly (k_wind_rec) instead of running the
 // wind update, the wind halo and the departure-point average as separate passes.
 //   deformational:  h = {1, K, K cos 2w, K sin 2w}, K = k cos(pi t/T), w = 2 pi t/T, from
 //                   sin^2(lon - w) = (1 - cos 2lon cos 2w - sin 2lon sin 2w) / 2 and
@@ -278,86 +351,14 @@ struct Coefs {
         for (int m = 0; m < M; ++m) s += c[m] * h[m];
         return s;
     }
+    // the same sum with fused multiply-adds (the FP64 records: every FP64 operation counts)
+    __device__ __forceinline__ W at_fma(const W *h) const {
+        W s = c[0] * h[0];
+#pragma unroll
+        for (int m = 1; m < M; ++m) s = fma(c[m], h[m], s);
+        return s;
+    }
 };
-
-// edge records of one step from the basis (the wind at the clock's current and previous
-// times): x-edges natural, y-edges transposed (as k_wind_avgprep_t).  Block (32, 8) covers a 32 x 32 (i, j) tile; the
-// wind and its RK2 extrapolation are evaluated once per edge (tile + one row / column of
-// neighbours) into shared memory, then averaged.
-template <class W, int M, class V>
-__global__ void k_wind_step(Dims d, const W *__restrict__ bu, const W *__restrict__ bv, const Clock *__restrict__ clk,
-                            const W *__restrict__ gpu, const W *__restrict__ gpvT, V *erx, V *ery, int rk2, W dto2,
-                            W dx) {
-    __shared__ W hn[4], ho[4];
-    __shared__ W xs[34][32], ys[32][35];  // extrapolated winds: x-edges rows ib-1.., y-edges cols jb-1..
-    __shared__ W xn[32][32], yn[32][33];  // winds now
-    __shared__ W tv[32][33];
-    __shared__ unsigned char tf[32][33];
-    const int p = blockIdx.z, jb = blockIdx.x * 32, ib = blockIdx.y * 32;
-    const int lane = threadIdx.x, wy = threadIdx.y, tid = wy * 32 + lane;
-    if (tid < 8) (tid < 4 ? hn : ho)[tid & 3] = (W)(tid < 4 ? clk->hn[tid] : clk->ho[tid - 4]);
-    __syncthreads();
-    // the wind now and 1.5 u - 0.5 u_old (the RK2 extrapolation) of edge (i, j), zero outside the
-    // plane; every coefficient load of a thread is issued before the first is used
-    constexpr int NE = (34 * 32 + 255) / 256;
-    Coefs<W, M> cx[NE], cy[NE];
-#pragma unroll
-    for (int q = 0; q < NE; ++q) {
-        const int e = tid + 256 * q;
-        {
-            const int r = e >> 5, c = e & 31, i = ib - 1 + r, j = jb + c;
-            if (e < 34 * 32 && i >= 0 && i <= d.n && j < d.pitch) cx[q].load(bu, at(d, p, i, j));
-            else cx[q].zero();
-        }
-        {
-            const int r = e / 34, c = e - r * 34, i = ib + r, j = jb - 1 + c;
-            if (e < 32 * 34 && i <= d.n && j >= 0 && j < d.pitch) cy[q].load(bv, at(d, p, i, j));
-            else cy[q].zero();
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < NE; ++q) {
-        const int e = tid + 256 * q;
-        if (e < 34 * 32) {
-            const int r = e >> 5, c = e & 31;
-            const W sn = cx[q].at(hn), so = cx[q].at(ho);
-            xs[r][c] = W(1.5) * sn - W(0.5) * so;
-            if (r >= 1 && r <= 32) xn[r - 1][c] = sn;
-        }
-        if (e < 32 * 34) {
-            const int r = e / 34, c = e - r * 34;
-            const W sn = cy[q].at(hn), so = cy[q].at(ho);
-            ys[r][c] = W(1.5) * sn - W(0.5) * so;
-            if (c >= 1 && c <= 32) yn[r][c - 1] = sn;
-        }
-    }
-    __syncthreads();
-    // averaged_velocity.py:14-62, given the wind and the three extrapolated winds along the line
-    auto average = [&](W u, W sm, W s0, W sp) {
-        const W a = u * dto2 / dx;
-        return (u >= W(0)) ? (W(1.0) - a) * s0 + a * sm : -a * sp + (W(1.0) + a) * s0;
-    };
-    for (int k = 0; k < 4; ++k) {
-        const int r = wy + 8 * k, i = ib + r, j = jb + lane;
-        const bool ok = i <= d.n && j < d.pitch;
-        const W u = xn[r][lane], v = yn[r][lane];
-        W au = u, av = v;
-        if (rk2) {
-            au = (j < d.n && i >= d.i0 && i <= d.iend) ? average(u, xs[r][lane], xs[r + 1][lane], xs[r + 2][lane])
-                                                       : W(0);
-            av = (i < d.n && j >= d.i0 && j <= d.iend) ? average(v, ys[r][lane], ys[r][lane + 1], ys[r][lane + 2])
-                                                       : W(0);
-        }
-        if (ok) erx[at(d, p, i, j)] = edge_record<V>(au, gpu[at2(d, i, j)], u >= W(0));
-        tv[r][lane] = av;
-        tf[r][lane] = (ok && v >= W(0)) ? 1 : 0;
-    }
-    __syncthreads();
-    for (int k = 0; k < 4; ++k) {
-        const int c = wy + 8 * k, j = jb + c, i = ib + lane;
-        if (j <= d.n && i < d.pitch) ery[at(d, p, j, i)] = edge_record<V>(tv[lane][c], gpvT[at2(d, j, i)], tf[lane][c] != 0);
-    }
-}
 
 // u, v <- the wind at the clock's current time, u_old, v_old <- at its previous time, on every
 // edge of the basis (for the staged operators used on a fused plan, e.g. csadv_divergence)
@@ -618,7 +619,8 @@ __global__ void k_wind_avgprep(Dims d, const W *__restrict__ U, const W *__restr
 template <class W, class V>
 __global__ void k_wind_avgprep_t(Dims d, const W *__restrict__ U, const W *__restrict__ Uo, const W *__restrict__ V_,
                                  const W *__restrict__ Vo, const W *__restrict__ gpu, const W *__restrict__ gpvT, V *erx,
-                                 V *ery, int rk2, W dto2, W dx) {
+                                 V *ery, int rk2, W dto2, W dx, long long cofs, W dtdx, UpwindMetric<W> mx,
+                                 UpwindMetric<W> my) {
     __shared__ W tv[32][33];
     __shared__ unsigned char tf[32][33];
     const int p = blockIdx.z, jb = blockIdx.x * 32, ib = blockIdx.y * 32;
@@ -637,7 +639,7 @@ __global__ void k_wind_avgprep_t(Dims d, const W *__restrict__ U, const W *__res
                 au = (j < d.n && i >= d.i0 && i <= d.iend) ? rk2_average(U, Uo, d, p, i, j, 0, dto2, dx) : W(0);
                 av = (i < d.n && j >= d.i0 && j <= d.iend) ? rk2_average(V_, Vo, d, p, i, j, 1, dto2, dx) : W(0);
             }
-            erx[t] = edge_record<V>(au, gpu[at2(d, i, j)], u >= W(0));
+            put_record(erx, t, cofs, au, gpu[at2(d, i, j)], u >= W(0), dtdx, mx, d, i, j);
         }
         tv[r][lane] = av;
         tf[r][lane] = (ok && v >= W(0)) ? 1 : 0;
@@ -645,7 +647,8 @@ __global__ void k_wind_avgprep_t(Dims d, const W *__restrict__ U, const W *__res
     __syncthreads();
     for (int k = 0; k < 4; ++k) {
         const int c = wy + 8 * k, j = jb + c, i = ib + lane;
-        if (j <= d.n && i < d.pitch) ery[at(d, p, j, i)] = edge_record<V>(tv[lane][c], gpvT[at2(d, j, i)], tf[lane][c] != 0);
+        if (j <= d.n && i < d.pitch)
+            put_record(ery, at(d, p, j, i), cofs, tv[lane][c], gpvT[at2(d, j, i)], tf[lane][c] != 0, dtdx, my, d, j, i);
     }
 }
 
@@ -885,48 +888,79 @@ __global__ void k_transpose_coefs(const W *__restrict__ src, W *dst, Dims d, int
     for (int m = 0; m < M; ++m) dst[t * M + m] = in ? src[(p * d.plane + (long long)b * d.pitch + a) * M + m] : W(0);
 }
 
-// Edge records of one step of the FP32 form from the basis: the x problem (coefficients bu, metric
-// gpu, records erx) and the y problem in transposed coordinates (bvT, gpvT, ery) are the same
-// computation, blockIdx.z = problem * 6 + panel.  A block covers 32 x 32 edges (rows ib.., columns
-// jb..): the wind at the clock's current and previous times and the RK2 extrapolation
-// 1.5 u - 0.5 u_old on rows ib-1 .. ib+32 into shared memory, then the departure-point average
-// along the row index (averaged_velocity.py:14-62) and the record {u_avg, +-g}.  Every coefficient
-// load of a thread is issued before the first is used.
-template <int M>
-__global__ void __launch_bounds__(256) k_wind_rec(Dims d, const float *__restrict__ bu, const float *__restrict__ bvT,
-                                                  const Clock *__restrict__ clk, const float *__restrict__ gpu,
-                                                  const float *__restrict__ gpvT, float2 *erx, float2 *ery, int rk2,
-                                                  float c_half) {
-    __shared__ float sx[34][33];  // extrapolated winds, rows ib-1 .. ib+32
-    __shared__ float sn[32][33];  // winds now, rows ib .. ib+31
+// Edge records of one step from the basis: the x problem (coefficients bu, metric gpu, records
+// erx) and the y problem in transposed coordinates (bvT, gpvT, ery) are the same computation,
+// blockIdx.z = problem * 6 + panel.  A block covers 32 x 32 edges (rows ib.., columns jb..): the
+// wind at the clock's current time and its RK2 extrapolation 1.5 u - 0.5 u_old on rows
+// ib-1 .. ib+32 into shared memory, then the departure-point average along the row index
+// (averaged_velocity.py:14-62) and the record (put_record).
+//   FP32 (W = float): every coefficient load of a thread is issued before the first is used; the
+//   wind and the extrapolation are sums over the basis at the two times (the records {u, +-g}).
+//   FP64 (W = double): the FP64 pipe bounds it, so the extrapolation is one fused sum over the basis
+//   with the time factors combined first, the average is written with fused multiply-adds, the
+//   rows are loaded one at a time (few registers: several blocks share an SM), no wind is formed in
+//   the padding columns, and the records carry the edges' flux coefficients (cofs) where fluxes go.
+template <class W, int M>
+__global__ void __launch_bounds__(256) k_wind_rec(Dims d, const W *__restrict__ bu, const W *__restrict__ bvT,
+                                                  const Clock *__restrict__ clk, const W *__restrict__ gpu,
+                                                  const W *__restrict__ gpvT, typename Vec2<W>::type *erx,
+                                                  typename Vec2<W>::type *ery, int rk2, W c_half, long long cofs, W dtdx,
+                                                  UpwindMetric<W> mx, UpwindMetric<W> my) {
+    using V = typename Vec2<W>::type;
+    constexpr bool F64 = sizeof(W) == 8;
+    __shared__ W sx[34][33];  // extrapolated winds, rows ib-1 .. ib+32
+    __shared__ W sn[32][33];  // winds now, rows ib .. ib+31
     const bool ydir = blockIdx.z >= NFACE;
     const int p = blockIdx.z - (ydir ? NFACE : 0);
-    const float *B = ydir ? bvT : bu;
-    const float *G = ydir ? gpvT : gpu;
-    float2 *E = (ydir ? ery : erx) + p * d.plane;
+    const W *B = ydir ? bvT : bu;
+    const W *G = ydir ? gpvT : gpu;
+    V *E = (ydir ? ery : erx) + p * d.plane;
+    const UpwindMetric<W> &um = ydir ? my : mx;
     const int jb = blockIdx.x * 32, ib = blockIdx.y * 32, lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
     const int j = jb + lane;
-    float hn[M], ho[M];
+    W hn[M], ho[M];
 #pragma unroll
     for (int m = 0; m < M; ++m) {
-        hn[m] = clk->hnf[m];
-        ho[m] = clk->hof[m];
+        if constexpr (F64) {
+            hn[m] = clk->hn[m];
+            ho[m] = W(1.5) * clk->hn[m] - W(0.5) * clk->ho[m];  // the extrapolation's time factors
+        } else {
+            hn[m] = clk->hnf[m];
+            ho[m] = clk->hof[m];
+        }
     }
     constexpr int NQ = 5;  // rows wy + 8 q, q < 5, cover the 34 rows
-    Coefs<float, M> c[NQ];
+    if constexpr (F64) {  // columns j >= n are padding: no wind there
+#pragma unroll 1
+        for (int q = 0; q < NQ; ++q) {
+            const int r = wy + 8 * q, i = ib - 1 + r;
+            if (r >= 34) break;
+            W xs = W(0), xn = W(0);
+            if (i >= 0 && i <= d.n && j < d.n) {
+                Coefs<W, M> c;
+                c.load(B, p * d.plane + (long long)i * d.pitch + j);
+                xs = c.at_fma(ho);
+                xn = c.at_fma(hn);
+            }
+            sx[r][lane] = xs;
+            if (r >= 1 && r <= 32) sn[r - 1][lane] = xn;
+        }
+    } else {
+        Coefs<W, M> c[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        const int r = wy + 8 * q, i = ib - 1 + r;
-        if (r < 34 && i >= 0 && i <= d.n && j < d.pitch) c[q].load(B, p * d.plane + (long long)i * d.pitch + j);
-        else c[q].zero();
-    }
+        for (int q = 0; q < NQ; ++q) {
+            const int r = wy + 8 * q, i = ib - 1 + r;
+            if (r < 34 && i >= 0 && i <= d.n && j < d.pitch) c[q].load(B, p * d.plane + (long long)i * d.pitch + j);
+            else c[q].zero();
+        }
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        const int r = wy + 8 * q;
-        if (r < 34) {
-            const float un = c[q].at(hn), uo = c[q].at(ho);
-            sx[r][lane] = 1.5f * un - 0.5f * uo;
-            if (r >= 1 && r <= 32) sn[r - 1][lane] = un;
+        for (int q = 0; q < NQ; ++q) {
+            const int r = wy + 8 * q;
+            if (r < 34) {
+                const W un = c[q].at(hn), uo = c[q].at(ho);
+                sx[r][lane] = W(1.5) * un - W(0.5) * uo;
+                if (r >= 1 && r <= 32) sn[r - 1][lane] = un;
+            }
         }
     }
     __syncthreads();
@@ -934,15 +968,23 @@ __global__ void __launch_bounds__(256) k_wind_rec(Dims d, const float *__restric
     for (int k = 0; k < 4; ++k) {
         const int r = wy + 8 * k, i = ib + r;
         if (i > d.n || j >= d.pitch) continue;
-        const float u = sn[r][lane];
-        float au = u;
+        const W u = sn[r][lane];
+        W au = u;
         if (rk2) {
-            const float a = u * c_half;
-            au = (j < d.n && i >= d.i0 && i <= d.iend)
-                     ? (u >= 0.f ? (1.f - a) * sx[r + 1][lane] + a * sx[r][lane] : -a * sx[r + 2][lane] + (1.f + a) * sx[r + 1][lane])
-                     : 0.f;
+            const W a = u * c_half;
+            const bool in = j < d.n && i >= d.i0 && i <= d.iend;
+            if constexpr (F64) {  // (1 - a) s0 + a sm = s0 + a (sm - s0); -a sp + (1 + a) s0 = s0 - a (sp - s0)
+                const W s0 = sx[r + 1][lane];
+                au = in ? (wind_up(u) ? fma(a, sx[r][lane] - s0, s0) : fma(-a, sx[r + 2][lane] - s0, s0)) : W(0);
+            } else {
+                au = in ? (u >= W(0) ? (W(1) - a) * sx[r + 1][lane] + a * sx[r][lane]
+                                     : -a * sx[r + 2][lane] + (W(1) + a) * sx[r + 1][lane])
+                        : W(0);
+            }
         }
-        E[(long long)i * d.pitch + j] = edge_record<float2>(au, G[(long long)i * d.pitch + j], u >= 0.f);
+        // fluxes go through x-edges of rows [i0, iend] at columns below n (y: the same transposed)
+        put_record(E, (long long)i * d.pitch + j, cofs, au, G[(long long)i * d.pitch + j], wind_up(u), dtdx, um, d, i,
+                   j, i >= d.i0 && i <= d.iend && j < d.n);
     }
 }
 
@@ -970,7 +1012,7 @@ static int basis_setup_t(const Options &o, const Grid &g, Winds &w, DeviceArena 
     }
     CSADV_CUDA(cudaMemsetAsync(w.u_pu, 0, F, st));
     CSADV_CUDA(cudaMemsetAsync(w.v_pv, 0, F, st));
-    if (sizeof(W) == 4) {  // the FP32 record kernel reads the y coefficients transposed
+    {  // the record kernel reads the y coefficients transposed
         w.btabT = mem.alloc<W>((long long)M * d.field);
         if (!mem.ok()) return CSADV_ERR_OOM;
         k_transpose_coefs<W><<<ceil_div(d.field, 256), 256, 0, st>>>((const W *)w.btab[1], (W *)w.btabT, d, M);
@@ -984,38 +1026,38 @@ int wind_basis_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem
     return o.precision == 64 ? basis_setup_t<double>(o, g, w, mem, st) : basis_setup_t<float>(o, g, w, mem, st);
 }
 
+// the metric the flux coefficients need (flux_coefs): x-lines natural, y-lines transposed
+template <class W>
+static void upwind_metrics(const Options &o, const Dims &d, const void *gpu, const void *gpvT, const void *crx,
+                           const void *cry, UpwindMetric<W> &mx, UpwindMetric<W> &my) {
+    using V = typename Vec2<W>::type;
+    mx = UpwindMetric<W>{(const W *)gpu, (const V *)crx, d.n, o.mt == MT_PL07 ? 1 : 0};
+    my = UpwindMetric<W>{(const W *)gpvT, (const V *)cry, d.n, o.mt == MT_PL07 ? 1 : 0};
+}
+
 template <class real, class V>
 int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
-              V *ery, cudaStream_t st) {
+              V *ery, const void *crx, const void *cry, cudaStream_t st) {
     const Dims d = g.d;
-    dim3 grid(d.pitch / 32, ceil_div(d.n + 1, 32), NFACE);
-    const real *bu = (const real *)w.btab[0], *bv = (const real *)w.btab[1];
+    if (!w.btabT) return CSADV_ERR_UNSUPPORTED;
+    const real *bu = (const real *)w.btab[0], *bvT = (const real *)w.btabT;
     const Clock *clk = (const Clock *)w.clock;
-    if (sizeof(real) == 4 && w.btabT) {
-        dim3 g2(d.pitch / 32, ceil_div(d.n + 1, 32), 2 * NFACE);
-        const float ch = (float)(dt * 0.5 / g.dx);
-        if (w.nbasis == 4)
-            k_wind_rec<4><<<g2, 256, 0, st>>>(d, (const float *)bu, (const float *)w.btabT, clk, (const float *)gpu,
-                                              (const float *)gpvT, (float2 *)erx, (float2 *)ery, o.dp == 2, ch);
-        else
-            k_wind_rec<1><<<g2, 256, 0, st>>>(d, (const float *)bu, (const float *)w.btabT, clk, (const float *)gpu,
-                                              (const float *)gpvT, (float2 *)erx, (float2 *)ery, o.dp == 2, ch);
-        CSADV_CUDA(cudaGetLastError());
-        return CSADV_OK;
-    }
+    dim3 g2(d.pitch / 32, ceil_div(d.n + 1, 32), 2 * NFACE);
+    const real ch = (real)(dt * 0.5 / g.dx), dtdx = (real)(dt / g.dx);
+    const long long cofs = record_coef_offset<real>(d);
+    UpwindMetric<real> mx{}, my{};
+    if (cofs) upwind_metrics<real>(o, d, gpu, gpvT, crx, cry, mx, my);
     if (w.nbasis == 4)
-        k_wind_step<real, 4, V><<<grid, dim3(32, 8), 0, st>>>(d, bu, bv, clk, gpu, gpvT, erx, ery, o.dp == 2,
-                                                               (real)(dt * 0.5), (real)g.dx);
+        k_wind_rec<real, 4><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my);
     else
-        k_wind_step<real, 1, V><<<grid, dim3(32, 8), 0, st>>>(d, bu, bv, clk, gpu, gpvT, erx, ery, o.dp == 2,
-                                                               (real)(dt * 0.5), (real)g.dx);
+        k_wind_rec<real, 1><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
 template int wind_step<double, double2>(const Options &, const Grid &, const Winds &, double, const double *,
-                                        const double *, double2 *, double2 *, cudaStream_t);
+                                        const double *, double2 *, double2 *, const void *, const void *, cudaStream_t);
 template int wind_step<float, float2>(const Options &, const Grid &, const Winds &, double, const float *,
-                                      const float *, float2 *, float2 *, cudaStream_t);
+                                      const float *, float2 *, float2 *, const void *, const void *, cudaStream_t);
 
 template <class W>
 static int sync_t(const Options &o, const Grid &g, const Winds &w, cudaStream_t st) {
@@ -1034,19 +1076,24 @@ int wind_sync(const Options &o, const Grid &g, const Winds &w, cudaStream_t st) 
 
 template <class real, class V>
 int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT,
-                   V *erx, V *ery, cudaStream_t st) {
+                   V *erx, V *ery, const void *crx, const void *cry, cudaStream_t st) {
     const Dims d = g.d;
     dim3 grid(d.pitch / 32, ceil_div(d.n + 1, 32), NFACE);
+    const long long cofs = record_coef_offset<real>(d);
+    UpwindMetric<real> mx{}, my{};
+    if (cofs) upwind_metrics<real>(o, d, gpu, gpvT, crx, cry, mx, my);
     k_wind_avgprep_t<real, V><<<grid, dim3(32, 8), 0, st>>>(d, (const real *)w.u_pu, (const real *)w.u_old,
                                                              (const real *)w.v_pv, (const real *)w.v_old, gpu, gpvT,
-                                                             erx, ery, o.dp == 2, (real)(dt * 0.5), (real)g.dx);
+                                                             erx, ery, o.dp == 2, (real)(dt * 0.5), (real)g.dx, cofs,
+                                                             (real)(dt / g.dx), mx, my);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
 template int wind_avgprep_t<double, double2>(const Options &, const Grid &, const Winds &, double, const double *,
-                                             const double *, double2 *, double2 *, cudaStream_t);
+                                             const double *, double2 *, double2 *, const void *, const void *,
+                                             cudaStream_t);
 template int wind_avgprep_t<float, float2>(const Options &, const Grid &, const Winds &, double, const float *,
-                                           const float *, float2 *, float2 *, cudaStream_t);
+                                           const float *, float2 *, float2 *, const void *, const void *, cudaStream_t);
 template int wind_avgprep<double>(const Options &, const Grid &, const Winds &, double, double *, double *, uint32_t *,
                                   uint32_t *, int, cudaStream_t);
 template int wind_avgprep<float>(const Options &, const Grid &, const Winds &, double, float *, float *, uint32_t *,
