@@ -10,16 +10,23 @@ Workload (the reference's scheme on the deformational-flow configuration):
   fixer, dt from CFL 0.5.  One step = both tracers advanced one time step (plus the
   wind update).  Metric: tracer cell-steps per second (6 N^2 x tracers per step).
 
-The headline line is the FP32 form (tracer state, PPM and fluxes in float32; geometry,
-winds, Lagrange weights, mass and error sums in float64); the FP64 ("plain") form of the
-same workload is reported in the same line.  Timed steps run as CUDA graphs; L2 is
-flushed (256 MB write) before every timed step and each step is timed alone with CUDA
-events on the launching stream.  N > 1 (torchrun): every rank runs an independent replica
-(the solve does not shard; "replicas only"), max time over ranks.
+The headline (`value`, `e2e`, `roofline`) is the FP64 ("plain") form, the reference's own
+arithmetic, so that it compares like for like with the reference arm.  The FP32 form
+(tracer state, PPM and fluxes in float32; geometry, winds, Lagrange weights, mass and error
+sums in float64) is the `fp32` sub-object, with its own end-to-end rate and HBM roofline.
+Timed steps run as CUDA graphs; L2 is flushed (256 MB write) before every timed step and each
+step is timed alone with CUDA events on the launching stream.  N > 1 (torchrun): every rank
+runs an independent replica (the solve does not shard; "replicas only"), max time over ranks.
 
---impl reference times the reference algorithm on the host cores: the CPU oracle (a
-numpy restatement of the reference, test infrastructure) advancing independent replicas of
-the same workload, one process per core, on a bounded number of steps.
+Further sub-objects: `accuracy` (one revolution at N = 48 and the deformational flow at
+N = 384 to t = T, FP64 and FP32, error norms against the exact solution), `batched` (256
+solves, 200 steps), `large` (N = 1536, 8 tracers, 500 steps), `serving` (the Poisson request
+stream) and `cpu_baseline` (the oracle on one host core).
+
+--impl reference times the reference algorithm on the host cores: the CPU oracle (a numpy
+restatement of the reference, test infrastructure) advancing one independent replica of the
+same workload per core, the same warm-up and timed step counts as the GPU arm, the aggregate
+taken over the replicas' common wall-clock window.
 """
 import argparse
 import json
@@ -45,9 +52,10 @@ METRIC = "tracer cell-steps/s"
 
 
 def workload_config():
+    """The workload only (identical in both arms); how each arm runs it is reported beside."""
     return {"workload": "deformational flow, N=384 (6x384^2 cells), 2 tracers, PPM-CW84 RK2 AVLT ET-DG MT-0 MF-PR, CFL 0.5",
             "N": N_CELLS, "tracers": NTRACERS, "cells_per_tracer": 6 * N_CELLS * N_CELLS,
-            "l2": "flushed (256 MB write) before every timed step", "execution": "CUDA graph per step"}
+            "wind": "deformational, k=0.48, T=5 (k = 2.4 R/T)", "ics": "cosine bells; smooth bells"}
 
 
 def dt_for_cfl(make_plan):
@@ -57,19 +65,41 @@ def dt_for_cfl(make_plan):
     return 1e-3 * CFL / c
 
 
-PROFILE = os.path.join(ROOT, "profiles", "k_sweep2_N384_T2.md")
+PROFILES = {32: os.path.join(ROOT, "profiles", "k_sweep2_N384_T2.md"),
+            64: os.path.join(ROOT, "profiles", "k_sweep_f64_N384_T2.md")}
+# the sources the step kernels are compiled from: a committed ncu summary states their digest,
+# and its figures are used only while the sources are unchanged
+KERNEL_SOURCES = ("sweep.cuh", "sweep2.cuh", "fused.cuh", "halo.cuh", "common.cuh", "tiles.h",
+                  "sweep_f32_pairs.cu", "sweep_f64.cu")
 
 
-def profiled(key):
-    """A figure of one launch of the step kernel on this workload from the committed ncu summary
-    (its `key = value` line, commas allowed); None when absent."""
+def kernel_digest():
+    import hashlib
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "py-cubed-sphere_gb300", "csrc", name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
+
+
+def profiled(precision, key):
+    """A figure of one launch of a step kernel on this workload from the committed ncu summary
+    (its `key = value` line, commas allowed).  None when absent, or when the summary was taken
+    from other kernel sources than the ones built (its `source_digest` line differs)."""
+    vals = {}
     try:
-        for ln in open(PROFILE):
-            if ln.strip().startswith(key + " ="):
-                return float(ln.split("=")[1].split()[0].replace(",", ""))
-    except (OSError, ValueError):
-        pass
-    return None
+        for ln in open(PROFILES[precision]):
+            if "=" in ln:
+                k, v = ln.split("=", 1)
+                vals[k.strip()] = v.split()[0].replace(",", "") if v.split() else ""
+    except OSError:
+        return None
+    if vals.get("source_digest") != kernel_digest() or key not in vals:
+        return None
+    try:
+        return float(vals[key])
+    except ValueError:
+        return None
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -195,7 +225,6 @@ def run_form(torch, precision, steps, warmup, flush, stream, world=1):
     pl.set_profiling(False)
     res = {"dt": dt, "ms_per_step": sum(ms) / steps, "ms_min": min(ms), "stats": st,
            "kernel_ms": pst["main_ms"] / max(pst["main_launches"], 1)}
-    res["errors_linf_l1_l2"] = pl.errors(ICS[0], pl.step * dt, tracer=0)
     pl.close()
     return res
 
@@ -250,12 +279,74 @@ def run_e2e(torch, precision, steps, stream, world=1):
     return sec, NTRACERS * nb_in, NTRACERS * nb_out
 
 
+# ----------------------------------------------------------------------------- accuracy runs
+def steps_to(Plan, N, vf, wp, tf, stream):
+    """(nsteps, dt): the fewest whole steps that end exactly at tf with CFL <= 0.5 (the
+    reference's CFL definition, advection_vars.py:89-98)."""
+    import math
+    with Plan(N, -CFL, vf=vf, wind_param=wp, stream=stream, **SCHEME) as pl:
+        n = int(math.ceil(tf / pl.dt - 1e-9))
+    return n, tf / n
+
+
+def run_to_end(Plan, N, dt, nsteps, vf, wp, ics, precision, stream):
+    """Error norms against the exact solution at the end time (advection_sphere.py:45-61,
+    errors.py:99-113), relative mass change and final fields of each tracer."""
+    with Plan(N, dt, vf=vf, wind_param=wp, ntracers=len(ics), precision=precision, stream=stream, **SCHEME) as pl:
+        for t, (ic, ip) in enumerate(ics):
+            pl.init_tracer(ic, ic_param=ip, tracer=t)
+        m0 = [pl.mass(t) for t in range(len(ics))]
+        t0 = time.perf_counter()
+        pl.advance(nsteps)
+        q = [pl.get_tracer(t) for t in range(len(ics))]
+        wall = time.perf_counter() - t0
+        errs = [pl.errors(ic, nsteps * dt, ic_param=ip, tracer=t) for t, (ic, ip) in enumerate(ics)]
+        dm = [abs(pl.mass(t) - m0[t]) / abs(m0[t]) for t in range(len(ics))]
+    return q, errs, dm, wall
+
+
+def run_accuracy(stream):
+    """Configurations 1 and 2 run to their end times in FP64 and FP32: one revolution of a
+    Gaussian hill (b0 = 5 at (0, 0)) in the solid-body wind at alpha = pi/4, N = 48; the cosine
+    bells and smooth bells in the deformational wind at N = 384 to t = T, where the exact
+    solution is the initial field.  FP32 is also compared with FP64 cell by cell."""
+    import math
+    import numpy as np
+    from csadv import Plan
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    out = {}
+    cases = (("revolution_N48", 48, 101, (math.pi / 4, 2 * math.pi / 5, 0.0, 0.0), [(101, (0.0, 0.0, 5.0, 0.0))],
+              "N=48, Gaussian hill b0=5 at (0,0), solid-body wind alpha=pi/4 u0=2pi/5, one revolution (t=T=5)"),
+             ("deformational_N384", N_CELLS, WIND, WIND_PARAM, [(ic, None) for ic in ICS],
+              "N=384, cosine bells and smooth bells, deformational wind k=0.48, to t=T=5 (exact = initial field)"))
+    for name, N, vf, wp, ics, desc in cases:
+        nsteps, dt = steps_to(Plan, N, vf, wp, 5.0, stream)
+        r = {}
+        for prec in (64, 32):
+            r[prec] = run_to_end(Plan, N, dt, nsteps, vf, wp, ics, prec, stream)
+        fmt = lambda v: [float("%.6e" % x) for x in v]  # noqa: E731
+        out[name] = {
+            "config": desc + ", PPM-CW84 RK2 AVLT ET-DG MT-0 MF-PR", "steps": nsteps, "dt": dt,
+            "fp64": {"linf_l1_l2": [fmt(e) for e in r[64][1]], "mass_change": [float("%.3e" % d) for d in r[64][2]],
+                     "wall_s": round(r[64][3], 3)},
+            "fp32": {"linf_l1_l2": [fmt(e) for e in r[32][1]], "mass_change": [float("%.3e" % d) for d in r[32][2]],
+                     "wall_s": round(r[32][3], 3),
+                     "max_diff_vs_fp64": [float("%.3e" % rel(a, b)) for a, b in zip(r[32][0], r[64][0])],
+                     "l2_vs_fp64_l2": [round(a[2] / b[2], 5) for a, b in zip(r[32][1], r[64][1])]},
+        }
+    return out
+
+
 # ----------------------------------------------------------------------------- batched and serving legs
 BATCH_SOLVES = 256
 BATCH_NS = (48, 96, 192, 384, 768)
+BATCH_STEPS = 200
 
 
-def batched_requests(n=BATCH_SOLVES, seed=0, steps=200):
+def batched_requests(n=BATCH_SOLVES, seed=0, steps=BATCH_STEPS):
     """256 independent FP32 solves: N uniform in {48, 96, 192, 384, 768}, 1-3 tracers of
     Gaussian hills (centres uniform on the sphere, width parameter uniform in [2, 10]),
     solid-body rotation at an angle uniform in [0, pi/2], CFL 0.5, 200 steps."""
@@ -274,10 +365,13 @@ def batched_requests(n=BATCH_SOLVES, seed=0, steps=200):
     return out
 
 
-def run_batched(torch, steps, warmup, stream, hbm):
-    """All 256 solves in one batch: one step-kernel launch per step for all of them, tile
-    shapes from the autotuner (one probe plan per distinct N and tracer count).  The resident
-    state (~10 GB) is far larger than L2, so no flush is needed between steps."""
+def run_batched(torch, warmup, stream, hbm):
+    """All 256 solves in one batch for their 200 steps: one step-kernel launch per step for all
+    of them, tile shapes from the autotuner (one probe plan per distinct N and tracer count).
+    The first `warmup` steps are untimed, the rest timed as one region.  The resident state
+    (~10 GB) is far larger than L2, so no flush is needed between steps.  At the end, each
+    solve's error norms against the exact rotated hills and its mass change."""
+    import numpy as np
     from csadv import Batch, serve, tune
     reqs = batched_requests()
     tiles = {}
@@ -289,22 +383,29 @@ def run_batched(torch, steps, warmup, stream, hbm):
     plans = [serve.make_plan(r, 32, 0.5, stream) for r in reqs]
     torch.cuda.synchronize()
     create_s = time.perf_counter() - t0
+    mass0 = [[pl.mass(t) for t in range(r.tracers)] for pl, r in zip(plans, reqs)]
     b = Batch(len(plans))
     for pl in plans:
         b.add(pl)
     b.advance(warmup, stream)
     torch.cuda.synchronize()
     b.reset_stats()
+    timed = BATCH_STEPS - warmup
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    b.advance(steps, stream)
+    b.advance(timed, stream)
     ev1.record(stream)
     torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / steps
+    ms = ev0.elapsed_time(ev1) / timed
     st = b.stats()
-    b.set_profiling(True)
+    l2, dm = [], []
+    for pl, r, m0 in zip(plans, reqs, mass0):
+        errs, d = serve.finish(pl, r, m0)
+        l2 += [e[2] for e in errs]
+        dm += d
+    b.set_profiling(True)  # after the 200 steps: these extra steps only time the step kernel
     b.reset_stats()
-    b.advance(max(3, steps // 4), stream)
+    b.advance(3, stream)
     pst = b.stats()
     b.set_profiling(False)
     kms = pst["main_ms"] / max(1, pst["main_launches"])
@@ -315,39 +416,51 @@ def run_batched(torch, steps, warmup, stream, hbm):
         pl.close()
     achieved = alg / (kms * 1e-3) / 1e9
     return {"value": round(cells / (ms * 1e-3), 1), "unit": "tracer cell-steps/s", "solves": len(reqs),
-            "ms_per_step": round(ms, 4), "kernels_per_step": st["kernels_per_step"],
+            "ms_per_step": round(ms, 4), "timed_steps": timed, "kernels_per_step": st["kernels_per_step"],
             "gpu_launches": st["kernel_launches"], "step_kernel_ms": round(kms, 4),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(achieved / hbm, 4), "alg_bytes_per_launch": alg},
             "plan_create_s": round(create_s, 2), "tiles": tiles,
+            "l2_error_median_max": [float("%.4e" % np.median(l2)), float("%.4e" % max(l2))],
+            "max_mass_change": float("%.3e" % max(dm)),
             "config": "256 solves, N in {48,96,192,384,768}, 1-3 tracers, solid-body wind at random angles, "
-                      "Gaussian hills, CFL 0.5, FP32 (timed: %d of the 200 steps)" % steps}
+                      "Gaussian hills, CFL 0.5, FP32, 200 steps (%d warm-up, %d timed); L2 errors against the "
+                      "exact rotated hills at the end" % (warmup, timed)}
 
 
-def run_large(torch, steps, warmup, stream, hbm):
+LARGE_STEPS = 500
+
+
+def run_large(torch, warmup, stream, hbm):
     """N = 1536 (6 x 1536^2 = 14.2 M cells per tracer), 8 FP32 tracers sharing one divergent
-    wind (solid body at alpha = pi/4 plus the 0.3 u0 divergent perturbation), CFL 0.7; the
-    timed steps are a sample of the 500-step run.  State ~3.6 GB, far above L2."""
+    wind (solid body at alpha = pi/4 plus the 0.3 u0 divergent perturbation), CFL 0.7, the
+    whole 500-step run: `warmup` steps untimed, the rest timed.  State ~3.6 GB, far above L2.
+    The divergent wind has no exact solution; mass (MF-PR) and the fields' range are reported."""
     import math
+    import numpy as np
     from csadv import Plan, tune
     N, T = 1536, 8
     kw = dict(vf=103, wind_param=(math.pi / 4, 2 * math.pi / 5, 0.3, 0.0), ntracers=T, precision=32,
               stream=stream, **SCHEME)
     pl = Plan(N, -0.7, **kw)
+    tile = tune(pl, reps=2, stream=stream)
     for t in range(T):
         lon = -math.pi + 2 * math.pi * t / T
         pl.init_tracer(101, ic_param=(lon, 0.3 * math.sin(3 * t), 5.0, 0.0), tracer=t)
-    tile = tune(pl, reps=2, stream=stream)
     m0 = [pl.mass(t) for t in range(T)]
+    hi0 = max(float(np.max(pl.get_tracer(t))) for t in range(T))
     pl.advance(warmup)
     torch.cuda.synchronize()
+    timed = LARGE_STEPS - warmup
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    pl.advance(steps)
+    pl.advance(timed)
     ev1.record(stream)
     torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / steps
-    pl.set_profiling(True)
+    ms = ev0.elapsed_time(ev1) / timed
+    dm = max(abs(pl.mass(t) - m0[t]) / abs(m0[t]) for t in range(T))
+    q = [pl.get_tracer(t) for t in range(T)]
+    pl.set_profiling(True)  # after the 500 steps
     pl.reset_stats()
     pl.advance(3)
     pst = pl.stats()
@@ -356,14 +469,16 @@ def run_large(torch, steps, warmup, stream, hbm):
     cells = T * 6 * N * N
     alg = 6 * N * N * (T * 2 * 4 + 3 * 4)
     achieved = alg / (kms * 1e-3) / 1e9
-    dm = max(abs(pl.mass(t) - m0[t]) / abs(m0[t]) for t in range(T))
     res = {"value": round(cells / (ms * 1e-3), 1), "unit": "tracer cell-steps/s", "ms_per_step": round(ms, 4),
-           "step_kernel_ms": round(kms, 4), "tile": tile, "cfl": round(pl.cfl, 4),
+           "timed_steps": timed, "step_kernel_ms": round(kms, 4), "tile": tile, "cfl": round(pl.cfl, 4),
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                         "frac": round(achieved / hbm, 4), "alg_bytes_per_launch": alg},
            "max_mass_change": float("%.3e" % dm),
-           "config": "N=1536, 8 FP32 tracers, solid body + 0.3 u0 divergent wind, CFL 0.7 (timed: %d of the "
-                     "500 steps)" % steps}
+           "min_max_at_end": [float("%.4e" % min(float(np.min(x)) for x in q)),
+                              float("%.4e" % max(float(np.max(x)) for x in q))],
+           "max_at_start": float("%.4e" % hi0),
+           "config": "N=1536, 8 FP32 tracers, solid body + 0.3 u0 divergent wind, CFL 0.7, 500 steps "
+                     "(%d warm-up, %d timed)" % (warmup, timed)}
     pl.close()
     return res
 
@@ -371,23 +486,36 @@ def run_large(torch, steps, warmup, stream, hbm):
 def run_serving(torch, nreq, stream, budget_gb=120.0):
     """The request loop on a seeded Poisson stream (200 req/s; N log-uniform in [32, 1024],
     steps uniform in [50, 2000], 1-4 tracers, solid-body or deformational wind 50/50, FP32,
-    120 GB budget), truncated to the first `nreq` requests."""
+    120 GB budget), its first `nreq` requests (the configuration's 10^4 by default)."""
+    import numpy as np
     from csadv import serve
     reqs = serve.poisson_requests(nreq, rate=200.0, seed=0)
     srv = serve.Server(budget_bytes=budget_gb * 1e9, precision=32, stream=stream)
-    _, summ = srv.run(reqs, realtime=True)
+    res, summ = srv.run(reqs, realtime=True)
     offered = sum(6 * r.N * r.N * r.tracers * r.steps for r in reqs) / max(reqs[-1].arrival, 1e-9)
-    return {"requests": summ["requests"], "failed": summ["failed"], "p50_latency_s": round(summ["p50_latency_s"], 3),
-            "p99_latency_s": round(summ["p99_latency_s"], 3), "value": round(summ["throughput"], 1),
-            "unit": "tracer cell-steps/s", "wall_s": round(summ["wall_s"], 2),
-            "offered_load": round(offered, 1), "peak_resident_gb": round(summ["peak_bytes"] / 1e9, 2),
-            "budget_gb": budget_gb, "max_mass_change": float("%.3e" % summ["max_mass_change"]),
-            "config": "Poisson 200 req/s, N log-uniform [32,1024], steps U[50,2000], 1-4 tracers, "
-                      "solid/deformational 50/50, FP32, first %d requests of the seeded stream" % nreq}
+    served = [r for r in res if r.error is None]
+    wait = np.array([r.admitted - r.arrival for r in served]) if served else np.zeros(1)
+    run = np.array([r.finished - r.admitted for r in served]) if served else np.zeros(1)
+    out = {"requests": summ["requests"], "failed": summ["failed"], "p50_latency_s": round(summ["p50_latency_s"], 3),
+           "p99_latency_s": round(summ["p99_latency_s"], 3),
+           "admission_wait_p50_p99_s": [round(float(np.percentile(wait, 50)), 3),
+                                        round(float(np.percentile(wait, 99)), 3)],
+           "on_gpu_p50_p99_s": [round(float(np.percentile(run, 50)), 3), round(float(np.percentile(run, 99)), 3)],
+           "value": round(summ["throughput"], 1), "unit": "tracer cell-steps/s", "wall_s": round(summ["wall_s"], 2),
+           "offered_load": round(offered, 1), "peak_resident_gb": round(summ["peak_bytes"] / 1e9, 2),
+           "budget_gb": budget_gb, "max_mass_change": float("%.3e" % summ["max_mass_change"]),
+           "batch_steps": summ["batch_steps"],
+           "config": "Poisson 200 req/s, N log-uniform [32,1024], steps U[50,2000], 1-4 tracers, "
+                     "solid/deformational 50/50, FP32, 120 GB budget, %d requests of the seeded stream" % nreq}
+    for k in ("membership_changes", "graph_builds", "graph_build_ms", "plan_build_s", "retire_s", "host_s"):
+        if k in summ:
+            out[k] = summ[k]
+    return out
 
 
-def cpu_sample(nsteps):
-    """The oracle (numpy restatement of the reference) on this host, one core."""
+def oracle_replica():
+    """The oracle (numpy restatement of the reference) on the bench workload: both tracers'
+    simulations on one grid, dt from CFL 0.5 as the GPU arm chooses it."""
     from oracle import cases, solver
     from oracle.grid import CubedSphere
     g = CubedSphere(N_CELLS)
@@ -400,14 +528,85 @@ def cpu_sample(nsteps):
         spec = cases.ICSpec(ic)
         q0 = spec(g.pc.lon[it], g.pc.lat[it])
         sims.append(solver.Simulation(g, dt, 5.0, 2, 2, *SCHEME.values(), ic_spec=spec, wind=wind, q0=q0))
-    t0 = time.perf_counter()
+    return sims
+
+
+def oracle_steps(sims, nsteps, k0=1):
+    from oracle import solver
     for s in sims:
-        solver.run_steps(s, nsteps)
+        solver.run_steps(s, nsteps, k0)
+
+
+def cpu_sample(nsteps):
+    """The oracle on this host, one core: tracer cell-steps/s over `nsteps` steps."""
+    sims = oracle_replica()
+    t0 = time.perf_counter()
+    oracle_steps(sims, nsteps)
     sec = time.perf_counter() - t0
     return NTRACERS * 6 * N_CELLS * N_CELLS * nsteps / sec
 
 
+def peaks_file():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def fp64_roofline(kms, fp64_flops, hbm):
+    """The FP64 step kernel against the FP64 pipe.  Its executed FP64 arithmetic instructions per
+    launch (DFMA + DADD + DMUL, each one issue of the pipe, from the committed ncu summary of this
+    kernel on this workload, used only while the kernel sources are unchanged) over its CUDA-event
+    launch time, against this GPU's DFMA issue rate measured here (csadv_fp64_rate / 2)."""
+    alg = 6 * N_CELLS * N_CELLS * (NTRACERS * 2 * 8 + 3 * 8)
+    inst = profiled(64, "fp64_inst_per_launch")
+    flops = profiled(64, "fp64_flops_per_launch")
+    hbm_gbs = alg / (kms * 1e-3) / 1e9
+    peak = fp64_flops / 2.0
+    roof = {"bound": "fp64", "kernel": "k_sweep<double, PPM-CW84, AVLT> (FP64 step kernel)", "unit": "T FP64 inst/s",
+            "peak": round(peak / 1e12, 4),
+            "peak_source": "csadv_fp64_rate (DFMA chains on every SM, measured here) / 2 flop per DFMA",
+            "achieved": None, "frac": None, "kernel_ms": round(kms, 5), "fp64_inst_per_launch": inst,
+            "fp64_flops_per_launch": flops, "traffic": None, "alg_bytes_per_launch": alg,
+            "hbm_gbs": round(hbm_gbs, 1), "hbm_frac": round(hbm_gbs / hbm, 4)}
+    tr = profiled(64, "dram_bytes_per_launch")
+    roof["traffic"] = int(tr) if tr else None
+    if inst and peak:
+        roof["achieved"] = round(inst / (kms * 1e-3) / 1e12, 4)
+        roof["frac"] = round(inst / (kms * 1e-3) / peak, 4)
+        if flops:
+            roof["achieved_tflops"] = round(flops / (kms * 1e-3) / 1e12, 4)
+    else:
+        roof["note"] = "no ncu summary for the current kernel sources: executed FP64 instructions unknown"
+    return roof
+
+
+def fp32_roofline(kms, hbm, peaks, mhz):
+    """The FP32 step kernel against HBM (algorithmic bytes over its CUDA-event launch time) and,
+    since it is bound by instruction issue, its warp instructions per launch (committed ncu
+    summary, current sources only) against 4 per SM per cycle at the sampled clock."""
+    alg = 6 * N_CELLS * N_CELLS * (NTRACERS * 2 * 4 + 3 * 4)
+    achieved = alg / (kms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_sweep2<PPM-CW84, AVLT> (paired-tracer FP32 step kernel)",
+            "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+            "traffic": None, "kernel_ms": round(kms, 5), "alg_bytes_per_launch": alg,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
+    tr = profiled(32, "dram_bytes_per_launch")
+    roof["traffic"] = int(tr) if tr else None
+    inst = profiled(32, "smsp__inst_executed.sum")
+    issue = None
+    if inst:
+        peak_issue = 152 * 4 * mhz * 1e6
+        issue = {"bound": "issue", "achieved": round(inst / (kms * 1e-3) / 1e12, 4),
+                 "peak": round(peak_issue / 1e12, 4), "unit": "T warp-inst/s",
+                 "frac": round(inst / (kms * 1e-3) / peak_issue, 4), "inst_per_launch": int(inst),
+                 "thread_inst_per_tracer_cell_step": profiled(32, "thread_inst_per_tracer_cell_step"),
+                 "source": "profiles/k_sweep2_N384_T2.md"}
+    return roof, issue
+
+
 def bench_gpu(args):
+    import ctypes
     import torch
     import __graft_entry__
     __graft_entry__.build()
@@ -424,80 +623,74 @@ def bench_gpu(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2 (129 MB)
 
     with ClockSampler(local) as clk:
+        f64 = run_form(torch, 64, args.steps, args.warmup, flush, stream, world)
         f32 = run_form(torch, 32, args.steps, args.warmup, flush, stream, world)
-    f64 = run_form(torch, 64, max(3, args.steps // 5), args.warmup, flush, stream, world)
-    e2e_sec, h2d, d2h = run_e2e(torch, 32, max(3, args.steps // 2), stream, world)
+    e64_sec, h2d64, d2h64 = run_e2e(torch, 64, max(3, args.steps // 2), stream, world)
+    e32_sec, h2d32, d2h32 = run_e2e(torch, 32, max(3, args.steps // 2), stream, world)
+    rate = ctypes.c_double()
+    _lib.check(_lib.lib().csadv_fp64_rate(512, ctypes.byref(rate), _lib.stream_handle(stream)), "csadv_fp64_rate")
 
-    ms, ms64, e2e_sec = max_over_ranks([f32["ms_per_step"], f64["ms_per_step"], e2e_sec], world)
+    ms64, ms32, e64_sec, e32_sec = max_over_ranks([f64["ms_per_step"], f32["ms_per_step"], e64_sec, e32_sec], world)
     cells = NTRACERS * 6 * N_CELLS * N_CELLS
-    value = job_rate(cells, world, ms)
     if rank != 0:
         return
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
+    peaks = peaks_file()
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # algorithmic bytes of one fused-kernel launch: per cell T*(read + write Q) + (u_avg, v_avg, g) once
-    s_q = 4
-    alg = 6 * N_CELLS * N_CELLS * (NTRACERS * 2 * s_q + 3 * 4)
-    kms = f32["kernel_ms"]
-    achieved = alg / (kms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_sweep2<PPM-CW84, AVLT> (paired-tracer FP32 step kernel)",
-            "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-            "traffic": None, "kernel_ms": round(kms, 5), "alg_bytes_per_launch": alg,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
-    tr = profiled("dram_bytes_per_launch")
-    roof["traffic"] = int(tr) if tr else None
-    # The kernel is bound by instruction issue (DRAM a few percent busy): its warp instructions per
-    # launch (ncu, committed summary) over the launch time, against 4 per SM per cycle at the
-    # clock sampled during the timed steps.
-    inst = profiled("smsp__inst_executed.sum")
     clk_s = clk.summary()
     mhz = clk_s.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    if inst:
-        peak_issue = 152 * 4 * mhz * 1e6
-        issue = {"bound": "issue", "achieved": round(inst / (kms * 1e-3) / 1e12, 4), "peak": round(peak_issue / 1e12, 4),
-                 "unit": "T warp-inst/s", "frac": round(inst / (kms * 1e-3) / peak_issue, 4),
-                 "inst_per_launch": int(inst), "source": "profiles/k_sweep2_N384_T2.md"}
-    else:
-        issue = None
+    roof64 = fp64_roofline(f64["kernel_ms"], rate.value, hbm)
+    roof32, issue32 = fp32_roofline(f32["kernel_ms"], hbm, peaks, mhz)
+    v64, v32 = job_rate(cells, world, ms64), job_rate(cells, world, ms32)
     line = {
-        "metric": METRIC, "value": round(value, 1), "unit": "tracer cell-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (analytic ICs and winds)",
-        "config": dict(workload_config(), parallelism="replicas" if world > 1 else "single GPU"),
-        "fp64": {"value": round(job_rate(cells, world, ms64), 1), "ms_per_step": round(ms64, 5),
-                 "kernel_ms": round(f64["kernel_ms"], 5), "dtype": "f64"},
-        "fp32_over_fp64": round(ms64 / ms, 2),
-        "e2e": {"value": round(job_rate(cells, world, e2e_sec * 1e3), 1), "unit": "tracer cell-steps/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(f32["stats"]["kernel_launches"]),
-        "kernels_per_step": int(f32["stats"]["kernels_per_step"]),
-        "roofline": roof,
-        "issue_roofline": issue,
+        "metric": METRIC, "value": round(v64, 1), "unit": "tracer cell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms64, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic ICs and winds)",
+        "config": workload_config(),
+        "timing": {"l2": "flushed (256 MB write) before every timed step", "execution": "CUDA graph per step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": round(job_rate(cells, world, e64_sec * 1e3), 1), "unit": "tracer cell-steps/s",
+                "h2d_bytes_per_step": h2d64, "d2h_bytes_per_step": d2h64},
+        "gpu_launches": int(f64["stats"]["kernel_launches"]),
+        "kernels_per_step": int(f64["stats"]["kernels_per_step"]),
+        "roofline": roof64,
         "clocks": clk_s,
-        "errors_fp32_linf_l1_l2_vs_exact": [float("%.4e" % e) for e in f32["errors_linf_l1_l2"]],
+        "fp32": {"value": round(v32, 1), "unit": "tracer cell-steps/s", "dtype": "f32", "ms_per_step": round(ms32, 5),
+                 "kernel_ms": round(f32["kernel_ms"], 5), "vs_fp64": round(ms64 / ms32, 2),
+                 "gpu_launches": int(f32["stats"]["kernel_launches"]),
+                 "kernels_per_step": int(f32["stats"]["kernels_per_step"]),
+                 "e2e": {"value": round(job_rate(cells, world, e32_sec * 1e3), 1), "unit": "tracer cell-steps/s",
+                         "h2d_bytes_per_step": h2d32, "d2h_bytes_per_step": d2h32},
+                 "roofline": roof32, "issue_roofline": issue32},
     }
+    if not args.no_accuracy:
+        line["accuracy"] = run_accuracy(stream)
     if not args.no_batched:
-        line["batched"] = run_batched(torch, args.batched_steps, args.warmup, stream, hbm)
-        line["batched"]["vs_fp64_single"] = round(line["batched"]["value"] / line["fp64"]["value"], 2)
+        line["batched"] = run_batched(torch, args.warmup, stream, hbm)
+        line["batched"]["vs_fp64_single"] = round(line["batched"]["value"] / v64, 2)
     if not args.no_large:
-        line["large"] = run_large(torch, args.large_steps, args.warmup, stream, hbm)
+        line["large"] = run_large(torch, args.warmup, stream, hbm)
     if args.serve_requests > 0:
         line["serving"] = run_serving(torch, args.serve_requests, stream)
     if world == 1 and not args.no_cpu:
         k = 2
         line["cpu_baseline"] = {"value": round(cpu_sample(k), 1), "unit": "tracer cell-steps/s", "cores": 1,
-                                "kind": "port", "sample": "oracle, N=384, 2 tracers, %d steps" % k}
+                                "kind": "port", "sample": "oracle (numpy restatement of the reference, FP64), "
+                                                          "N=384, 2 tracers, %d steps on one core" % k}
     print(json.dumps(line))
 
 
 # ----------------------------------------------------------------------------- reference arm
-def _ref_worker(args):
-    nsteps, = args
-    return cpu_sample(nsteps)
+def _ref_replica(warmup, steps, barrier, results):
+    """One replica on one core: build, `warmup` steps, then the `steps` timed steps between two
+    barriers shared by all replicas; reports its window on the system-wide monotonic clock."""
+    sims = oracle_replica()
+    oracle_steps(sims, warmup)
+    barrier.wait()
+    t0 = time.monotonic()
+    oracle_steps(sims, steps, warmup + 1)
+    t1 = time.monotonic()
+    barrier.wait()
+    results.put((t0, t1))
 
 
 def bench_reference(args):
@@ -506,28 +699,33 @@ def bench_reference(args):
         return
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    nsteps = 1
-    timed = max(1, min(args.steps, 3))
     ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        pool.map(_ref_worker, [(1,)] * cores)  # warm-up: imports, grid, first step
-        t1 = time.perf_counter()
-        rates = []
-        for _ in range(timed):
-            rates.append(sum(pool.map(_ref_worker, [(nsteps,)] * cores)))
-    value = sorted(rates)[len(rates) // 2]
+    barrier = ctx.Barrier(cores)
+    results = ctx.Queue()
+    t_start = time.perf_counter()
+    procs = [ctx.Process(target=_ref_replica, args=(args.warmup, args.steps, barrier, results)) for _ in range(cores)]
+    for p in procs:
+        p.start()
+    windows = [results.get() for _ in procs]
+    for p in procs:
+        p.join()
+    window = max(w[1] for w in windows) - min(w[0] for w in windows)
     cells = NTRACERS * 6 * N_CELLS * N_CELLS
+    value = cores * cells * args.steps / window
     line = {"metric": METRIC, "value": round(value, 1), "unit": "tracer cell-steps/s", "impl": "reference",
-            "n_gpus": 0, "steps": timed, "warmup": 1, "ms_per_step": round(cores * cells / value * 1e3, 3),
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(window / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (analytic ICs and winds)", "config": workload_config(),
+            "timing": {"execution": "oracle (numpy restatement of the reference), one independent replica per host "
+                                    "core, all replicas' timed steps inside one common wall-clock window"},
             "cpu_baseline": {"value": round(value, 1), "unit": "tracer cell-steps/s", "cores": cores, "kind": "port",
-                             "sample": "oracle (numpy restatement of the reference), N=384, 2 tracers; one independent "
-                                       "replica per core, %d step(s) each, median of %d" % (nsteps, timed)},
+                             "sample": "oracle (numpy restatement of the reference, FP64), N=384, 2 tracers; %d "
+                                       "replicas (one per core), %d warm-up + %d timed steps each; cells of all "
+                                       "replicas over the window from the first start to the last end"
+                                       % (cores, args.warmup, args.steps)},
             "e2e": {"value": round(value, 1), "unit": "tracer cell-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "wall_s": round(time.perf_counter() - t0, 1)}
+            "wall_s": round(time.perf_counter() - t_start, 1)}
     print(json.dumps(line))
 
 
@@ -538,11 +736,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="csadv", choices=("csadv", "reference"))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the runs to the end times")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-solve batched leg")
-    ap.add_argument("--batched-steps", type=int, default=20, help="timed steps of the batched leg")
     ap.add_argument("--no-large", action="store_true", help="skip the N=1536, 8-tracer leg")
-    ap.add_argument("--large-steps", type=int, default=20, help="timed steps of the N=1536 leg")
-    ap.add_argument("--serve-requests", type=int, default=100,
+    ap.add_argument("--serve-requests", type=int, default=10000,
                     help="run the serving leg on the first N requests of the seeded stream (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
