@@ -490,7 +490,9 @@ def run_serving(torch, nreq, stream, budget_gb=120.0):
     import numpy as np
     from csadv import serve
     reqs = serve.poisson_requests(nreq, rate=200.0, seed=0)
-    srv = serve.Server(budget_bytes=budget_gb * 1e9, precision=32, stream=stream)
+    # the loop on its own non-blocking streams: plans are built and read out beside the step loop
+    srv = serve.Server(budget_bytes=budget_gb * 1e9, precision=32, stream=torch.cuda.Stream(),
+                       build_stream=torch.cuda.Stream(), device=torch.cuda.current_device())
     res, summ = srv.run(reqs, realtime=True)
     offered = sum(6 * r.N * r.N * r.tracers * r.steps for r in reqs) / max(reqs[-1].arrival, 1e-9)
     served = [r for r in res if r.error is None]
@@ -507,7 +509,7 @@ def run_serving(torch, nreq, stream, budget_gb=120.0):
            "batch_steps": summ["batch_steps"],
            "config": "Poisson 200 req/s, N log-uniform [32,1024], steps U[50,2000], 1-4 tracers, "
                      "solid/deformational 50/50, FP32, 120 GB budget, %d requests of the seeded stream" % nreq}
-    for k in ("membership_changes", "graph_builds", "graph_build_ms", "plan_build_s", "retire_s", "host_s"):
+    for k in ("membership_changes", "graph_builds", "graph_build_ms", "plan_build_s", "release_s"):
         if k in summ:
             out[k] = summ[k]
     return out

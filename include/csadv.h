@@ -202,6 +202,9 @@ typedef struct csadv_stats {
     int tile;                   /* fused tile configuration in use (1..8, as csadv_options.tile), 0 for staged */
     int reserved;
     size_t device_bytes;        /* device memory held by the plan (with its grid, which plans of one N share) */
+    long long graph_builds;     /* step graphs captured and instantiated (a batch: one per membership change
+                                   and buffer parity) */
+    double graph_build_ms;      /* host time spent capturing and instantiating them */
 } csadv_stats;
 int csadv_get_stats(csadv_plan *plan, csadv_stats *out);
 int csadv_reset_stats(csadv_plan *plan);

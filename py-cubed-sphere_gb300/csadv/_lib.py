@@ -50,6 +50,7 @@ class Stats(ctypes.Structure):
         ("steps", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong), ("main_launches", ctypes.c_longlong),
         ("main_ms", ctypes.c_double), ("kernels_per_step", ctypes.c_int), ("engine", ctypes.c_int),
         ("tile", ctypes.c_int), ("reserved", ctypes.c_int), ("device_bytes", ctypes.c_size_t),
+        ("graph_builds", ctypes.c_longlong), ("graph_build_ms", ctypes.c_double),
     ]
 
 

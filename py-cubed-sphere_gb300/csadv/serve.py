@@ -124,20 +124,37 @@ def plane_elems(N):
 class Server:
     """The request loop.  budget_bytes bounds the device memory of resident solves.
 
+    With `stream` and `build_stream` given (two non-blocking CUDA streams; `threads` True by
+    default then), plans are made and read off the step loop: `builders` threads create the plans
+    of admitted requests (grid, winds, initial conditions, on `build_stream`) while the batch
+    steps, and a retirement thread reads a finished solve's error norms and mass on `stream`, after
+    its last step.  A plan joins the batch at the first step boundary after it is ready; when
+    nothing is resident, the requests admitted together are awaited and start together.  Freeing a
+    plan's device memory waits for the whole device, so released plans are destroyed by the loop
+    itself, between steps, in groups (when their memory is needed for an admission, or every
+    `release_s` seconds).  Without the two streams everything runs inline on `stream`.
+
     Failures stay with their request: a request whose plan cannot be made (bad size, no
     memory), whose state turns non-finite, or that waits past its deadline gets a Result with
-    `error` set and no cell-steps; the loop carries on with the others."""
+    `error` set and no cell-steps; the loop carries on with the others.  Deadlines are checked
+    for every queued request at every step boundary, not only for the head of the queue."""
 
     def __init__(self, budget_bytes, precision=32, cfl=0.5, max_active=512, stream=None, clock=time.perf_counter,
-                 keep_state=False, max_steps_per_tick=8):
+                 keep_state=False, max_steps_per_tick=8, threads=None, build_stream=None, device=None, builders=2,
+                 release_s=0.5):
         self.budget = int(budget_bytes)
         self.precision = precision
         self.cfl = cfl
         self.max_active = max_active
         self.stream = stream
+        self.build_stream = build_stream
+        self.device = device
         self.clock = clock
         self.keep_state = keep_state
         self.max_steps_per_tick = max_steps_per_tick
+        self.threads = (stream is not None and build_stream is not None) if threads is None else bool(threads)
+        self.builders = builders
+        self.release_s = release_s
         self._coef = {}
 
     # device bytes of a plan ~ plane elements x (a + b T), per wind kind; measured once
@@ -153,11 +170,49 @@ class Server:
         a, b = self._coef[key]
         return int(plane_elems(req.N) * (a + b * req.tracers) * 1.02) + (1 << 20)
 
+    def _thread_init(self):
+        if self.device is not None:
+            L.check(L.lib().csadv_set_device(int(self.device)), "csadv_set_device")
+
+    def _build(self, req):
+        """The plan of one request with its initial conditions in place (its mass read back, which
+        waits for the build stream); its later work runs on the loop's stream."""
+        t0 = time.perf_counter()
+        stream = self.build_stream if self.threads else self.stream
+        pl = make_plan(req, self.precision, self.cfl, stream)
+        try:
+            mass0 = [pl.mass(t) for t in range(req.tracers)]
+            nbytes = pl.stats()["device_bytes"]
+        except Exception:
+            pl.close()
+            raise
+        pl.stream = L.stream_handle(self.stream)
+        return pl, mass0, nbytes, time.perf_counter() - t0
+
+    def _retire(self, pl, req, admitted, mass0, t0, realtime):
+        """Result of a finished solve (error norms, mass change, optionally its fields), read on
+        the loop's stream after the solve's last step."""
+        try:
+            errs, dm = finish(pl, req, mass0)  # synchronises the plan's stream
+            failed = None
+        except L.CsadvError as e:  # e.g. a non-finite state: this request only
+            errs, dm, failed = [], [], str(e)
+        state = [pl.get_tracer(t) for t in range(req.tracers)] if self.keep_state else None
+        fin = self.clock() - t0
+        res = Result(req.rid, req.N, req.tracers, req.steps, req.arrival if realtime else 0.0, admitted, fin, errs,
+                     dm, 0 if failed else 6 * req.N * req.N * req.tracers * req.steps, error=failed)
+        res.state = state
+        return res
+
     def run(self, requests, realtime=True, on_step=None):
         """Serve `requests` (sorted by arrival).  realtime: arrivals follow the wall clock;
         otherwise every request is available at once.  Returns (results, summary)."""
+        import concurrent.futures as cf
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         queue = collections.deque()
+        building = collections.deque()  # [req, future, bytes reserved]
+        retiring = []                     # [future of Result, plan, bytes]
+        released = []                     # [plan, bytes]: read out, memory not yet freed
         active = {}      # id(plan) -> [plan, req, remaining, admitted, mass0, bytes]
         used = 0
         results = []
@@ -165,35 +220,98 @@ class Server:
         t0 = self.clock()
         steps = 0
         peak = 0
+        members_changed = 0
+        build_s = 0.0
+        release_s = 0.0
+        last_release = time.perf_counter()
+        builder = retirer = None
+        if self.threads:
+            builder = cf.ThreadPoolExecutor(max_workers=self.builders, initializer=self._thread_init)
+            retirer = cf.ThreadPoolExecutor(max_workers=1, initializer=self._thread_init)
+
+        def run_inline(fn, *a):
+            f = cf.Future()
+            try:
+                f.set_result(fn(*a))
+            except BaseException as e:  # noqa: B902 -- delivered like a worker's exception
+                f.set_exception(e)
+            return f
+
+        def collect_retired(block=False):
+            keep = []
+            for item in retiring:
+                if block or item[0].done():
+                    results.append(item[0].result())
+                    released.append(item[1:])
+                else:
+                    keep.append(item)
+            retiring[:] = keep
+
+        def release():  # free the memory of plans that have been read out (waits for the device)
+            nonlocal used, release_s, last_release
+            tr = time.perf_counter()
+            for pl, nbytes in released:
+                pl.close()
+                used -= nbytes
+            released.clear()
+            release_s += time.perf_counter() - tr
+            last_release = time.perf_counter()
+
         try:
-            while pending or queue or active:
+            while pending or queue or building or active or retiring or released:
                 now = self.clock() - t0
                 while pending and (not realtime or pending[0].arrival <= now):
                     queue.append(pending.popleft())
-                while queue and len(active) < self.max_active:
+                collect_retired()
+                if released and (time.perf_counter() - last_release > self.release_s or not (active or building)):
+                    release()
+                # admission deadlines, for every queued request
+                if any(r.deadline is not None for r in queue):
+                    keep = collections.deque()
+                    for req in queue:
+                        waited = now - (req.arrival if realtime else 0.0)
+                        if req.deadline is not None and waited > req.deadline:
+                            results.append(self._failed(req, realtime, t0, "not admitted within %.3g s" % req.deadline))
+                        else:
+                            keep.append(req)
+                    queue = keep
+                # admission by memory budget, in arrival order: reserve the estimate, build beside the loop
+                while queue and len(active) + len(building) < self.max_active:
                     req = queue[0]
-                    waited = now - (req.arrival if realtime else 0.0)
-                    if req.deadline is not None and waited > req.deadline:
-                        queue.popleft()
-                        results.append(self._failed(req, realtime, t0, "not admitted within %.3g s" % req.deadline))
-                        continue
                     need = self.estimate(req)
-                    if used + need > self.budget and active:
+                    if used + need > self.budget and released:
+                        release()
+                    if used + need > self.budget and (active or building or retiring):
                         break
                     queue.popleft()
+                    used += need
+                    fut = builder.submit(self._build, req) if builder else run_inline(self._build, req)
+                    building.append([req, fut, need])
+                # plans that are ready join the batch at this step boundary
+                if building and not active:  # nothing to step: the requests admitted together start together
+                    cf.wait([b[1] for b in building], return_when=cf.ALL_COMPLETED)
+                still = collections.deque()
+                for req, fut, need in building:
+                    if not fut.done():
+                        still.append([req, fut, need])
+                        continue
                     try:
-                        pl = make_plan(req, self.precision, self.cfl, self.stream)
+                        pl, mass0, nbytes, bs = fut.result()
                     except L.CsadvError as e:
+                        used -= need
                         results.append(self._failed(req, realtime, t0, str(e)))
                         continue
-                    nbytes = pl.stats()["device_bytes"]
-                    mass0 = [pl.mass(t) for t in range(req.tracers)]
+                    build_s += bs
+                    used += nbytes - need
                     batch.add(pl)
+                    members_changed += 1
                     active[id(pl)] = [pl, req, req.steps, self.clock() - t0, mass0, nbytes]
-                    used += nbytes
+                building = still
                 peak = max(peak, used)
                 if not active:
-                    if pending and realtime:
+                    if retiring:
+                        cf.wait([r[0] for r in retiring], return_when=cf.FIRST_COMPLETED)
+                    elif pending and realtime and not queue and not building:
                         time.sleep(max(0.0, min(0.01, pending[0].arrival - (self.clock() - t0))))
                     continue
                 k = min(v[2] for v in active.values())
@@ -210,23 +328,36 @@ class Server:
                 for key in done:
                     pl, req, _, admitted, mass0, nbytes = active.pop(key)
                     batch.remove(pl)
-                    try:
-                        errs, dm = finish(pl, req, mass0)  # synchronises the plan's stream
-                        failed = None
-                    except L.CsadvError as e:  # e.g. a non-finite state: this request only
-                        errs, dm, failed = [], [], str(e)
-                    fin = self.clock() - t0
-                    res = Result(req.rid, req.N, req.tracers, req.steps, req.arrival if realtime else 0.0, admitted,
-                                 fin, errs, dm, 0 if failed else 6 * req.N * req.N * req.tracers * req.steps,
-                                 error=failed)
-                    if self.keep_state:
-                        res.state = [pl.get_tracer(t) for t in range(req.tracers)]
-                    results.append(res)
-                    pl.close()
-                    used -= nbytes
+                    members_changed += 1
+                    args = (pl, req, admitted, mass0, t0, realtime)
+                    fut = retirer.submit(self._retire, *args) if retirer else run_inline(self._retire, *args)
+                    retiring.append([fut, pl, nbytes])
+            collect_retired(block=True)
+            release()
         finally:
+            for req, fut, need in building:
+                try:
+                    fut.result()[0].close()
+                except Exception:
+                    pass
             for v in active.values():
                 v[0].close()
+            for item in retiring:
+                try:
+                    item[0].result()
+                except Exception:
+                    pass
+                item[1].close()
+            for pl, _ in released:
+                pl.close()
+            if builder:
+                builder.shutdown(wait=True)
+            if retirer:
+                retirer.shutdown(wait=True)
+            graph_builds, graph_ms = 0, 0.0
+            if hasattr(batch, "stats"):
+                st = batch.stats()
+                graph_builds, graph_ms = st.get("graph_builds", 0), round(st.get("graph_build_ms", 0.0), 1)
             batch.close()
         wall = self.clock() - t0
         served = [r for r in results if r.error is None]
@@ -237,6 +368,8 @@ class Server:
                    "throughput": cs / wall if wall > 0 else 0.0,
                    "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                    "batch_steps": steps, "peak_bytes": peak, "budget_bytes": self.budget,
+                   "membership_changes": members_changed, "plan_build_s": round(build_s, 3),
+                   "release_s": round(release_s, 3), "graph_builds": graph_builds, "graph_build_ms": graph_ms,
                    "max_mass_change": max((max(r.mass_change) for r in served), default=0.0)}
         return results, summary
 

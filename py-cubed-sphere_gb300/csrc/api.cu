@@ -3,6 +3,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <chrono>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -255,6 +256,7 @@ int run_step(csadv_plan *pl, int kind, cudaStream_t st) {
     const int par = pl->cur;
     const bool use_graph = pl->graphs && !pl->prof;  // profiled steps launch directly (events on the stream)
     if (use_graph && !pl->gexec[kind][par]) {
+        const auto tb = std::chrono::steady_clock::now();
         if (!pl->cap) CSADV_CUDA(cudaStreamCreateWithFlags(&pl->cap, cudaStreamNonBlocking));
         CSADV_CUDA(cudaStreamBeginCapture(pl->cap, cudaStreamCaptureModeThreadLocal));
         int rc = step_work(pl, kind, pl->cap);
@@ -275,6 +277,9 @@ int run_step(csadv_plan *pl, int kind, cudaStream_t st) {
                 pl->graphs = false;
             }
         }
+        pl->stats.graph_builds += 1;
+        pl->stats.graph_build_ms +=
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
     }
     if (use_graph && pl->graphs && pl->gexec[kind][par]) {
         CSADV_CUDA(cudaGraphLaunch(pl->gexec[kind][par], st));

@@ -13,6 +13,7 @@
 // tile configuration is the same.
 #include <algorithm>
 #include <map>
+#include <chrono>
 #include <mutex>
 #include <new>
 #include <tuple>
@@ -185,6 +186,7 @@ int batch_run_step(csadv_batch *b, int kind, cudaStream_t st) {
     const int ph = b->phase;
     const bool use_graph = b->graphs && !b->prof;
     if (use_graph && !b->gexec[ph]) {
+        const auto tb = std::chrono::steady_clock::now();
         if (!b->cap) CSADV_CUDA(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
         CSADV_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
         int rc = batch_step_work(b, kind, b->cap);
@@ -204,6 +206,9 @@ int batch_run_step(csadv_batch *b, int kind, cudaStream_t st) {
                 b->graphs = false;
             }
         }
+        b->stats.graph_builds += 1;
+        b->stats.graph_build_ms +=
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
     }
     if (use_graph && b->graphs && b->gexec[ph]) {
         CSADV_CUDA(cudaGraphLaunch(b->gexec[ph], st));

@@ -95,3 +95,23 @@ def test_failed_requests_stay_with_their_request():
         assert got.error is None
         for a, b in zip(got.state, alone(req, 32)):
             np.testing.assert_array_equal(a, b)
+
+
+def test_threaded_loop_on_own_streams_identical_to_alone():
+    """Plans made by builder threads on their own stream and read out by the retirement thread:
+    every request's fields are the same bits as run alone, FP32 and FP64, with arrivals in real
+    time and all at once."""
+    import torch
+    from csadv import serve
+    reqs = small_stream(n=12, seed=9)
+    for precision, realtime in ((32, True), (64, False)):
+        srv = serve.Server(budget_bytes=8 << 30, precision=precision, keep_state=True, max_steps_per_tick=5,
+                           stream=torch.cuda.Stream(), build_stream=torch.cuda.Stream())
+        assert srv.threads
+        results, summary = srv.run(reqs, realtime=realtime)
+        assert summary["requests"] == len(reqs) and summary["failed"] == 0
+        assert summary["graph_builds"] >= 1
+        by_id = {r.rid: r for r in results}
+        for req in reqs:
+            for a, b in zip(by_id[req.rid].state, alone(req, precision)):
+                np.testing.assert_array_equal(a, b)
