@@ -431,7 +431,7 @@ def run_batched(torch, warmup, stream, hbm):
 LARGE_STEPS = 500
 
 
-def run_large(torch, warmup, stream, hbm):
+def run_large(torch, warmup, stream, hbm, total=LARGE_STEPS):
     """N = 1536 (6 x 1536^2 = 14.2 M cells per tracer), 8 FP32 tracers sharing one divergent
     wind (solid body at alpha = pi/4 plus the 0.3 u0 divergent perturbation), CFL 0.7, the
     whole 500-step run: `warmup` steps untimed, the rest timed.  State ~3.6 GB, far above L2.
@@ -451,7 +451,7 @@ def run_large(torch, warmup, stream, hbm):
     hi0 = max(float(np.max(pl.get_tracer(t))) for t in range(T))
     pl.advance(warmup)
     torch.cuda.synchronize()
-    timed = LARGE_STEPS - warmup
+    timed = total - warmup
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     pl.advance(timed)
@@ -477,8 +477,8 @@ def run_large(torch, warmup, stream, hbm):
            "min_max_at_end": [float("%.4e" % min(float(np.min(x)) for x in q)),
                               float("%.4e" % max(float(np.max(x)) for x in q))],
            "max_at_start": float("%.4e" % hi0),
-           "config": "N=1536, 8 FP32 tracers, solid body + 0.3 u0 divergent wind, CFL 0.7, 500 steps "
-                     "(%d warm-up, %d timed)" % (warmup, timed)}
+           "config": "N=1536, 8 FP32 tracers, solid body + 0.3 u0 divergent wind, CFL 0.7, %d steps "
+                     "(%d warm-up, %d timed)" % (total, warmup, timed)}
     pl.close()
     return res
 
@@ -623,6 +623,11 @@ def bench_gpu(args):
     _lib.check(_lib.lib().csadv_set_device(local))
     stream = torch.cuda.current_stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2 (129 MB)
+    if args.large_only:  # profiling aid: the N=1536 leg alone, `--large-steps` steps
+        peaks = peaks_file()
+        print(json.dumps({"large": run_large(torch, args.warmup, stream, peaks.get("hbm_gbs", 6800.0),
+                                             args.large_steps)}))
+        return
 
     with ClockSampler(local) as clk:
         f64 = run_form(torch, 64, args.steps, args.warmup, flush, stream, world)
@@ -670,7 +675,7 @@ def bench_gpu(args):
         line["batched"] = run_batched(torch, args.warmup, stream, hbm)
         line["batched"]["vs_fp64_single"] = round(line["batched"]["value"] / v64, 2)
     if not args.no_large:
-        line["large"] = run_large(torch, args.warmup, stream, hbm)
+        line["large"] = run_large(torch, args.warmup, stream, hbm, args.large_steps)
     if args.serve_requests > 0:
         line["serving"] = run_serving(torch, args.serve_requests, stream)
     if world == 1 and not args.no_cpu:
@@ -741,6 +746,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the runs to the end times")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-solve batched leg")
     ap.add_argument("--no-large", action="store_true", help="skip the N=1536, 8-tracer leg")
+    ap.add_argument("--large-only", action="store_true", help="run only the N=1536 leg (profiling aid)")
+    ap.add_argument("--large-steps", type=int, default=LARGE_STEPS, help="steps of the N=1536 run")
     ap.add_argument("--serve-requests", type=int, default=10000,
                     help="run the serving leg on the first N requests of the seeded stream (0: skip)")
     args = ap.parse_args()
