@@ -66,23 +66,17 @@ struct Pred<double> {
     }
     __device__ static __forceinline__ bool prod_nonpos(double x, double y) { return !prod_pos(x, y); }
     __device__ static __forceinline__ bool abs_lt(double x, double y) { return (b(x) & MAG) < (b(y) & MAG); }
-    __device__ static __forceinline__ double min_nonneg(double x, double y) { return b(x) < b(y) ? x : y; }
+    __device__ static __forceinline__ double min_nonneg(double x, double y) {
+        return __longlong_as_double(b(x) < b(y) ? b(x) : b(y));
+    }
     __device__ static __forceinline__ bool gt_nonneg(double p, double d) { return b(p) > b(d); }
     __device__ static __forceinline__ bool lt_neg(double p, double d) { return b(p) < 0 && (b(p) & MAG) > b(d); }
 };
 
 // FP64 helpers on the integer pipe.  GB300 issues FP64 arithmetic at 1/64 of the FP32 rate, so
 // the FP64 kernel moves every operation that needs no FP64 rounding off the FP64 pipe: absolute
-// values and sign transfers on the sign bit, exact scalings by powers of two on the exponent
-// field, orderings on the bit patterns.
-__device__ __forceinline__ double iabs(double x) {
-    return __hiloint2double(__double2hiint(x) & 0x7fffffff, __double2loint(x));
-}
-// |v| with the sign of a
-__device__ __forceinline__ double icopysign(double v, double a) {
-    return __hiloint2double((__double2hiint(v) & 0x7fffffff) | (__double2hiint(a) & (int)0x80000000),
-                            __double2loint(v));
-}
+// values, sign transfers and selections on the bit patterns, exact scalings by powers of two on
+// the exponent field, orderings of the bit patterns.
 // x 2^K, equal to the FP64 product whenever that is a normal number (every value of an advected
 // field); results below the normal range become a zero of x's sign, and x is returned unchanged
 // when it is infinite, NaN or so large (> 2^1022) that the product would overflow
@@ -96,6 +90,11 @@ __device__ __forceinline__ double pow2_scale(double x) {
     const int hi2 = in ? hi + K * (1 << 20) : (tiny ? (hi & (int)0x80000000) : hi);
     return __hiloint2double(hi2, tiny ? 0 : lo);
 }
+// c ? a : b on the bit patterns (integer selects; no FP64 instruction)
+__device__ __forceinline__ double dsel(bool c, double a, double b) {
+    return __longlong_as_double(c ? __double_as_longlong(a) : __double_as_longlong(b));
+}
+__device__ __forceinline__ float dsel(bool c, float a, float b) { return c ? a : b; }
 // x as a signed integer key whose order is the floating-point order of finite values (+0 and -0
 // equal)
 __device__ __forceinline__ long long order_key(double x) {
@@ -177,11 +176,22 @@ __device__ __forceinline__ real ppm0_edge(real qam, real qa, real qb, real qbp) 
 // edge value 0.5 (qa + qb) - (sb - sa)/6; the limiter (reconstruction_1d.py:102-153) with the
 // monotonicity test as an ordering of the bit patterns (R - qc and qc - L have the signs of
 // those comparisons) and the flattened case's DL = 0, mid = 0 selected.
+// |x| 2^K on the bit pattern m = |x| (as pow2_scale): the magnitudes of the slope stay integers
+// from the subtractions to the result, so no step of it can become an FP64 instruction
+template <int K>
+__device__ __forceinline__ long long mag_scale(long long m) {
+    const int e = (int)(m >> 52);
+    constexpr int EMIN = K < 0 ? 1 - K : 1, EMAX = K > 0 ? 0x7fe - K : 0x7fe;
+    return (e >= EMIN && e <= EMAX) ? m + ((long long)K << 52) : (e < EMIN ? 0LL : m);
+}
 __device__ __forceinline__ double cw84_slope_d(double a, double b, double c) {
     using B = Pred<double>;
-    const double m = B::min_nonneg(iabs(b), iabs(c));
-    const double v = B::min_nonneg(pow2_scale<-1>(iabs(a)), pow2_scale<1>(m));
-    return B::prod_pos(b, c) ? icopysign(v, a) : 0.0;
+    constexpr long long MAG = 0x7fffffffffffffffLL;
+    const long long ka = B::b(a), kb = B::b(b) & MAG, kc = B::b(c) & MAG;
+    const long long m = mag_scale<1>(kb < kc ? kb : kc);
+    const long long h = mag_scale<-1>(ka & MAG);
+    const long long v = (h < m ? h : m) | (ka & ~MAG);
+    return __longlong_as_double(B::prod_pos(b, c) ? v : 0LL);
 }
 __device__ __forceinline__ double cw84_edge_d(double qa, double qb, double sa, double sb) {
     return fma(-(sb - sa), 1.0 / 6.0, pow2_scale<-1>(qb + qa));
@@ -189,21 +199,21 @@ __device__ __forceinline__ double cw84_edge_d(double qa, double qb, double sa, d
 __device__ __forceinline__ void cw84_limit_d(double qc, double &L, double &R) {
     using B = Pred<double>;
     const double dq = R - L, RpL = R + L;
-    const double q3 = 3.0 * qc;
+    const double q3 = fma(2.0, qc, qc);  // 3 qc, one rounding
     const double q6 = fma(-3.0, RpL, pow2_scale<1>(q3));
     const long long kR = order_key(R), kq = order_key(qc), kL = order_key(L);
     const bool flat = !((kR > kq && kq > kL) || (kR < kq && kq < kL));
     const bool over = B::abs_lt(dq, q6);
-    const double DL = flat ? 0.0 : dq;
-    const double mid = flat ? 0.0 : fma(-0.5, RpL, qc);
+    const double DL = dsel(flat, 0.0, dq);
+    const double mid = dsel(flat, 0.0, fma(-0.5, RpL, qc));
     const double d2 = DL * DL * (1.0 / 6.0);
     const double prod = DL * mid;
     const bool ml = over && B::gt_nonneg(prod, d2);
     const bool mr = over && !ml && B::lt_neg(prod, d2);
     const double Ln = fma(-2.0, R, q3), Rn = fma(-2.0, L, q3);
-    const double Lf = flat ? qc : L, Rf = flat ? qc : R;
-    L = ml ? Ln : Lf;
-    R = mr ? Rn : Rf;
+    const double Lf = dsel(flat, qc, L), Rf = dsel(flat, qc, R);
+    L = dsel(ml, Ln, Lf);
+    R = dsel(mr, Rn, Rf);
 }
 
 // Marching reconstruction: init() with the window of the first cell, then cell() once per
@@ -352,7 +362,7 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
             const real u = eA.x;
             const bool up = !signbit(eA.y);
             const real ig = igp;
-            const real eL = up ? pL : L, eR = up ? pR : R, eQ = up ? pQ : w[2];
+            const real eL = dsel(up, pL, L), eR = dsel(up, pR, R), eQ = dsel(up, pQ, w[2]);
             const real F = fma(gA, eQ, fma(fA.y, eL, fA.x * eR));
             const real cm = split == SP_AVLT ? real(0) : gl * (u * dtdx);  // g u dt/dx at edge m (SP-L04, SP-PL07)
             if (m > ma) {
