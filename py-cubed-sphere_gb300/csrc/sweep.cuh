@@ -57,49 +57,83 @@ struct Pred {
     __device__ static __forceinline__ bool gt_nonneg(real p, real d) { return p > d; }
     __device__ static __forceinline__ bool lt_neg(real p, real d) { return -d > p; }
 };
-template <>
-struct Pred<double> {
-    static constexpr long long MAG = 0x7fffffffffffffffLL;
-    __device__ static __forceinline__ long long b(double x) { return __double_as_longlong(x); }
-    __device__ static __forceinline__ bool prod_pos(double x, double y) {
-        return (b(x) ^ b(y)) >= 0 && (b(x) & MAG) != 0 && (b(y) & MAG) != 0;
-    }
-    __device__ static __forceinline__ bool prod_nonpos(double x, double y) { return !prod_pos(x, y); }
-    __device__ static __forceinline__ bool abs_lt(double x, double y) { return (b(x) & MAG) < (b(y) & MAG); }
-    __device__ static __forceinline__ double min_nonneg(double x, double y) {
-        return __longlong_as_double(b(x) < b(y) ? b(x) : b(y));
-    }
-    __device__ static __forceinline__ bool gt_nonneg(double p, double d) { return b(p) > b(d); }
-    __device__ static __forceinline__ bool lt_neg(double p, double d) { return b(p) < 0 && (b(p) & MAG) > b(d); }
-};
-
 // FP64 helpers on the integer pipe.  GB300 issues FP64 arithmetic at 1/64 of the FP32 rate, so
 // the FP64 kernel moves every operation that needs no FP64 rounding off the FP64 pipe: absolute
 // values, sign transfers and selections on the bit patterns, exact scalings by powers of two on
-// the exponent field, orderings of the bit patterns.
-// x 2^K, equal to the FP64 product whenever that is a normal number (every value of an advected
-// field); results below the normal range become a zero of x's sign, and x is returned unchanged
-// when it is infinite, NaN or so large (> 2^1022) that the product would overflow
+// the exponent field, orderings of the bit patterns.  All of it works on the 32-bit halves of the
+// patterns: measured on GB300, 64-bit integer comparisons run as FP64-pipe instructions (they
+// counted as DADD), so a 64-bit compare would cost as much as the arithmetic it replaces.
+struct Bits {  // a double as its two 32-bit words
+    int h;       // sign, exponent, high mantissa
+    unsigned l;  // low mantissa
+    __device__ __forceinline__ explicit Bits(double x) {
+        h = __double2hiint(x);
+        l = (unsigned)__double2loint(x);
+    }
+    __device__ __forceinline__ Bits(int h_, unsigned l_) {
+        h = h_;
+        l = l_;
+    }
+    __device__ __forceinline__ double d() const { return __hiloint2double(h, (int)l); }
+    __device__ __forceinline__ int mh() const { return h & 0x7fffffff; }  // high word of |x|
+    __device__ __forceinline__ bool zero() const { return (mh() | (int)l) == 0; }
+};
+// |x| < |y| (magnitudes compared word by word)
+__device__ __forceinline__ bool mag_lt(const Bits &x, const Bits &y) {
+    return x.mh() < y.mh() || (x.mh() == y.mh() && x.l < y.l);
+}
+// c ? a : b on the bit patterns
+__device__ __forceinline__ Bits bsel(bool c, const Bits &a, const Bits &b) { return Bits(c ? a.h : b.h, c ? a.l : b.l); }
+__device__ __forceinline__ double dsel(bool c, double a, double b) { return bsel(c, Bits(a), Bits(b)).d(); }
+__device__ __forceinline__ float dsel(bool c, float a, float b) { return c ? a : b; }
+// the order of finite values (+0 and -0 equal): x > y
+__device__ __forceinline__ bool ord_gt(const Bits &x, const Bits &y) {
+    const bool nx = x.h < 0 && !x.zero(), ny = y.h < 0 && !y.zero();
+    if (nx != ny) return ny;                  // exactly one of them negative (zeros count as +0)
+    const bool gt_mag = mag_lt(y, x), lt_mag = mag_lt(x, y);
+    return nx ? lt_mag : gt_mag;              // both negative: the smaller magnitude is greater
+}
+template <>
+struct Pred<double> {
+    __device__ static __forceinline__ bool prod_pos(double x, double y) {
+        const Bits a(x), b(y);
+        return (a.h ^ b.h) >= 0 && !a.zero() && !b.zero();
+    }
+    __device__ static __forceinline__ bool prod_nonpos(double x, double y) { return !prod_pos(x, y); }
+    __device__ static __forceinline__ bool abs_lt(double x, double y) { return mag_lt(Bits(x), Bits(y)); }
+    // a, b >= 0
+    __device__ static __forceinline__ double min_nonneg(double x, double y) {
+        const Bits a(x), b(y);
+        return bsel(mag_lt(a, b), a, b).d();
+    }
+    // p > d and p < -d, with d >= 0
+    __device__ static __forceinline__ bool gt_nonneg(double p, double d) {
+        const Bits a(p), b(d);
+        return a.h >= 0 && mag_lt(b, a);
+    }
+    __device__ static __forceinline__ bool lt_neg(double p, double d) {
+        const Bits a(p), b(d);
+        return a.h < 0 && mag_lt(b, a);
+    }
+};
+
+// |x| 2^K on the pattern of a magnitude m (sign bit clear): equal to the FP64 product whenever that
+// is a normal number (every value of an advected field); results below the normal range become
+// 0, and m is returned unchanged when it is infinite, NaN or so large (> 2^1022) that the product
+// would overflow
+template <int K>
+__device__ __forceinline__ Bits mag_scale(const Bits &m) {
+    const int e = m.h >> 20;
+    constexpr int EMIN = K < 0 ? 1 - K : 1, EMAX = K > 0 ? 0x7fe - K : 0x7fe;
+    if (e < EMIN) return Bits(0, 0u);
+    return Bits(e <= EMAX ? m.h + K * (1 << 20) : m.h, m.l);
+}
+// x 2^K for a double of either sign, as mag_scale (the sign kept)
 template <int K>
 __device__ __forceinline__ double pow2_scale(double x) {
-    const int hi = __double2hiint(x), lo = __double2loint(x);
-    const int e = (hi >> 20) & 0x7ff;
-    constexpr int EMIN = K < 0 ? 1 - K : 1, EMAX = K > 0 ? 0x7fe - K : 0x7fe;
-    const bool in = e >= EMIN && e <= EMAX;
-    const bool tiny = e < EMIN;
-    const int hi2 = in ? hi + K * (1 << 20) : (tiny ? (hi & (int)0x80000000) : hi);
-    return __hiloint2double(hi2, tiny ? 0 : lo);
-}
-// c ? a : b on the bit patterns (integer selects; no FP64 instruction)
-__device__ __forceinline__ double dsel(bool c, double a, double b) {
-    return __longlong_as_double(c ? __double_as_longlong(a) : __double_as_longlong(b));
-}
-__device__ __forceinline__ float dsel(bool c, float a, float b) { return c ? a : b; }
-// x as a signed integer key whose order is the floating-point order of finite values (+0 and -0
-// equal)
-__device__ __forceinline__ long long order_key(double x) {
-    const long long b = __double_as_longlong(x);
-    return b < 0 ? -(b & 0x7fffffffffffffffLL) : b;
+    const Bits b(x);
+    const Bits m = mag_scale<K>(Bits(b.mh(), b.l));
+    return Bits(m.h | (b.h & (int)0x80000000), m.l).d();
 }
 
 // --------------------------------------------------------------------------- reconstructions
@@ -176,22 +210,14 @@ __device__ __forceinline__ real ppm0_edge(real qam, real qa, real qb, real qbp) 
 // edge value 0.5 (qa + qb) - (sb - sa)/6; the limiter (reconstruction_1d.py:102-153) with the
 // monotonicity test as an ordering of the bit patterns (R - qc and qc - L have the signs of
 // those comparisons) and the flattened case's DL = 0, mid = 0 selected.
-// |x| 2^K on the bit pattern m = |x| (as pow2_scale): the magnitudes of the slope stay integers
-// from the subtractions to the result, so no step of it can become an FP64 instruction
-template <int K>
-__device__ __forceinline__ long long mag_scale(long long m) {
-    const int e = (int)(m >> 52);
-    constexpr int EMIN = K < 0 ? 1 - K : 1, EMAX = K > 0 ? 0x7fe - K : 0x7fe;
-    return (e >= EMIN && e <= EMAX) ? m + ((long long)K << 52) : (e < EMIN ? 0LL : m);
-}
 __device__ __forceinline__ double cw84_slope_d(double a, double b, double c) {
-    using B = Pred<double>;
-    constexpr long long MAG = 0x7fffffffffffffffLL;
-    const long long ka = B::b(a), kb = B::b(b) & MAG, kc = B::b(c) & MAG;
-    const long long m = mag_scale<1>(kb < kc ? kb : kc);
-    const long long h = mag_scale<-1>(ka & MAG);
-    const long long v = (h < m ? h : m) | (ka & ~MAG);
-    return __longlong_as_double(B::prod_pos(b, c) ? v : 0LL);
+    const Bits A(a), B(b), C(c);
+    const Bits mb(B.mh(), B.l), mc(C.mh(), C.l);
+    const Bits m = mag_scale<1>(bsel(mag_lt(mb, mc), mb, mc));   // 2 min(|b|, |c|)
+    const Bits h = mag_scale<-1>(Bits(A.mh(), A.l));                // |a| / 2
+    const Bits v = bsel(mag_lt(h, m), h, m);
+    const bool pos = (B.h ^ C.h) >= 0 && !B.zero() && !C.zero();  // b c > 0
+    return pos ? Bits(v.h | (A.h & (int)0x80000000), v.l).d() : 0.0;
 }
 __device__ __forceinline__ double cw84_edge_d(double qa, double qb, double sa, double sb) {
     return fma(-(sb - sa), 1.0 / 6.0, pow2_scale<-1>(qb + qa));
@@ -201,8 +227,8 @@ __device__ __forceinline__ void cw84_limit_d(double qc, double &L, double &R) {
     const double dq = R - L, RpL = R + L;
     const double q3 = fma(2.0, qc, qc);  // 3 qc, one rounding
     const double q6 = fma(-3.0, RpL, pow2_scale<1>(q3));
-    const long long kR = order_key(R), kq = order_key(qc), kL = order_key(L);
-    const bool flat = !((kR > kq && kq > kL) || (kR < kq && kq < kL));
+    const Bits bR(R), bq(qc), bL(L);
+    const bool flat = !((ord_gt(bR, bq) && ord_gt(bq, bL)) || (ord_gt(bq, bR) && ord_gt(bL, bq)));
     const bool over = B::abs_lt(dq, q6);
     const double DL = dsel(flat, 0.0, dq);
     const double mid = dsel(flat, 0.0, fma(-0.5, RpL, qc));

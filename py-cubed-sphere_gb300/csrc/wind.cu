@@ -60,12 +60,12 @@ struct UpwindMetric {
     int pl07;                             // MT-PL07: every weight is the edge's metric
 };
 
-// the upwind choice of an edge: wind >= 0 (flux.py:48-61), on the integer pipe for FP64 (-0 counts
-// as >= 0, as the comparison does)
+// the upwind choice of an edge: wind >= 0 (flux.py:48-61), for FP64 on the integer pipe with 32-bit
+// operations on the pattern's words (-0 counts as >= 0, as the comparison does)
 __device__ __forceinline__ bool wind_up(float u) { return u >= 0.f; }
 __device__ __forceinline__ bool wind_up(double u) {
-    const long long b = __double_as_longlong(u);
-    return b >= 0 || (b << 1) == 0;
+    const int h = __double2hiint(u);
+    return h >= 0 || ((h & 0x7fffffff) | __double2loint(u)) == 0;
 }
 
 template <class W>
