@@ -67,16 +67,16 @@ def dt_for_cfl(make_plan):
 
 PROFILES = {32: os.path.join(ROOT, "profiles", "k_sweep2_N384_T2.md"),
             64: os.path.join(ROOT, "profiles", "k_sweep_f64_N384_T2.md")}
-# the sources the step kernels are compiled from: a committed ncu summary states their digest,
-# and its figures are used only while the sources are unchanged
-KERNEL_SOURCES = ("sweep.cuh", "sweep2.cuh", "fused.cuh", "halo.cuh", "common.cuh", "tiles.h",
-                  "sweep_f32_pairs.cu", "sweep_f64.cu")
+# the sources each step kernel is compiled from: a committed ncu summary states their digest,
+# and its figures are used only while those sources are unchanged
+KERNEL_SOURCES = {32: ("sweep2.cuh", "fused.cuh", "halo.cuh", "common.cuh", "tiles.h", "sweep_f32_pairs.cu"),
+                  64: ("sweep.cuh", "fused.cuh", "halo.cuh", "common.cuh", "tiles.h", "sweep_f64.cu")}
 
 
-def kernel_digest():
+def kernel_digest(precision):
     import hashlib
     h = hashlib.sha256()
-    for name in KERNEL_SOURCES:
+    for name in KERNEL_SOURCES[precision]:
         with open(os.path.join(ROOT, "py-cubed-sphere_gb300", "csrc", name), "rb") as f:
             h.update(name.encode() + b"\0" + f.read())
     return h.hexdigest()[:16]
@@ -94,7 +94,7 @@ def profiled(precision, key):
                 vals[k.strip()] = v.split()[0].replace(",", "") if v.split() else ""
     except OSError:
         return None
-    if vals.get("source_digest") != kernel_digest() or key not in vals:
+    if vals.get("source_digest") != kernel_digest(precision) or key not in vals:
         return None
     try:
         return float(vals[key])
