@@ -509,10 +509,51 @@ def run_serving(torch, nreq, stream, budget_gb=120.0):
            "batch_steps": summ["batch_steps"],
            "config": "Poisson 200 req/s, N log-uniform [32,1024], steps U[50,2000], 1-4 tracers, "
                      "solid/deformational 50/50, FP32, 120 GB budget, %d requests of the seeded stream" % nreq}
-    for k in ("membership_changes", "graph_builds", "graph_build_ms", "plan_build_s", "release_s"):
+    for k in ("membership_changes", "graph_builds", "graph_build_ms", "plan_build_s", "release_s", "advance_s"):
         if k in summ:
             out[k] = summ[k]
+    cap = serving_capacity(torch, srv, reqs, budget_gb)
+    out["mix_capacity"] = cap
+    out["vs_mix_capacity"] = round(summ["throughput"] / cap["value"], 4) if cap["value"] else None
     return out
+
+
+def serving_capacity(torch, srv, reqs, budget_gb, steps=20, warmup=3):
+    """The GPU's throughput on the serving mix with no arrivals or departures: the stream's
+    requests in arrival order, admitted by the loop's own estimate up to the budget and its
+    resident limit, stepped as one static batch (graph per step; CUDA events on the batch's
+    stream).  The served throughput over this is the loop's efficiency."""
+    from csadv import Batch, serve
+    st = torch.cuda.Stream()
+    used, plans = 0, []
+    try:
+        for r in reqs:
+            need = srv.estimate(r)
+            if used + need > budget_gb * 1e9 or len(plans) >= srv.max_active:
+                break
+            plans.append((serve.make_plan(r, 32, srv.cfl, st), r))
+            used += need
+        cells = sum(6 * r.N * r.N * r.tracers for _, r in plans)
+        with Batch(len(plans)) as b:
+            for pl, _ in plans:
+                b.add(pl)
+            b.advance(warmup, st)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st.synchronize()
+            e0.record(st)
+            b.advance(steps, st)
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            for pl, _ in plans:
+                b.remove(pl)
+    finally:
+        for pl, _ in plans:
+            pl.release(st)
+        st.synchronize()
+    return {"value": round(cells / (ms * 1e-3), 1), "unit": "tracer cell-steps/s", "solves": len(plans),
+            "resident_gb": round(used / 1e9, 2), "ms_per_step": round(ms, 4), "timed_steps": steps,
+            "solid_fraction": round(sum(r.wind == "solid" for _, r in plans) / max(len(plans), 1), 3)}
 
 
 def oracle_replica():

@@ -99,7 +99,14 @@ int csadv_set_device(int device);
  * Errors: CSADV_ERR_OPTION, CSADV_ERR_OPTION_PAIR, CSADV_ERR_ARG, CSADV_ERR_OOM. */
 int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, void *stream,
                       csadv_plan **out);
+/* Frees the plan after waiting for all work on its device. */
 int csadv_plan_destroy(csadv_plan *plan);
+/* Frees the plan without waiting (no reference counterpart: the reference's simulation objects
+ * are garbage-collected Python objects; this serves many short-lived plans).  `stream` is the
+ * stream of the plan's last work, or one ordered after it: the plan's device memory, and its
+ * grid if no other plan shares it, return to the library's memory pool in that stream's order
+ * and are reused by later plans.  Detaches the plan from its batch first. */
+int csadv_plan_release(csadv_plan *plan, void *stream);
 int csadv_get_dt(const csadv_plan *plan, double *dt);
 
 /* q0_adv (advection_ic.py:208-210) evaluated on the device at the interior cell centres

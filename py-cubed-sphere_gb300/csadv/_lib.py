@@ -64,6 +64,7 @@ _SIGS = {
     "csadv_set_device": ([_c_int], _c_int),
     "csadv_plan_create": ([_c_int, _c_double, _c_int, ctypes.POINTER(Options), _vp, ctypes.POINTER(_vp)], _c_int),
     "csadv_plan_destroy": ([_vp], _c_int),
+    "csadv_plan_release": ([_vp, _vp], _c_int),
     "csadv_get_dt": ([_vp, _dp], _c_int),
     "csadv_init_tracer": ([_vp, _c_int, _c_int, _dp, _vp], _c_int),
     "csadv_set_tracer": ([_vp, _c_int, _vp, _c_int, _vp], _c_int),

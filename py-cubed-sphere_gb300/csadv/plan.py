@@ -39,8 +39,18 @@ class Plan:
 
     # ------------------------------------------------------------------ lifecycle
     def close(self):
+        """Free the plan after all work on its device has finished."""
         if getattr(self, "_h", None) and self._h.value:
             L.lib().csadv_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def release(self, stream=None):
+        """Free the plan without waiting: its device memory returns to the library's pool in the
+        order of ``stream`` (the stream of its last work, or one ordered after it; default: the
+        plan's own stream) and is reused by later plans.  Detaches it from its batch."""
+        if getattr(self, "_h", None) and self._h.value:
+            st = self.stream if stream is None else L.stream_handle(stream)
+            L.check(L.lib().csadv_plan_release(self._h, st), "csadv_plan_release")
             self._h = ctypes.c_void_p()
 
     def __del__(self):

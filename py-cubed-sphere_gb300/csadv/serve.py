@@ -129,10 +129,10 @@ class Server:
     of admitted requests (grid, winds, initial conditions, on `build_stream`) while the batch
     steps, and a retirement thread reads a finished solve's error norms and mass on `stream`, after
     its last step.  A plan joins the batch at the first step boundary after it is ready; when
-    nothing is resident, the requests admitted together are awaited and start together.  Freeing a
-    plan's device memory waits for the whole device, so released plans are destroyed by the loop
-    itself, between steps, in groups (when their memory is needed for an admission, or every
-    `release_s` seconds).  Without the two streams everything runs inline on `stream`.
+    nothing is resident, the requests admitted together are awaited and start together.  A plan
+    that has been read out is freed by the loop at once, in the order of `stream`
+    (csadv_plan_release: nothing waits for the device), and its memory is reused by the next
+    plans from the library's pool.  Without the two streams everything runs inline on `stream`.
 
     Failures stay with their request: a request whose plan cannot be made (bad size, no
     memory), whose state turns non-finite, or that waits past its deadline gets a Result with
@@ -140,8 +140,7 @@ class Server:
     for every queued request at every step boundary, not only for the head of the queue."""
 
     def __init__(self, budget_bytes, precision=32, cfl=0.5, max_active=512, stream=None, clock=time.perf_counter,
-                 keep_state=False, max_steps_per_tick=8, threads=None, build_stream=None, device=None, builders=2,
-                 release_s=0.5):
+                 keep_state=False, max_steps_per_tick=8, threads=None, build_stream=None, device=None, builders=2):
         self.budget = int(budget_bytes)
         self.precision = precision
         self.cfl = cfl
@@ -154,7 +153,6 @@ class Server:
         self.max_steps_per_tick = max_steps_per_tick
         self.threads = (stream is not None and build_stream is not None) if threads is None else bool(threads)
         self.builders = builders
-        self.release_s = release_s
         self._coef = {}
 
     # device bytes of a plan ~ plane elements x (a + b T), per wind kind; measured once
@@ -184,7 +182,7 @@ class Server:
             mass0 = [pl.mass(t) for t in range(req.tracers)]
             nbytes = pl.stats()["device_bytes"]
         except Exception:
-            pl.close()
+            pl.release()
             raise
         pl.stream = L.stream_handle(self.stream)
         return pl, mass0, nbytes, time.perf_counter() - t0
@@ -212,7 +210,6 @@ class Server:
         queue = collections.deque()
         building = collections.deque()  # [req, future, bytes reserved]
         retiring = []                     # [future of Result, plan, bytes]
-        released = []                     # [plan, bytes]: read out, memory not yet freed
         active = {}      # id(plan) -> [plan, req, remaining, admitted, mass0, bytes]
         used = 0
         results = []
@@ -223,7 +220,7 @@ class Server:
         members_changed = 0
         build_s = 0.0
         release_s = 0.0
-        last_release = time.perf_counter()
+        advance_s = 0.0
         builder = retirer = None
         if self.threads:
             builder = cf.ThreadPoolExecutor(max_workers=self.builders, initializer=self._thread_init)
@@ -237,34 +234,26 @@ class Server:
                 f.set_exception(e)
             return f
 
-        def collect_retired(block=False):
+        def collect_retired(block=False):  # results of the plans read out; their memory is freed
+            nonlocal used, release_s
             keep = []
             for item in retiring:
                 if block or item[0].done():
                     results.append(item[0].result())
-                    released.append(item[1:])
+                    tr = time.perf_counter()
+                    item[1].release(self.stream)
+                    release_s += time.perf_counter() - tr
+                    used -= item[2]
                 else:
                     keep.append(item)
             retiring[:] = keep
 
-        def release():  # free the memory of plans that have been read out (waits for the device)
-            nonlocal used, release_s, last_release
-            tr = time.perf_counter()
-            for pl, nbytes in released:
-                pl.close()
-                used -= nbytes
-            released.clear()
-            release_s += time.perf_counter() - tr
-            last_release = time.perf_counter()
-
         try:
-            while pending or queue or building or active or retiring or released:
+            while pending or queue or building or active or retiring:
                 now = self.clock() - t0
                 while pending and (not realtime or pending[0].arrival <= now):
                     queue.append(pending.popleft())
                 collect_retired()
-                if released and (time.perf_counter() - last_release > self.release_s or not (active or building)):
-                    release()
                 # admission deadlines, for every queued request
                 if any(r.deadline is not None for r in queue):
                     keep = collections.deque()
@@ -279,8 +268,6 @@ class Server:
                 while queue and len(active) + len(building) < self.max_active:
                     req = queue[0]
                     need = self.estimate(req)
-                    if used + need > self.budget and released:
-                        release()
                     if used + need > self.budget and (active or building or retiring):
                         break
                     queue.popleft()
@@ -316,7 +303,9 @@ class Server:
                     continue
                 k = min(v[2] for v in active.values())
                 k = max(1, min(k, self.max_steps_per_tick))
+                ta = time.perf_counter()
                 batch.advance(k, self.stream)
+                advance_s += time.perf_counter() - ta
                 steps += k
                 if on_step:
                     on_step(steps, len(active), used)
@@ -333,7 +322,6 @@ class Server:
                     fut = retirer.submit(self._retire, *args) if retirer else run_inline(self._retire, *args)
                     retiring.append([fut, pl, nbytes])
             collect_retired(block=True)
-            release()
         finally:
             for req, fut, need in building:
                 try:
@@ -348,8 +336,6 @@ class Server:
                 except Exception:
                     pass
                 item[1].close()
-            for pl, _ in released:
-                pl.close()
             if builder:
                 builder.shutdown(wait=True)
             if retirer:
@@ -369,7 +355,7 @@ class Server:
                    "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                    "batch_steps": steps, "peak_bytes": peak, "budget_bytes": self.budget,
                    "membership_changes": members_changed, "plan_build_s": round(build_s, 3),
-                   "release_s": round(release_s, 3), "graph_builds": graph_builds, "graph_build_ms": graph_ms,
+                   "release_s": round(release_s, 3), "advance_s": round(advance_s, 3), "graph_builds": graph_builds, "graph_build_ms": graph_ms,
                    "max_mass_change": max((max(r.mass_change) for r in served), default=0.0)}
         return results, summary
 

@@ -70,30 +70,117 @@ int default_tile(const Options &o, int N, int T) {
     return N >= 116 ? 4 : 7;
 }
 
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+
 // grids shared by the plans of one resolution and device
 std::mutex g_grid_mu;
 std::map<std::pair<int, int>, std::weak_ptr<GridHolder>> g_grids;
 
-int acquire_grid(int N, int device, cudaStream_t st, std::shared_ptr<GridHolder> &out) {
-    std::lock_guard<std::mutex> lock(g_grid_mu);
-    const auto key = std::make_pair(device, N);
-    auto it = g_grids.find(key);
-    if (it != g_grids.end()) {
-        out = it->second.lock();
-        if (out) return CSADV_OK;
+}  // namespace
+
+cudaMemPool_t csadv::device_pool() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return nullptr;
+        }
+        unsigned long long keep = ~0ULL;  // freed memory stays in the pool for the next plans
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev] = pool;
     }
-    auto h = std::make_shared<GridHolder>();
-    int rc = build_grid(N, h->mem, h->grid, st);
-    if (rc) return rc;
-    CSADV_CUDA(cudaStreamSynchronize(st));  // plans on other streams may use it next
-    g_grids[key] = h;
+    return g_pools[dev];
+}
+
+namespace {
+
+// The grid of resolution N on this device, built by the first plan that asks for it.  The map's
+// lock is held only to find or insert the holder: the build itself (host tables, uploads, a wait
+// for the stream) runs under the holder's own lock, so plans of other sizes are made and
+// released meanwhile.
+int acquire_grid(int N, int device, cudaStream_t st, std::shared_ptr<GridHolder> &out) {
+    const auto key = std::make_pair(device, N);
+    std::shared_ptr<GridHolder> h;
+    {
+        std::lock_guard<std::mutex> lock(g_grid_mu);
+        auto it = g_grids.find(key);
+        if (it != g_grids.end()) h = it->second.lock();
+        if (!h) {
+            h = std::make_shared<GridHolder>();
+            g_grids[key] = h;
+        }
+    }
+    std::lock_guard<std::mutex> build(h->build_mu);
+    if (!h->built) {
+        cudaMemPool_t pool = device_pool();
+        int rc = pool ? CSADV_OK : CSADV_ERR_CUDA;
+        if (!rc) {
+            h->mem.use_pool(pool, st);
+            rc = build_grid(N, h->mem, h->grid, st);
+        }
+        // plans on other streams use it next
+        if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = CSADV_ERR_CUDA;
+        (void)cudaGetLastError();
+        if (rc) {
+            h->mem.release();
+            std::lock_guard<std::mutex> lock(g_grid_mu);
+            auto it = g_grids.find(key);
+            if (it != g_grids.end() && it->second.lock() == h) g_grids.erase(it);  // the next plan retries
+            return rc;
+        }
+        h->built = true;
+    }
     out = h;
     return CSADV_OK;
+}
+
+// Drops the plan's reference to its grid.  The last plan to leave frees the grid in the order of
+// stream st, after the work that the plans released before it had queued.
+void release_grid(csadv_plan *pl, cudaStream_t st) {
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    std::shared_ptr<GridHolder> &h = pl->gref;
+    if (!h) return;
+    if (h.use_count() > 1) {
+        auto &left = h->left;
+        for (size_t i = 0; i < left.size();) {  // forget the marks whose work has ended
+            if (cudaEventQuery(left[i]) == cudaSuccess) {
+                cudaEventDestroy(left[i]);
+                left[i] = left.back();
+                left.pop_back();
+            } else {
+                ++i;
+            }
+        }
+        (void)cudaGetLastError();
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
+            if (cudaEventRecord(e, st) == cudaSuccess) left.push_back(e);
+            else cudaEventDestroy(e);
+        }
+    } else {
+        for (cudaEvent_t e : h->left) {
+            cudaStreamWaitEvent(st, e, 0);
+            cudaEventDestroy(e);
+        }
+        h->left.clear();
+        h->mem.release_on(st);
+    }
+    (void)cudaGetLastError();
+    h.reset();
 }
 
 // the staged engine's per-tracer scratch, allocated on first use
 int ensure_scratch(csadv_plan *pl, cudaStream_t st) {
     if (pl->s.Qx) return CSADV_OK;
+    pl->mem.set_stream(st);
     const long long F = pl->grid.d.field;
     const size_t es = pl->esize();
     void **sa[] = {&pl->s.Qx, &pl->s.Qy, &pl->s.qLx, &pl->s.qRx, &pl->s.qLy, &pl->s.qRy, &pl->s.fx, &pl->s.fy, &pl->s.div};
@@ -442,24 +529,32 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     pl->device = dev;
     cudaStream_t st = S(stream);
     rc = acquire_grid(N, dev, st, pl->gref);
-    if (!rc) pl->grid = pl->gref->grid;
     if (rc) {
         delete pl;
         return rc;
     }
+    pl->grid = pl->gref->grid;
+    // failures below: the queued work ends before the memory returns to the pool
+    auto fail = [&](int e) {
+        cudaStreamSynchronize(st);
+        (void)cudaGetLastError();
+        release_grid(pl, st);
+        delete pl;
+        return e;
+    };
     const Dims d = pl->grid.d;
     const long long F = d.field;
     const size_t es = pl->esize();
+    cudaMemPool_t pool = device_pool();
+    if (!pool) return fail(CSADV_ERR_CUDA);
+    pl->mem.use_pool(pool, st);
     pl->Q = pl->mem.alloc<char>((long long)ntracers * F * es);
     pl->npart = staged_partial_count(pl->grid);
     pl->partials = pl->mem.alloc<double>(pl->npart);
     pl->scal = pl->mem.alloc<double>(8);
     pl->stage = pl->mem.alloc<double>((long long)NFACE * d.n * d.n);
     pl->tmp = pl->mem.alloc<double>(3LL * diag_partials(pl->grid) + 8);
-    if (!pl->mem.ok()) {
-        delete pl;
-        return CSADV_ERR_OOM;
-    }
+    if (!pl->mem.ok()) return fail(CSADV_ERR_OOM);
     // the staged engine's scratch (fused plans allocate it on first use: csadv_divergence)
     if (!fused) rc = ensure_scratch(pl, st);
     if (!rc && fused) {
@@ -467,10 +562,7 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
         rc = fused_alloc(o, pl->grid, ntracers, pl->mem, pl->f, st);
     }
     if (!rc) rc = zero(pl->Q, (size_t)ntracers * F * es, st);
-    if (rc) {
-        delete pl;
-        return rc;
-    }
+    if (rc) return fail(rc);
     // init_vars_adv (advection_vars.py:19-107): t = 0 winds, wind halo, old <- current,
     // departure-point winds, CFL
     rc = wind_setup(o, pl->grid, pl->w, pl->mem, dt, st);
@@ -496,10 +588,7 @@ int csadv_plan_create(int N, double dt, int ntracers, const csadv_options *opt, 
     if (!rc) rc = wind_cfl(o, pl->grid, pl->w, dt, pl->tmp, pl->cfl, st);
     if (!rc && fused) rc = fused_prep_winds(o, pl->grid, pl->w, dt, pl->f, pl->cur, st);
     pl->f.rec_ready = true;
-    if (rc) {
-        delete pl;
-        return rc;
-    }
+    if (rc) return fail(rc);
     *out = pl;
     return CSADV_OK;
 }
@@ -515,7 +604,19 @@ int csadv_plan_destroy(csadv_plan *plan) {
     batch_forget(plan);
     select_device(plan);
     cudaDeviceSynchronize();
+    release_grid(plan, cudaStreamPerThread);
     delete plan;
+    return CSADV_OK;
+}
+
+int csadv_plan_release(csadv_plan *plan, void *stream) {
+    if (!plan) return CSADV_ERR_ARG;
+    batch_forget(plan);
+    select_device(plan);
+    cudaStream_t st = S(stream);
+    plan->mem.release_on(st);
+    release_grid(plan, st);
+    delete plan;  // its graphs, streams and events are released by CUDA once their work is done
     return CSADV_OK;
 }
 

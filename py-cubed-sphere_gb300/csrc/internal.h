@@ -18,15 +18,29 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
         if (_e != cudaSuccess) return ::csadv::cuda_fail(_e, #call, __FILE__, __LINE__); \
     } while (0)
 
-// Owner of a plan's device allocations (one cudaMalloc per array, freed together).
+// The library's stream-ordered memory pool of the current device (created on first use; memory
+// freed into it stays reserved for the library's next allocations).  Plans and grids allocate
+// from it, so that csadv_plan_release can free a plan in the order of a stream instead of
+// waiting for the whole device.
+cudaMemPool_t device_pool();
+
+// Owner of a plan's device allocations (one allocation per array, freed together): cudaMalloc,
+// or, after use_pool(), the library's pool in the order of a stream.
 class DeviceArena {
    public:
+    void use_pool(cudaMemPool_t pool, cudaStream_t st) {
+        pool_ = pool;
+        st_ = st;
+    }
+    // the stream of the next allocations (pool mode)
+    void set_stream(cudaStream_t st) { st_ = st; }
     template <class T>
     T *alloc(long long count) {
         if (failed_) return nullptr;
         void *p = nullptr;
         size_t bytes = (size_t)(count > 0 ? count : 1) * sizeof(T);
-        if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        const cudaError_t e = pool_ ? cudaMallocFromPoolAsync(&p, bytes, pool_, st_) : cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
             (void)cudaGetLastError();
             failed_ = true;
             return nullptr;
@@ -37,18 +51,26 @@ class DeviceArena {
     }
     bool ok() const { return !failed_; }
     size_t bytes() const { return bytes_; }
-    void release() {
-        for (void *p : ptrs_) cudaFree(p);
+    // free in the order of stream s (pool allocations; others with cudaFree)
+    void release_on(cudaStream_t s) {
+        for (void *p : ptrs_) {
+            if (pool_) cudaFreeAsync(p, s);
+            else cudaFree(p);
+        }
         ptrs_.clear();
         bytes_ = 0;
         failed_ = false;
     }
+    // free now: the caller has made sure no work that uses the memory is pending
+    void release() { release_on(cudaStreamPerThread); }
     ~DeviceArena() { release(); }
 
    private:
     std::vector<void *> ptrs_;
     size_t bytes_ = 0;
     bool failed_ = false;
+    cudaMemPool_t pool_ = nullptr;
+    cudaStream_t st_ = nullptr;
 };
 
 struct Options {

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <memory>
+#include <mutex>
+#include <vector>
 
 #include "../../include/csadv.h"
 #include "common.cuh"
@@ -18,8 +20,15 @@ namespace csadv {
 // the first, freed with the last).
 struct GridHolder {
     DeviceArena mem;
-    std::shared_ptr<GridHolder> gref;  // shared grid; `grid` is a copy of its descriptor
     Grid grid;
+    std::mutex build_mu;  // held while the first plan builds the grid
+    bool built = false;
+    // events recorded where the work of plans released while others still used the grid ends;
+    // the last plan's stream waits for them before the grid is freed
+    std::vector<cudaEvent_t> left;
+    ~GridHolder() {
+        for (cudaEvent_t e : left) cudaEventDestroy(e);
+    }
 };
 }  // namespace csadv
 

@@ -142,6 +142,9 @@ class _FakePlan:
     def close(self):
         self.closed = True
 
+    def release(self, stream=None):
+        self.closed = True
+
 
 class _FakeBatch:
     def __init__(self, capacity):
