@@ -223,23 +223,23 @@ __device__ __forceinline__ double cw84_edge_d(double qa, double qb, double sa, d
     return fma(-(sb - sa), 1.0 / 6.0, pow2_scale<-1>(qb + qa));
 }
 __device__ __forceinline__ void cw84_limit_d(double qc, double &L, double &R) {
-    using B = Pred<double>;
     const double dq = R - L, RpL = R + L;
     const double q3 = fma(2.0, qc, qc);  // 3 qc, one rounding
     const double q6 = fma(-3.0, RpL, pow2_scale<1>(q3));
-    const Bits bR(R), bq(qc), bL(L);
+    const Bits bR(R), bq(qc), bL(L), bd(dq), b6(q6);
     const bool flat = !((ord_gt(bR, bq) && ord_gt(bq, bL)) || (ord_gt(bq, bR) && ord_gt(bL, bq)));
-    const bool over = B::abs_lt(dq, q6);
-    const double DL = dsel(flat, 0.0, dq);
-    const double mid = dsel(flat, 0.0, fma(-0.5, RpL, qc));
-    const double d2 = DL * DL * (1.0 / 6.0);
-    const double prod = DL * mid;
-    const bool ml = over && B::gt_nonneg(prod, d2);
-    const bool mr = over && !ml && B::lt_neg(prod, d2);
-    const double Ln = fma(-2.0, R, q3), Rn = fma(-2.0, L, q3);
-    const double Lf = dsel(flat, qc, L), Rf = dsel(flat, qc, R);
-    L = dsel(ml, Ln, Lf);
-    R = dsel(mr, Rn, Rf);
+    // A cell that is not flattened has R != L, so dq != 0; with |dq| < |q6| the reference's tests
+    // dq (qc - (R + L)/2) > dq^2/6 and -dq^2/6 > dq (qc - (R + L)/2), i.e. q6/dq > 1 and q6/dq < -1,
+    // are the signs of q6 and dq agreeing (move left) or not (move right).  Where a rounding of
+    // the reference's products could decide a tie the other way, both branches give the same
+    // parabola (q6 = +-dq makes 3 qc - 2 R = L and 3 qc - 2 L = R).
+    const bool over = !flat && mag_lt(bd, b6);
+    const bool same = (bd.h ^ b6.h) >= 0;
+    const bool ml = over && same, mr = over && !same;
+    const double T = fma(-2.0, dsel(ml, R, L), q3);  // 3 qc - 2 R (move left), 3 qc - 2 L (move right)
+    const double Lk = dsel(ml, T, L), Rk = dsel(mr, T, R);
+    L = dsel(flat, qc, Lk);
+    R = dsel(flat, qc, Rk);
 }
 
 // Marching reconstruction: init() with the window of the first cell, then cell() once per

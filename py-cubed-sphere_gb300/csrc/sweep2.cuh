@@ -131,22 +131,24 @@ __device__ __forceinline__ V cw84_edge2(V qa, V qb, V Sa, V Sb) {
 // CW84 monotonicity limiter (reconstruction_1d.py:102-153) on the doubled parabola (L2, R2) of
 // the cell with doubled mean Q2.  With dq = R - L and q6 = 6 q - 3 (R + L) taken before the
 // flattening, the reference's overshoot tests (R - L)(q - (R + L)/2) >< +-(R - L)^2 / 6 on the
-// flattened values read dq q6 >< +-dq^2 when the cell is not flattened and never fire when it
-// is; 3 q - 2 R = q - 2 (R - q) and 3 q - 2 L = q + 2 (q - L).
+// flattened values never fire for a flattened cell; for one that is not flattened (R != L, so
+// dq != 0) they read q6/dq > 1 and q6/dq < -1, which under |dq| < |q6| are the signs of q6 and
+// dq agreeing (move left) or not (move right).  At the ties a rounding could decide, both branches
+// give the same parabola.  3 q - 2 R = q - 2 (R - q) and 3 q - 2 L = q + 2 (q - L).
 template <class V>
 __device__ __forceinline__ void cw84_limit2(V Q2, V &L2, V &R2) {
     const V dq = vsub(R2, L2);
     const V q6 = vmul(vsub(vadd(Q2, Q2), vadd(R2, L2)), bc<V>(3.f));
     const V u = vsub(R2, Q2), v = vsub(Q2, L2);
     const V pf = vmul(u, v);
-    const V a = vmul(dq, q6), b = vmul(dq, dq);
     const V Ln = vsub(Q2, vadd(u, u)), Rn = vadd(Q2, vadd(v, v));
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
         const bool flat = lane(pf, l) <= 0.f;
         const bool over = !flat && fabsf(lane(dq, l)) < fabsf(lane(q6, l));
-        const bool ml = over && lane(a, l) > lane(b, l);
-        const bool mr = over && !ml && -lane(b, l) > lane(a, l);
+        const bool same = (__float_as_int(lane(dq, l)) ^ __float_as_int(lane(q6, l))) >= 0;
+        const bool ml = over && same;
+        const bool mr = over && !same;
         set_lane(L2, l, flat ? lane(Q2, l) : (ml ? lane(Ln, l) : lane(L2, l)));
         set_lane(R2, l, flat ? lane(Q2, l) : (mr ? lane(Rn, l) : lane(R2, l)));
     }
