@@ -194,10 +194,10 @@ int csadv_set_graphs(csadv_plan *plan, int enable);
  * csadv_stats.main_ms.  Profiled steps launch directly (no graph) and synchronise. */
 int csadv_set_profiling(csadv_plan *plan, int enable);
 /* Where the ET-DG ghost cells of a fused plan come from (interpolation.py:154-314): enable = 1
- * (the default for FP32 plans) has the step kernel evaluate the ghost cells of its tiles from the
- * neighbouring panels itself; enable = 0 fills them with a separate ghost-cell launch before each
- * step (the default for FP64 plans).  Both give the same bits.  CSADV_ERR_UNSUPPORTED for a plan
- * that does not run the line-marching step kernel.  Outside stream capture. */
+ * (the default) has the step kernel evaluate the ghost cells of its tiles from the neighbouring
+ * panels itself; enable = 0 fills them with a separate ghost-cell launch before each step.  Both
+ * give the same bits.  CSADV_ERR_UNSUPPORTED for a plan that does not run the line-marching step
+ * kernel.  Outside stream capture. */
 int csadv_set_inline_ghosts(csadv_plan *plan, int enable);
 typedef struct csadv_stats {
     long long steps;            /* steps advanced */

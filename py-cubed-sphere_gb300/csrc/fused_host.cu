@@ -33,10 +33,11 @@ __global__ void k_plane_xform(const real *__restrict__ src, real *dst, Dims d, i
 }
 
 // cell records {g, 1/g} of the n x n centres, natural (dst(i, j)) or transposed (dst(j, i));
-// zero outside
+// zero outside.  dtdx != 0: {g, dtdx (1/g)}, the factor of the update (FP64 with AVLT splitting:
+// the kernel's per-cell product dt/dx * (1/g), made once per plan with the same two roundings)
 template <class real>
 __global__ void k_cell_records(const real *__restrict__ g, typename Vec2<real>::type *dst, Dims d, int n,
-                               int transpose) {
+                               int transpose, real dtdx) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= d.plane) return;
     const int a = (int)(t / d.pitch), b = (int)(t % d.pitch);
@@ -47,6 +48,7 @@ __global__ void k_cell_records(const real *__restrict__ g, typename Vec2<real>::
     if (i < n && j < n) {
         v.x = g[(long long)i * d.pitch + j];
         v.y = real(1) / v.x;
+        if (dtdx != real(0)) v.y = dtdx * v.y;
     }
     dst[t] = v;
 }
@@ -99,8 +101,8 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     const Dims d = g.d;
     const size_t es = o.precision == 64 ? sizeof(double) : sizeof(float);
     f.on = true;
-    // the FP32 step kernel evaluates the ET-DG ghost cells of its tiles itself (no ghost-cell launch)
-    f.inline_ghosts = o.precision == 32;
+    // the step kernel evaluates the ET-DG ghost cells of its tiles itself (no ghost-cell launch)
+    f.inline_ghosts = true;
     f.Qbuf[1] = mem.alloc<char>((long long)T * d.field * es);
     for (int b = 0; b < 2; ++b) f.corr[b] = mem.alloc<double>(T);
     int maxb = 0;
@@ -157,13 +159,13 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
         const int n = d.n;
         if (o.precision == 64) {
             const double *gpc = (const double *)f.g_pc, *gpv = (const double *)f.g_pv;
-            k_cell_records<double><<<nb, 256, 0, st>>>(gpc, (double2 *)f.crx, d, n, 0);
-            k_cell_records<double><<<nb, 256, 0, st>>>(gpc, (double2 *)f.cry, d, n, 1);
+            k_cell_records<double><<<nb, 256, 0, st>>>(gpc, (double2 *)f.crx, d, n, 0, 0.0);
+            k_cell_records<double><<<nb, 256, 0, st>>>(gpc, (double2 *)f.cry, d, n, 1, 0.0);
             k_plane_xform<double><<<nb, 256, 0, st>>>(gpv, (double *)gpvT, d, n, n + 1, 1, 0);
         } else {
             const float *gpc = (const float *)f.g_pc, *gpv = (const float *)f.g_pv;
-            k_cell_records<float><<<nb, 256, 0, st>>>(gpc, (float2 *)f.crx, d, n, 0);
-            k_cell_records<float><<<nb, 256, 0, st>>>(gpc, (float2 *)f.cry, d, n, 1);
+            k_cell_records<float><<<nb, 256, 0, st>>>(gpc, (float2 *)f.crx, d, n, 0, 0.f);
+            k_cell_records<float><<<nb, 256, 0, st>>>(gpc, (float2 *)f.cry, d, n, 1, 0.f);
             k_plane_xform<float><<<nb, 256, 0, st>>>(gpv, (float *)gpvT, d, n, n + 1, 1, 0);
         }
         CSADV_CUDA(cudaGetLastError());
@@ -182,8 +184,9 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
 
 int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceArena &mem, FusedState &f,
                         cudaStream_t st) {
-    if (o.precision != 32 || !w.nbasis) return CSADV_OK;
-    const size_t bytes = 2 * (size_t)g.d.field * sizeof(float);
+    if (!w.nbasis) return CSADV_OK;
+    // the same layout as the first buffer (FP64: the flux coefficients behind the records)
+    const size_t bytes = o.precision == 64 ? 6 * (size_t)g.d.field * sizeof(double) : 2 * (size_t)g.d.field * sizeof(float);
     f.erx1 = mem.alloc<char>(bytes);
     f.ery1 = mem.alloc<char>(bytes);
     if (!mem.ok()) return CSADV_ERR_OOM;
@@ -197,8 +200,8 @@ int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt,
                      cudaStream_t st) {
     if (f.sweep && w.nbasis) {
         if (o.precision == 64)
-            return wind_step<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT, (double2 *)f.erx,
-                                     (double2 *)f.ery, f.crx, f.cry, st);
+            return wind_step<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT,
+                                     (double2 *)f.rec_x(buf), (double2 *)f.rec_y(buf), f.crx, f.cry, st);
         return wind_step<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.rec_x(buf),
                                 (float2 *)f.rec_y(buf), nullptr, nullptr, st);
     }
@@ -270,6 +273,17 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
         s.hlag_k = g.lag_k;
         s.gside = g.gside;
         s.gcorner = g.gcorner;
+    }
+    if (o.precision == 64 && o.opsplit == SP_AVLT) {
+        // the FP64 AVLT kernel reads dt/dx (1/g) from the cell records (once, for the final dt)
+        const double dtdx = dt / g.dx;
+        if (f.crec_dtdx != dtdx) {
+            const int nb = ceil_div(g.d.plane, 256);
+            k_cell_records<double><<<nb, 256, 0, st>>>((const double *)f.g_pc, (double2 *)f.crx, g.d, g.d.n, 0, dtdx);
+            k_cell_records<double><<<nb, 256, 0, st>>>((const double *)f.g_pc, (double2 *)f.cry, g.d, g.d.n, 1, dtdx);
+            CSADV_CUDA(cudaGetLastError());
+            f.crec_dtdx = dtdx;
+        }
     }
     f.nitems = NFACE * h[0].ntiles;
     f.smem = o.precision == 64 ? sweep_smem_bytes<double>(f.scfg) : sweep_smem_bytes<float>(f.scfg);

@@ -171,6 +171,7 @@ struct FusedState {
     void *rec_x(int b) const { return wpipe && b == 1 ? erx1 : erx; }
     void *rec_y(int b) const { return wpipe && b == 1 ? ery1 : ery; }
     void *crx = nullptr, *cry = nullptr;  // cell records {g, 1/g} (natural, transposed)
+    double crec_dtdx = 0.0;  // FP64 AVLT: the cell records hold {g, dtdx / g} for this dt/dx
     const void *gpvT = nullptr;           // y-edge metric transposed
     SweepSolve *dsolve = nullptr;  // [2]
     int nitems = 0;             // work items of one sweep launch (6 x tiles)
@@ -186,7 +187,8 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
 // departure-point winds of the step that reads Qbuf[buf] (edge records buffer buf when pipelined)
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, int buf,
                      cudaStream_t st);
-// FP32 step kernel with a time-dependent (basis) wind: allocate the second record buffer
+// step kernel with a time-dependent (basis) wind: allocate the second record buffer (the next
+// step's records are made while the step kernel runs)
 int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceArena &mem, FusedState &f,
                         cudaStream_t st);
 // ghost cells of every tracer of Qbuf[cur] (with the pending correction applied)

@@ -136,6 +136,10 @@ __device__ __forceinline__ double pow2_scale(double x) {
     return Bits(m.h | (b.h & (int)0x80000000), m.l).d();
 }
 
+// x / 2 (exact: on the exponent for FP64, an FP32 product otherwise)
+__device__ __forceinline__ double half_of(double x) { return pow2_scale<-1>(x); }
+__device__ __forceinline__ float half_of(float x) { return 0.5f * x; }
+
 // --------------------------------------------------------------------------- reconstructions
 // CW84 limited slope of the cell q0 between qm and qp (reconstruction_1d.py:64-100);
 // min(...) * sign(d0) written as copysign: equal for every finite input
@@ -355,6 +359,9 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
                                                 const real *Qc, int qs, real *qout) {
     using O = RealOps<real>;
     using V = typename Vec2<real>::type;
+    // FP64 with AVLT splitting: the cell records carry dt/dx (1/g) (k_cell_records), and the
+    // split's (dt/dx / 2)(1/g) is half of it, exactly
+    const bool HDT = sizeof(real) == 8 && split == SP_AVLT;
     real w[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) w[k] = ln.s[(ma - 3 + k) * ln.ss];
@@ -398,7 +405,7 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
                     const real dF = -(F - Fp) * dtdx;
                     real o;
                     if (split == SP_AVLT)  // q + dF / (2 g), dF = -(F - Fp) dt/dx
-                        o = fma(-(F - Fp), (real(0.5) * dtdx) * ig, q);
+                        o = fma(-(F - Fp), HDT ? half_of(ig) : (real(0.5) * dtdx) * ig, q);
                     else if (split == SP_L04)
                         o = (q * gcp + real(0.5) * dF + real(0.5) * (cm - cp) * q) * ig;
                     else
@@ -408,7 +415,7 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
                     out[k * os] = F - Fp;
                 } else {
                     const real sdiv = (F - Fp) + dY[k * os];
-                    const real qn = fma(-sdiv, dtdx * ig, Qc[k * qs]);
+                    const real qn = fma(-sdiv, HDT ? ig : dtdx * ig, Qc[k * qs]);
                     qout[(long long)k * P] = qn;
                     if (mfpr) acc += sdiv;  // sum(div g) = sum(sdiv) / dx: div = sdiv / (dx g)
                 }

@@ -29,12 +29,18 @@ struct WindParams {
     double prm[4];
 };
 
+// -x for a double by its sign bit (an integer instruction, not one of the FP64 pipe)
+__device__ __forceinline__ double neg_bits(double x) {
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+__device__ __forceinline__ float neg_bits(float x) { return -x; }
+
 // edge record {wind, +-g}: the sign carries the upwind flag (+: wind >= 0), g = |value|
 template <class V, class W>
 __device__ __forceinline__ V edge_record(W wind, W g, bool up) {
     V r;
     r.x = wind;
-    r.y = up ? g : -g;
+    r.y = up ? g : neg_bits(g);
     return r;
 }
 
@@ -80,16 +86,17 @@ __device__ __forceinline__ void flux_coefs(W u, W g, bool up, W dtdx, const Upwi
         gC = um.gc[at2(d, cm, col)].x;
     }
     // one branch-free form of both cases: s = 1 -+ c, P = u s^2, R = u c s;
-    // wind >= 0: (alpha, beta) = (gR P, -gL R), else (gR R, gL P); gamma = gC u c (+-3 - 2c)
+    // wind >= 0: (alpha, beta) = (gR P, -gL R), else (gR R, gL P); gamma = +-gC u c (3 -+ 2c),
+    // and u c (3 -+ 2c) = u c + 2 u c (1 -+ c) = u c + 2 R
     const W c = u * dtdx;
     const W uc = u * c;
-    const W sg = up ? W(1) : W(-1);
-    const W s = fma(-sg, c, W(1));
-    const W P = (u * s) * s, R = uc * s;
-    const W X = up ? P : R, Y = up ? -R : P;
-    al = gR * X;
-    be = gL * Y;
-    ga = gC * (uc * fma(W(-2), c, W(3) * sg));
+    const W s = fma(up ? W(-1) : W(1), c, W(1));
+    const W us = u * s;
+    const W P = us * s, R = uc * s;
+    al = gR * (up ? P : R);
+    be = gL * (up ? neg_bits(R) : P);
+    const W G = gC * fma(W(2), R, uc);
+    ga = up ? G : neg_bits(G);
 }
 
 // FP64 records: {u, +-g} (the sign carries the upwind choice) at rec[idx], the coefficients
@@ -200,14 +207,17 @@ struct Clock {
     double f[4];  // deformational: k cos(pi t/T), sin(2 pi t/T), cos(2 pi t/T), 2 pi/T; vf 3: cos(pi t/5)
     double t_old; // time of the previous wind (RK2 extrapolation)
     double hn[4], ho[4];  // time-basis values at t and t_old (basis winds, see wind_basis_h)
+    double hx[4];         // 1.5 hn - 0.5 ho: the basis values of the RK2 extrapolation
     float hnf[4], hof[4]; // the same rounded to FP32 (GB300 converts FP64 at the FP64 rate: once here,
                           // not in every thread of the FP32 record kernel)
 };
 
+// the values derived from hn and ho once per step instead of in every thread of the record kernels
 __device__ __forceinline__ void clock_round(Clock *c) {
     for (int m = 0; m < 4; ++m) {
         c->hnf[m] = (float)c->hn[m];
         c->hof[m] = (float)c->ho[m];
+        c->hx[m] = 1.5 * c->hn[m] - 0.5 * c->ho[m];
     }
 }
 
@@ -351,9 +361,11 @@ struct Coefs {
         for (int m = 0; m < M; ++m) s += c[m] * h[m];
         return s;
     }
-    // the same sum with fused multiply-adds (the FP64 records: every FP64 operation counts)
+    // the same sum with fused multiply-adds (the FP64 records: every FP64 operation counts); the
+    // 4-function basis's first function is the constant 1 (wind_basis_h), and so is its RK2
+    // extrapolation 1.5 - 0.5, so its term is c[0] itself (the product by 1 is exact)
     __device__ __forceinline__ W at_fma(const W *h) const {
-        W s = c[0] * h[0];
+        W s = M == 4 ? c[0] : c[0] * h[0];
 #pragma unroll
         for (int m = 1; m < M; ++m) s = fma(c[m], h[m], s);
         return s;
@@ -923,7 +935,7 @@ __global__ void __launch_bounds__(256) k_wind_rec(Dims d, const W *__restrict__ 
     for (int m = 0; m < M; ++m) {
         if constexpr (F64) {
             hn[m] = clk->hn[m];
-            ho[m] = W(1.5) * clk->hn[m] - W(0.5) * clk->ho[m];  // the extrapolation's time factors
+            ho[m] = clk->hx[m];  // the extrapolation's time factors
         } else {
             hn[m] = clk->hnf[m];
             ho[m] = clk->hof[m];
@@ -940,7 +952,7 @@ __global__ void __launch_bounds__(256) k_wind_rec(Dims d, const W *__restrict__ 
                 Coefs<W, M> c;
                 c.load(B, p * d.plane + (long long)i * d.pitch + j);
                 xs = c.at_fma(ho);
-                xn = c.at_fma(hn);
+                if (r >= 1 && r <= 32) xn = c.at_fma(hn);  // the wind now only on the block's own rows
             }
             sx[r][lane] = xs;
             if (r >= 1 && r <= 32) sn[r - 1][lane] = xn;

@@ -230,8 +230,8 @@ def test_fp32_mass_anchored_over_long_run():
 
 @pytest.mark.parametrize("prec", [32, 64])
 def test_inline_ghost_cells_match_ghost_cell_kernel(prec):
-    """The step kernel's own ghost cells (the FP32 default) and the separate ghost-cell launch
-    (the FP64 default) give the same bits: N = 48 (one tile per panel: every tile touches all
+    """The step kernel's own ghost cells (the default) and the separate ghost-cell launch give
+    the same bits: N = 48 (one tile per panel: every tile touches all
     four panel edges and the corners), N = 120 (interior tiles too), three tracers (a pair and
     an odd one), time-dependent wind with RK2 and MF-PR, several steps; the full-layout fields
     (ghost cells included) agree as well."""
@@ -319,7 +319,7 @@ def test_pipelined_wind_records_follow_every_call_pattern():
 
 @pytest.mark.parametrize("prec,vf,wp,inline", [(64, 2, (0, 0, 0, 0), None), (32, 102, (0.48, 5.0, 0, 0), None),
                                                (32, 101, (0.7, 1.25, 0, 0), None), (32, 102, (0.48, 5.0, 0, 0), False),
-                                               (64, 102, (0.48, 5.0, 0, 0), True)])
+                                               (64, 102, (0.48, 5.0, 0, 0), False)])
 def test_checkpoint_resume_gives_the_same_bits(tmp_path, prec, vf, wp, inline):
     """A run saved after k steps and resumed in a new plan continues with the same bits as the
     run that was not interrupted (time-dependent and static winds, FP64 and FP32 forms, and
