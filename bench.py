@@ -66,11 +66,13 @@ def dt_for_cfl(make_plan):
 
 
 PROFILES = {32: os.path.join(ROOT, "profiles", "k_sweep2_N384_T2.md"),
-            64: os.path.join(ROOT, "profiles", "k_sweep_f64_N384_T2.md")}
-# the sources each step kernel is compiled from: a committed ncu summary states their digest,
-# and its figures are used only while those sources are unchanged
+            64: os.path.join(ROOT, "profiles", "k_sweep_f64_N384_T2.md"),
+            "rec64": os.path.join(ROOT, "profiles", "k_wind_rec_f64_N384.md")}
+# the sources each kernel is compiled from: a committed ncu summary states their digest, and its
+# figures are used only while those sources are unchanged
 KERNEL_SOURCES = {32: ("sweep2.cuh", "fused.cuh", "halo.cuh", "common.cuh", "tiles.h", "sweep_f32_pairs.cu"),
-                  64: ("sweep.cuh", "fused.cuh", "halo.cuh", "common.cuh", "tiles.h", "sweep_f64.cu")}
+                  64: ("sweep.cuh", "fused.cuh", "halo.cuh", "common.cuh", "tiles.h", "sweep_f64.cu"),
+                  "rec64": ("wind.cu", "common.cuh", "internal.h")}
 
 
 def kernel_digest(precision):
@@ -596,29 +598,31 @@ def peaks_file():
         return {}
 
 
-def fp64_roofline(kms, fp64_flops, hbm):
-    """The FP64 step kernel against the FP64 pipe.  Its executed FP64 arithmetic instructions per
-    launch (DFMA + DADD + DMUL, each one issue of the pipe, from the committed ncu summary of this
-    kernel on this workload, used only while the kernel sources are unchanged) over its CUDA-event
-    launch time, against this GPU's DFMA issue rate measured here (csadv_fp64_rate / 2)."""
+def fp64_roofline(step_ms, kms, fp64_flops, hbm):
+    """The FP64 step against the FP64 pipe.  Its two FP64 kernels, the step kernel and the next
+    step's edge records (on a second stream, beside it), are both bound by the FP64 pipe, so the
+    step is the unit: the FP64 arithmetic instructions (DFMA + DADD + DMUL, each one issue of the
+    pipe) that the two execute per step, from the committed ncu summaries of these kernels on this
+    workload (used only while their sources are unchanged), over the CUDA-event step time, against
+    this GPU's DFMA issue rate measured here (csadv_fp64_rate / 2).  `kernel_ms` is the step
+    kernel's own CUDA-event time, with the records running beside it."""
     alg = 6 * N_CELLS * N_CELLS * (NTRACERS * 2 * 8 + 3 * 8)
-    inst = profiled(64, "fp64_inst_per_launch")
-    flops = profiled(64, "fp64_flops_per_launch")
-    hbm_gbs = alg / (kms * 1e-3) / 1e9
+    inst_s, inst_r = profiled(64, "fp64_inst_per_launch"), profiled("rec64", "fp64_inst_per_launch")
+    inst = inst_s + inst_r if inst_s and inst_r else None
+    hbm_gbs = alg / (step_ms * 1e-3) / 1e9
     peak = fp64_flops / 2.0
-    roof = {"bound": "fp64", "kernel": "k_sweep<double, PPM-CW84, AVLT> (FP64 step kernel)", "unit": "T FP64 inst/s",
-            "peak": round(peak / 1e12, 4),
+    roof = {"bound": "fp64", "kernel": "k_sweep<double, PPM-CW84, AVLT> + k_wind_rec<double> (the FP64 step)",
+            "unit": "T FP64 inst/s", "peak": round(peak / 1e12, 4),
             "peak_source": "csadv_fp64_rate (DFMA chains on every SM, measured here) / 2 flop per DFMA",
-            "achieved": None, "frac": None, "kernel_ms": round(kms, 5), "fp64_inst_per_launch": inst,
-            "fp64_flops_per_launch": flops, "traffic": None, "alg_bytes_per_launch": alg,
-            "hbm_gbs": round(hbm_gbs, 1), "hbm_frac": round(hbm_gbs / hbm, 4)}
-    tr = profiled(64, "dram_bytes_per_launch")
-    roof["traffic"] = int(tr) if tr else None
+            "achieved": None, "frac": None, "step_ms": round(step_ms, 5), "kernel_ms": round(kms, 5),
+            "fp64_inst_per_step": inst, "fp64_inst_step_kernel": inst_s, "fp64_inst_records": inst_r,
+            "traffic": None, "alg_bytes_per_step": alg, "hbm_gbs": round(hbm_gbs, 1),
+            "hbm_frac": round(hbm_gbs / hbm, 4)}
+    tr_s, tr_r = profiled(64, "dram_bytes_per_launch"), profiled("rec64", "dram_bytes_per_launch")
+    roof["traffic"] = int(tr_s + tr_r) if tr_s and tr_r else None
     if inst and peak:
-        roof["achieved"] = round(inst / (kms * 1e-3) / 1e12, 4)
-        roof["frac"] = round(inst / (kms * 1e-3) / peak, 4)
-        if flops:
-            roof["achieved_tflops"] = round(flops / (kms * 1e-3) / 1e12, 4)
+        roof["achieved"] = round(inst / (step_ms * 1e-3) / 1e12, 4)
+        roof["frac"] = round(inst / (step_ms * 1e-3) / peak, 4)
     else:
         roof["note"] = "no ncu summary for the current kernel sources: executed FP64 instructions unknown"
     return roof
@@ -686,7 +690,7 @@ def bench_gpu(args):
     hbm = peaks.get("hbm_gbs", 6800.0)
     clk_s = clk.summary()
     mhz = clk_s.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    roof64 = fp64_roofline(f64["kernel_ms"], rate.value, hbm)
+    roof64 = fp64_roofline(ms64, f64["kernel_ms"], rate.value, hbm)
     roof32, issue32 = fp32_roofline(f32["kernel_ms"], hbm, peaks, mhz)
     v64, v32 = job_rate(cells, world, ms64), job_rate(cells, world, ms32)
     line = {
