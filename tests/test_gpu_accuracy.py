@@ -107,3 +107,24 @@ def test_deformational_flow_N384_to_T_fp64_and_fp32():
         assert dm64 < 1e-12
         assert dm32 < 1e-6
         assert rel(q32, q64) < 1e-3
+
+
+def test_fp32_mass_sums_hold_at_N1536():
+    """The FP32 form sums its MF-PR partials (sum of Q g per tracer) in FP32 within a thread's
+    march line (up to 55 cells) and a warp's butterfly, and in FP64 across warps and CTAs.  At
+    N = 1536 (14.2 M cells per tracer, 4704 tiles), an error e in those sums would move each
+    tracer's mass by about e: over 50 steps of the divergent wind at CFL 0.7 the mass, computed in
+    FP64 from the FP32 state, stays within 1e-7 of its initial value (the FP32 state's own
+    rounding is 6e-8 per cell)."""
+    from csadv import Plan
+    kw = dict(vf=103, wind_param=(math.pi / 4, 2 * math.pi / 5, 0.3, 0.0), ntracers=2, precision=32, **SCHEME)
+    with Plan(1536, -0.7, **kw) as pl:
+        pl.init_tracer(101, ic_param=(0.0, 0.2, 5.0, 0.0), tracer=0)
+        pl.init_tracer(102, tracer=1)
+        m0 = [pl.mass(t) for t in range(2)]
+        pl.advance(50)
+        dm = [abs(pl.mass(t) - m0[t]) / abs(m0[t]) for t in range(2)]
+        q = pl.get_tracer(0)
+    print("N=1536 FP32, 50 steps: relative mass change %s" % dm)
+    assert np.all(np.isfinite(q))
+    assert max(dm) < 1e-7
