@@ -234,6 +234,11 @@ int csadv_batch_add(csadv_batch *batch, csadv_plan *plan);       /* CSADV_ERR_TO
 int csadv_batch_remove(csadv_batch *batch, csadv_plan *plan);
 int csadv_batch_size(const csadv_batch *batch, int *n);
 int csadv_batch_advance(csadv_batch *batch, int nsteps, void *stream);
+/* depth > 0: csadv_batch_advance first waits until the call `depth` calls before it has finished
+ * on the device, so the host runs at most `depth` calls ahead of the GPU (a serving loop then sees
+ * finished solves, and frees their memory, within that many calls); 0 (the default): no wait.
+ * CSADV_ERR_ARG outside 0..64. */
+int csadv_batch_set_queue_depth(csadv_batch *batch, int depth);
 int csadv_batch_set_graphs(csadv_batch *batch, int enable);
 /* profiling: steps launch directly and the step kernel is timed (csadv_stats.main_ms) */
 int csadv_batch_set_profiling(csadv_batch *batch, int enable);

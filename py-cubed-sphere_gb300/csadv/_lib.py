@@ -88,6 +88,7 @@ _SIGS = {
     "csadv_batch_remove": ([_vp, _vp], _c_int),
     "csadv_batch_size": ([_vp, ctypes.POINTER(_c_int)], _c_int),
     "csadv_batch_advance": ([_vp, _c_int, _vp], _c_int),
+    "csadv_batch_set_queue_depth": ([_vp, _c_int], _c_int),
     "csadv_batch_set_graphs": ([_vp, _c_int], _c_int),
     "csadv_batch_get_stats": ([_vp, ctypes.POINTER(Stats)], _c_int),
     "csadv_batch_set_profiling": ([_vp, _c_int], _c_int),

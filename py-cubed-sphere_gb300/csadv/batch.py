@@ -50,6 +50,10 @@ class Batch:
     def advance(self, nsteps, stream=None):
         L.check(L.lib().csadv_batch_advance(self._h, int(nsteps), L.stream_handle(stream)), "csadv_batch_advance")
 
+    def set_queue_depth(self, depth):
+        """advance() waits until the call `depth` calls back has finished on the GPU (0: never)."""
+        L.check(L.lib().csadv_batch_set_queue_depth(self._h, int(depth)), "csadv_batch_set_queue_depth")
+
     def set_graphs(self, enable):
         L.check(L.lib().csadv_batch_set_graphs(self._h, int(bool(enable))), "csadv_batch_set_graphs")
 

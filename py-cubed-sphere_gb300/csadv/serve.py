@@ -18,6 +18,7 @@ The reference has no counterpart (it runs one solve per process: advection_spher
 import collections
 import dataclasses
 import math
+import sys
 import time
 
 import numpy as np
@@ -132,7 +133,10 @@ class Server:
     nothing is resident, the requests admitted together are awaited and start together.  A plan
     that has been read out is freed by the loop at once, in the order of `stream`
     (csadv_plan_release: nothing waits for the device), and its memory is reused by the next
-    plans from the library's pool.  Without the two streams everything runs inline on `stream`.
+    plans from the library's pool.  The loop runs at most `queue_depth` ticks ahead of the GPU
+    (csadv_batch_set_queue_depth), so a solve's end is seen, and its memory reused, within that
+    many ticks of its last step on the device instead of a full launch queue later.  Without the
+    two streams everything runs inline on `stream`.
 
     Failures stay with their request: a request whose plan cannot be made (bad size, no
     memory), whose state turns non-finite, or that waits past its deadline gets a Result with
@@ -140,7 +144,8 @@ class Server:
     for every queued request at every step boundary, not only for the head of the queue."""
 
     def __init__(self, budget_bytes, precision=32, cfl=0.5, max_active=512, stream=None, clock=time.perf_counter,
-                 keep_state=False, max_steps_per_tick=8, threads=None, build_stream=None, device=None, builders=2):
+                 keep_state=False, max_steps_per_tick=8, threads=None, build_stream=None, device=None, builders=2,
+                 queue_depth=2):
         self.budget = int(budget_bytes)
         self.precision = precision
         self.cfl = cfl
@@ -153,6 +158,7 @@ class Server:
         self.max_steps_per_tick = max_steps_per_tick
         self.threads = (stream is not None and build_stream is not None) if threads is None else bool(threads)
         self.builders = builders
+        self.queue_depth = queue_depth
         self._coef = {}
 
     # device bytes of a plan ~ plane elements x (a + b T), per wind kind; measured once
@@ -189,7 +195,8 @@ class Server:
 
     def _retire(self, pl, req, admitted, mass0, t0, realtime):
         """Result of a finished solve (error norms, mass change, optionally its fields), read on
-        the loop's stream after the solve's last step."""
+        the loop's stream after the solve's last step; then the plan is freed in that stream's
+        order (it has left the batch, and every step that used it was queued before)."""
         try:
             errs, dm = finish(pl, req, mass0)  # synchronises the plan's stream
             failed = None
@@ -197,6 +204,9 @@ class Server:
             errs, dm, failed = [], [], str(e)
         state = [pl.get_tracer(t) for t in range(req.tracers)] if self.keep_state else None
         fin = self.clock() - t0
+        tr = time.perf_counter()
+        pl.release(self.stream)
+        self._release_s += time.perf_counter() - tr
         res = Result(req.rid, req.N, req.tracers, req.steps, req.arrival if realtime else 0.0, admitted, fin, errs,
                      dm, 0 if failed else 6 * req.N * req.N * req.tracers * req.steps, error=failed)
         res.state = state
@@ -214,13 +224,18 @@ class Server:
         used = 0
         results = []
         batch = Batch(self.max_active)
+        if self.threads:  # finished solves are seen (and their memory freed) within two ticks
+            batch.set_queue_depth(self.queue_depth)
         t0 = self.clock()
         steps = 0
         peak = 0
         members_changed = 0
         build_s = 0.0
-        release_s = 0.0
+        self._release_s = 0.0
         advance_s = 0.0
+        switch = sys.getswitchinterval()
+        if self.threads:  # the loop, builders and retirement hand the interpreter over quickly
+            sys.setswitchinterval(min(switch, 2e-4))
         builder = retirer = None
         if self.threads:
             builder = cf.ThreadPoolExecutor(max_workers=self.builders, initializer=self._thread_init)
@@ -234,15 +249,12 @@ class Server:
                 f.set_exception(e)
             return f
 
-        def collect_retired(block=False):  # results of the plans read out; their memory is freed
-            nonlocal used, release_s
+        def collect_retired(block=False):  # results of the plans read out and freed
+            nonlocal used
             keep = []
             for item in retiring:
                 if block or item[0].done():
                     results.append(item[0].result())
-                    tr = time.perf_counter()
-                    item[1].release(self.stream)
-                    release_s += time.perf_counter() - tr
                     used -= item[2]
                 else:
                     keep.append(item)
@@ -345,6 +357,7 @@ class Server:
                 st = batch.stats()
                 graph_builds, graph_ms = st.get("graph_builds", 0), round(st.get("graph_build_ms", 0.0), 1)
             batch.close()
+            sys.setswitchinterval(switch)
         wall = self.clock() - t0
         served = [r for r in results if r.error is None]
         lat = np.array([r.latency for r in served]) if served else np.zeros(1)
@@ -355,7 +368,7 @@ class Server:
                    "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                    "batch_steps": steps, "peak_bytes": peak, "budget_bytes": self.budget,
                    "membership_changes": members_changed, "plan_build_s": round(build_s, 3),
-                   "release_s": round(release_s, 3), "advance_s": round(advance_s, 3), "graph_builds": graph_builds, "graph_build_ms": graph_ms,
+                   "release_s": round(self._release_s, 3), "advance_s": round(advance_s, 3), "graph_builds": graph_builds, "graph_build_ms": graph_ms,
                    "max_mass_change": max((max(r.mass_change) for r in served), default=0.0)}
         return results, summary
 

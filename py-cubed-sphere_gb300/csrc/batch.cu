@@ -45,6 +45,10 @@ struct csadv_batch {
     int gkernels[2] = {0, 0};
     bool prof = false;               // time the step kernel (direct launches)
     cudaEvent_t pev[2] = {nullptr, nullptr};
+    // csadv_batch_set_queue_depth: the ends of the last `qdepth` advance calls
+    int qdepth = 0;
+    long long qn = 0;
+    std::vector<cudaEvent_t> qev;
     csadv_stats stats{};
     void drop_graphs() {
         for (auto &e : gexec)
@@ -60,6 +64,7 @@ struct csadv_batch {
         if (cap) cudaStreamDestroy(cap);
         for (auto &e : pev)
             if (e) cudaEventDestroy(e);
+        for (auto &e : qev) cudaEventDestroy(e);
     }
 };
 
@@ -330,6 +335,11 @@ int csadv_batch_advance(csadv_batch *b, int nsteps, void *stream) {
     if (!b || nsteps < 0) return CSADV_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (b->plans.empty()) return CSADV_OK;
+    cudaEvent_t qe = nullptr;
+    if (b->qdepth > 0) {  // the advance `qdepth` calls back has finished before this one is queued
+        qe = b->qev[b->qn % b->qdepth];
+        if (b->qn >= b->qdepth) CSADV_CUDA(cudaEventSynchronize(qe));
+    }
     for (int s = 0; s < nsteps; ++s) {
         if (batch_stale(b)) {
             int rc = batch_rebuild(b, st);
@@ -338,6 +348,25 @@ int csadv_batch_advance(csadv_batch *b, int nsteps, void *stream) {
         int rc = batch_run_step(b, 1, st);
         if (rc) return rc;
     }
+    if (qe) {
+        CSADV_CUDA(cudaEventRecord(qe, st));
+        b->qn += 1;
+    }
+    return CSADV_OK;
+}
+
+int csadv_batch_set_queue_depth(csadv_batch *b, int depth) {
+    if (!b || depth < 0 || depth > 64) return CSADV_ERR_ARG;
+    for (auto &e : b->qev) cudaEventDestroy(e);  // (a pending record completes on its own)
+    b->qev.clear();
+    b->qdepth = 0;
+    b->qn = 0;
+    for (int k = 0; k < depth; ++k) {
+        cudaEvent_t e = nullptr;
+        CSADV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming | cudaEventBlockingSync));
+        b->qev.push_back(e);
+    }
+    b->qdepth = depth;
     return CSADV_OK;
 }
 

@@ -149,3 +149,31 @@ def test_tune_keeps_state_and_is_remembered():
             np.testing.assert_array_equal(a, r)
     with make(m, 32) as later:  # default tile = the tuned one
         assert later.stats()["tile"] == tile
+
+
+def test_queue_depth_keeps_results():
+    """With the host held at most one or three advance calls ahead of the GPU the batch gives the
+    same bits as without; depths outside 0..64 are refused."""
+    from csadv import Batch, CsadvError
+    ref = []
+    for depth in (0, 1, 3):
+        plans = [make(m, 32) for m in MEMBERS[:3]]
+        with Batch(8) as b:
+            b.set_queue_depth(depth)
+            for pl in plans:
+                b.add(pl)
+            for _ in range(7):
+                b.advance(2)
+            out = [pl.get_tracer(t) for pl in plans for t in range(pl.ntracers)]
+            for pl in plans:
+                b.remove(pl)
+        for pl in plans:
+            pl.close()
+        if depth == 0:
+            ref = out
+        else:
+            for a, r in zip(out, ref):
+                np.testing.assert_array_equal(a, r)
+    with Batch(2) as b:
+        with pytest.raises(CsadvError):
+            b.set_queue_depth(65)

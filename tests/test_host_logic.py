@@ -161,6 +161,9 @@ class _FakeBatch:
         for pl in self.members:
             pl.step += k
 
+    def set_queue_depth(self, depth):
+        self.depth = depth
+
     def close(self):
         pass
 
