@@ -50,8 +50,38 @@ __host__ __device__ inline void panel_xyz(int p, double invD, double XoD, double
 }
 
 // equiangular tangent vectors (cs_transform.py:245-397): the equidistant tangent at
-// (a tan x, a tan y) scaled by a / cos^2
-__device__ inline void tangents(int p, double x, double y, double ex[3], double ey[3]) {
+// (a tan x, a tan y) scaled by a / cos^2, from the per-axis values tx = tan x, sx = a / cos^2 x
+// (and ty, sy); |r|^3 is formed as r^2 |r|
+__device__ inline void tangents(int p, double tx, double sx, double ty, double sy, double ex[3], double ey[3]) {
+    const double a = 1.0 / sqrt(3.0);
+    double xe = a * tx, ye = a * ty;
+    double r2 = a * a + xe * xe + ye * ye;
+    double invr = 1.0 / (r2 * sqrt(r2));
+    double a2 = a * a, ax = a * xe, ay = a * ye, xy = xe * ye;
+    double bx = (a2 + ye * ye) * invr, by = (a2 + xe * xe) * invr;
+    double axr = ax * invr, ayr = ay * invr, xyr = xy * invr;
+    switch (p) {
+        case 0: ex[0] = -axr; ex[1] = bx; ex[2] = -xyr; ey[0] = -ayr; ey[1] = -xyr; ey[2] = by; break;
+        case 1: ex[0] = -bx; ex[1] = -axr; ex[2] = -xyr; ey[0] = xyr; ey[1] = -ayr; ey[2] = by; break;
+        case 2: ex[0] = axr; ex[1] = -bx; ex[2] = -xyr; ey[0] = ayr; ey[1] = xyr; ey[2] = by; break;
+        case 3: ex[0] = bx; ex[1] = axr; ex[2] = -xyr; ey[0] = -xyr; ey[1] = ayr; ey[2] = by; break;
+        case 4: ex[0] = xyr; ex[1] = bx; ex[2] = -axr; ey[0] = -by; ey[1] = -xyr; ey[2] = -ayr; break;
+        default: ex[0] = -xyr; ex[1] = bx; ex[2] = axr; ey[0] = by; ey[1] = -xyr; ey[2] = ayr; break;
+    }
+    for (int c = 0; c < 3; ++c) {
+        ex[c] = ex[c] * sx;
+        ey[c] = ey[c] * sy;
+    }
+}
+// the per-axis values of `tangents` for angle x
+__host__ __device__ inline void axis_values(double x, double &t, double &sc) {
+    const double c = cos(x);
+    t = tan(x);
+    sc = (1.0 / sqrt(3.0)) / (c * c);
+}
+// the same vectors with the reference's sequence of operations per point (r^3 as a power, the
+// scaling as a division): the grid file's tangent arrays, compared element by element
+__device__ inline void tangents_file(int p, double x, double y, double ex[3], double ey[3]) {
     const double a = 1.0 / sqrt(3.0);
     double xe = a * tan(x), ye = a * tan(y);
     double r2 = a * a + xe * xe + ye * ye;
@@ -81,7 +111,14 @@ struct PointOut {
     double *metric;      // single plane
 };
 
-__global__ void k_grid_points(Dims d, const double *__restrict__ xs, int nx, const double *__restrict__ ys, int ny,
+// One thread per point (panel p, row i, column j) of a family of points over the axes with
+// per-axis tables {tan, a / cos^2} (ax[2 i], ax[2 i + 1]; ay likewise): position, lon/lat, the
+// tangent vectors' lon/lat components, and (panel 0) the metric.  The unit vectors
+// e_lon = (-sin lon, cos lon, 0) and e_lat = (-sin lat cos lon, -sin lat sin lon, cos lat) are
+// formed from the position itself (cos lon = X/h, sin lon = Y/h, cos lat = h, sin lat = Z with
+// h = hypot(X, Y)), not from sines and cosines of the angles; on the polar axis (h = 0) from the
+// angles as atan2 gives them.
+__global__ void k_grid_points(Dims d, const double *__restrict__ ax, int nx, const double *__restrict__ ay, int ny,
                               PointOut out) {
     long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     long long total = (long long)NFACE * nx * ny;
@@ -89,20 +126,32 @@ __global__ void k_grid_points(Dims d, const double *__restrict__ xs, int nx, con
     int j = (int)(tid % ny);
     int i = (int)((tid / ny) % nx);
     int p = (int)(tid / ((long long)nx * ny));
-    double x = xs[i], y = ys[j];
-    double tx = tan(x), ty = tan(y);
+    const double tx = ax[2 * i], sx = ax[2 * i + 1], ty = ay[2 * j], sy = ay[2 * j + 1];
     double D = sqrt(1.0 + tx * tx + ty * ty);
     double invD = 1.0 / D;
     double X, Y, Z;
     panel_xyz(p, invD, invD * tx, invD * ty, X, Y, Z);
+    const double h = hypot(X, Y);
     double lon = atan2(Y, X);
-    double lat = atan2(Z, hypot(X, Y));
+    double lat = atan2(Z, h);
     long long o = at(d, p, i, j);
     out.lon[o] = lon;
     out.lat[o] = lat;
     double ex[3], ey[3];
-    tangents(p, x, y, ex, ey);
-    double sl = sin(lon), cl = cos(lon), sp = sin(lat), cp = cos(lat);
+    tangents(p, tx, sx, ty, sy, ex, ey);
+    double sl, cl, sp, cp;
+    if (h > 0.0) {
+        const double ih = 1.0 / h;
+        sl = Y * ih;
+        cl = X * ih;
+        sp = Z;
+        cp = h;
+    } else {
+        sl = sin(lon);
+        cl = cos(lon);
+        sp = sin(lat);
+        cp = cos(lat);
+    }
     double elon[3] = {-sl, cl, 0.0};
     double elat[3] = {-sp * cl, -sp * sl, cp};
     double exlon = ex[0] * elon[0] + ex[1] * elon[1] + ex[2] * elon[2];
@@ -148,7 +197,7 @@ __global__ void k_grid_file(const double *__restrict__ xs, int nx, const double 
     }
     if (EX || EY) {
         double ex[3], ey[3];
-        tangents(p, x, y, ex, ey);
+        tangents_file(p, x, y, ex, ey);
         for (int c = 0; c < 5; ++c) {
             if (EX) EX[o + c] = c < 3 ? ex[c] : 0.0;
             if (EY) EY[o + c] = c < 3 ? ey[c] : 0.0;
@@ -156,23 +205,30 @@ __global__ void k_grid_file(const double *__restrict__ xs, int nx, const double 
     }
 }
 
-// sum of g_pc^2 over the interior of all panels (discrete_operators.py:99), fixed order
-__global__ void k_sum_g2(Dims d, const double *__restrict__ g, double *out) {
-    __shared__ double red[1024];
+// sum of g_pc^2 over the interior of all panels (discrete_operators.py:99), fixed order: block b
+// of G2_BLOCKS sums cells b*256 + tid, stepping by the grid, into part[b]; then part in block order
+constexpr int G2_BLOCKS = 64;
+__global__ void k_sum_g2(Dims d, const double *__restrict__ g, double *part) {
+    __shared__ double red[256];
     double acc = 0.0;
-    long long cnt = (long long)d.N * d.N;
-    for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const long long cnt = (long long)d.N * d.N;
+    for (long long t = blockIdx.x * 256LL + threadIdx.x; t < cnt; t += (long long)gridDim.x * 256) {
         int i = d.i0 + (int)(t / d.N), j = d.i0 + (int)(t % d.N);
         double v = g[at2(d, i, j)];
         acc += v * v;
     }
     red[threadIdx.x] = acc;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    for (int s = 128; s > 0; s >>= 1) {
         if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = 6.0 * red[0];
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+__global__ void k_sum_g2_final(const double *__restrict__ part, int n, double *out) {
+    double s = 0.0;
+    for (int b = 0; b < n; ++b) s += part[b];
+    *out = 6.0 * s;
 }
 
 // ---------------------------------------------------------------- Lagrange tables (host)
@@ -324,8 +380,13 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     double *cu[5], *cv[5], *cc[4];
     for (int c = 0; c < 5; ++c) { cu[c] = mem.alloc<double>(P6); cv[c] = mem.alloc<double>(P6); }
     for (int c = 0; c < 4; ++c) cc[c] = mem.alloc<double>(P6);
-    double *xs_dev = mem.alloc<double>(xc.size() + xe.size());
-    double *a2 = mem.alloc<double>(1);
+    // per-axis {tan, a / cos^2} of the centre and edge angles (the grid points' 1-D factors)
+    std::vector<double> axes(2 * (xc.size() + xe.size()));
+    for (size_t k = 0; k < xc.size(); ++k) axis_values(xc[k], axes[2 * k], axes[2 * k + 1]);
+    for (size_t k = 0; k < xe.size(); ++k)
+        axis_values(xe[k], axes[2 * (xc.size() + k)], axes[2 * (xc.size() + k) + 1]);
+    double *xs_dev = mem.alloc<double>(axes.size());
+    double *a2 = mem.alloc<double>(1 + G2_BLOCKS);  // the sum, then the blocks' partials
     std::vector<double> lw;
     std::vector<int> lk;
     int rc = lagrange_tables(N, xc, dx, lw, lk);
@@ -337,12 +398,11 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     GhostTerm *gcorner = mem.alloc<GhostTerm>(GHOST_CORNER_TERMS * ncorner);
     if (!mem.ok()) return CSADV_ERR_OOM;
     for (double *g : {g_pc, g_pu, g_pv}) CSADV_CUDA(cudaMemsetAsync(g, 0, P1 * sizeof(double), st));
-    CSADV_CUDA(cudaMemcpyAsync(xs_dev, xc.data(), xc.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    CSADV_CUDA(cudaMemcpyAsync(xs_dev + xc.size(), xe.data(), xe.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaMemcpyAsync(xs_dev, axes.data(), axes.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(lag_w, lw.data(), lw.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaMemcpyAsync(lag_k, lk.data(), lk.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     k_ghost_tables<<<ceil_div(nside + ncorner, 128), 128, 0, st>>>(d, lag_w, lag_k, gside, gcorner);
-    const double *xcd = xs_dev, *xed = xs_dev + xc.size();
+    const double *xcd = xs_dev, *xed = xs_dev + 2 * xc.size();
     const int n = d.n;
     PointOut o;
     o.lon = lon_pc; o.lat = lat_pc; o.metric = g_pc;
@@ -357,7 +417,8 @@ int build_grid(int N, DeviceArena &mem, Grid &grid, cudaStream_t st) {
     o.lon = lon_pv; o.lat = lat_pv; o.metric = g_pv;
     for (int c = 0; c < 5; ++c) o.coef[c] = cv[c];
     k_grid_points<<<ceil_div(tot, 128), 128, 0, st>>>(d, xcd, n, xed, n + 1, o);
-    k_sum_g2<<<1, 1024, 0, st>>>(d, g_pc, a2);
+    k_sum_g2<<<G2_BLOCKS, 256, 0, st>>>(d, g_pc, a2 + 1);
+    k_sum_g2_final<<<1, 1, 0, st>>>(a2 + 1, G2_BLOCKS, a2);
     CSADV_CUDA(cudaGetLastError());
     double a2h = 0.0;
     CSADV_CUDA(cudaMemcpyAsync(&a2h, a2, sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -291,9 +291,11 @@ __device__ void wind_basis_h(const WindParams &wp, int tkind, double t, double h
     }
 }
 
-// coefficient field m on the interior edges (the other entries of u, v are left as they are)
+// the M coefficient fields of the interior edges (the other entries are left as they are):
+// field m of the x-edges at u + m * field, of the y-edges at v + m * field; each edge's
+// trigonometry is evaluated once for all of them
 template <class W>
-__global__ void k_wind_basis(Grid g, WindParams wp, int m, int tkind, W *u, W *v) {
+__global__ void k_wind_basis(Grid g, WindParams wp, int M, int tkind, W *u, W *v) {
     const Dims d = g.d;
     const int N = d.N;
     long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -308,26 +310,23 @@ __global__ void k_wind_basis(Grid g, WindParams wp, int m, int tkind, W *u, W *v
     long long o = at(d, p, i, j);
     const double *lon = which == 0 ? g.lon_pu : g.lon_pv, *lat = which == 0 ? g.lat_pu : g.lat_pv;
     const double *const *cf = which == 0 ? g.cu : g.cv;
+    W *out = (which == 0 ? u : v) + o;
     // contravariant = a * ulon + b * vlat  (sphgeo.py:120-125)
     const double ca = which == 0 ? cf[3][o] / cf[4][o] : -cf[1][o] / cf[4][o];
     const double cb = which == 0 ? -cf[2][o] / cf[4][o] : cf[0][o] / cf[4][o];
-    double c;
     if (tkind == 1) {
         const double L = lon[o], P = lat[o];
         const double Tp = wp.vf == 2 ? 5.0 : wp.prm[1];
         const double s2p = sin(2.0 * P), cp = cos(P), s2l = sin(2.0 * L), c2l = cos(2.0 * L);
-        switch (m) {
-            case 0: c = ca * (2.0 * PI / Tp) * cp; break;
-            case 1: c = ca * 0.5 * s2p; break;
-            case 2: c = -ca * 0.5 * s2p * c2l + cb * cp * s2l; break;
-            default: c = -ca * 0.5 * s2p * s2l - cb * cp * c2l; break;
-        }
+        out[0] = (W)(ca * (2.0 * PI / Tp) * cp);
+        out[d.field] = (W)(ca * 0.5 * s2p);
+        out[2 * d.field] = (W)(-ca * 0.5 * s2p * c2l + cb * cp * s2l);
+        out[3 * d.field] = (W)(-ca * 0.5 * s2p * s2l - cb * cp * c2l);
     } else {
         double ulon, vlat;
         wind_latlon(wp.vf, wp.prm, lon[o], lat[o], 0.0, ulon, vlat);  // vf 3 at t = 0 (h = 1); vf 4
-        c = ca * ulon + cb * vlat;
+        out[0] = (W)(ca * ulon + cb * vlat);
     }
-    (which == 0 ? u : v)[o] = (W)c;
 }
 
 // the basis coefficients of edge o (M = 4: one vector load)
@@ -1009,19 +1008,36 @@ static int basis_setup_t(const Options &o, const Grid &g, Winds &w, DeviceArena 
     if (!mem.ok()) return CSADV_ERR_OOM;
     const size_t F = (size_t)d.field * sizeof(W);
     const long long tot = 2LL * NFACE * (d.N + 1) * d.N;
-    for (int m = 0; m < M; ++m) {
+    // the interior coefficients of all M fields in one pass, into a scratch of 2 M fields (freed
+    // in stream order at the end)
+    W *scr = nullptr;
+    cudaMemPool_t pool = device_pool();
+    if (!pool || cudaMallocFromPoolAsync((void **)&scr, 2 * M * F, pool, st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return CSADV_ERR_OOM;
+    }
+    int rc = CSADV_OK;
+    if (cudaMemsetAsync(scr, 0, 2 * M * F, st) != cudaSuccess) rc = CSADV_ERR_CUDA;
+    if (!rc) {
+        k_wind_basis<W><<<ceil_div(tot, 128), 128, 0, st>>>(g, wparams(o), M, w.tkind, scr, scr + (size_t)M * d.field);
+        if (cudaGetLastError() != cudaSuccess) rc = CSADV_ERR_CUDA;
+    }
+    for (int m = 0; m < M && !rc; ++m) {
         // the halo of coefficient field m, computed with the reference's wind-halo operators
-        CSADV_CUDA(cudaMemsetAsync(w.u_pu, 0, F, st));
-        CSADV_CUDA(cudaMemsetAsync(w.v_pv, 0, F, st));
-        k_wind_basis<W><<<ceil_div(tot, 128), 128, 0, st>>>(g, wparams(o), m, w.tkind, (W *)w.u_pu, (W *)w.v_pv);
-        CSADV_CUDA(cudaGetLastError());
-        int rc = wind_halo(o, g, w, st);
-        if (rc) return rc;
+        if (cudaMemcpyAsync(w.u_pu, scr + (size_t)m * d.field, F, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(w.v_pv, scr + (size_t)(M + m) * d.field, F, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+            rc = CSADV_ERR_CUDA;
+            break;
+        }
+        rc = wind_halo(o, g, w, st);
+        if (rc) break;
         const int nb = ceil_div(d.field, 256);
         k_interleave<W><<<nb, 256, 0, st>>>((const W *)w.u_pu, (W *)w.btab[0], d.field, M, m);
         k_interleave<W><<<nb, 256, 0, st>>>((const W *)w.v_pv, (W *)w.btab[1], d.field, M, m);
-        CSADV_CUDA(cudaGetLastError());
+        if (cudaGetLastError() != cudaSuccess) rc = CSADV_ERR_CUDA;
     }
+    cudaFreeAsync(scr, st);
+    if (rc) return rc;
     CSADV_CUDA(cudaMemsetAsync(w.u_pu, 0, F, st));
     CSADV_CUDA(cudaMemsetAsync(w.v_pv, 0, F, st));
     {  // the record kernel reads the y coefficients transposed
