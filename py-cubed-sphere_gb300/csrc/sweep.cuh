@@ -85,6 +85,8 @@ __device__ __forceinline__ bool mag_lt(const Bits &x, const Bits &y) {
 // c ? a : b on the bit patterns
 __device__ __forceinline__ Bits bsel(bool c, const Bits &a, const Bits &b) { return Bits(c ? a.h : b.h, c ? a.l : b.l); }
 __device__ __forceinline__ double dsel(bool c, double a, double b) { return bsel(c, Bits(a), Bits(b)).d(); }
+// -x by the sign bit
+__device__ __forceinline__ double neg_d(double x) { return Bits(Bits(x).h ^ (int)0x80000000, Bits(x).l).d(); }
 __device__ __forceinline__ float dsel(bool c, float a, float b) { return c ? a : b; }
 // the order of finite values (+0 and -0 equal): x > y
 __device__ __forceinline__ bool ord_gt(const Bits &x, const Bits &y) {
@@ -226,21 +228,21 @@ __device__ __forceinline__ double cw84_slope_d(double a, double b, double c) {
 __device__ __forceinline__ double cw84_edge_d(double qa, double qb, double sa, double sb) {
     return fma(-(sb - sa), 1.0 / 6.0, pow2_scale<-1>(qb + qa));
 }
+// The limiter in the offsets u = R - qc, v = qc - L.  The reference's tests (reconstruction_1d.py:
+// 102-153) with dq = u + v and q6 = 3 (v - u): flattened when u v <= 0 (the extremum test); for a
+// cell that is not flattened (u, v of one sign) the overshoot tests |dq| < |q6| and
+// dq (qc - (R + L)/2) >< +-dq^2/6 hold exactly when |v| > 2|u| (L moves to 3 qc - 2 R = qc - 2u)
+// or |u| > 2|v| (R moves to 3 qc - 2 L = qc + 2v).  At the ties a rounding could decide, both
+// branches give the same parabola (|v| = 2|u| makes qc - 2u = L).  FP64 work: u, v and the
+// moved edge; the rest is integer work on the bit patterns (2|u|, 2|v| exact on the exponent).
 __device__ __forceinline__ void cw84_limit_d(double qc, double &L, double &R) {
-    const double dq = R - L, RpL = R + L;
-    const double q3 = fma(2.0, qc, qc);  // 3 qc, one rounding
-    const double q6 = fma(-3.0, RpL, pow2_scale<1>(q3));
-    const Bits bR(R), bq(qc), bL(L), bd(dq), b6(q6);
-    const bool flat = !((ord_gt(bR, bq) && ord_gt(bq, bL)) || (ord_gt(bq, bR) && ord_gt(bL, bq)));
-    // A cell that is not flattened has R != L, so dq != 0; with |dq| < |q6| the reference's tests
-    // dq (qc - (R + L)/2) > dq^2/6 and -dq^2/6 > dq (qc - (R + L)/2), i.e. q6/dq > 1 and q6/dq < -1,
-    // are the signs of q6 and dq agreeing (move left) or not (move right).  Where a rounding of
-    // the reference's products could decide a tie the other way, both branches give the same
-    // parabola (q6 = +-dq makes 3 qc - 2 R = L and 3 qc - 2 L = R).
-    const bool over = !flat && mag_lt(bd, b6);
-    const bool same = (bd.h ^ b6.h) >= 0;
-    const bool ml = over && same, mr = over && !same;
-    const double T = fma(-2.0, dsel(ml, R, L), q3);  // 3 qc - 2 R (move left), 3 qc - 2 L (move right)
+    const double u = R - qc, v = qc - L;
+    const Bits bu(u), bv(v);
+    const bool flat = !((bu.h ^ bv.h) >= 0 && !bu.zero() && !bv.zero());  // u v <= 0
+    const Bits mu(bu.mh(), bu.l), mv(bv.mh(), bv.l);                     // |u|, |v|
+    const bool ml = !flat && mag_lt(mag_scale<1>(mu), mv);              // |v| > 2|u|
+    const bool mr = !flat && mag_lt(mag_scale<1>(mv), mu);              // |u| > 2|v|
+    const double T = qc - dsel(ml, pow2_scale<1>(u), neg_d(pow2_scale<1>(v)));  // qc - 2u or qc + 2v
     const double Lk = dsel(ml, T, L), Rk = dsel(mr, T, R);
     L = dsel(flat, qc, Lk);
     R = dsel(flat, qc, Rk);

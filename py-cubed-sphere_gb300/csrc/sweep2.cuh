@@ -129,26 +129,22 @@ __device__ __forceinline__ V cw84_edge2(V qa, V qb, V Sa, V Sb) {
     return vfma(vsub(Sb, Sa), bc<V>(-1.0f / 6.0f), vadd(qa, qb));
 }
 // CW84 monotonicity limiter (reconstruction_1d.py:102-153) on the doubled parabola (L2, R2) of
-// the cell with doubled mean Q2.  With dq = R - L and q6 = 6 q - 3 (R + L) taken before the
-// flattening, the reference's overshoot tests (R - L)(q - (R + L)/2) >< +-(R - L)^2 / 6 on the
-// flattened values never fire for a flattened cell; for one that is not flattened (R != L, so
-// dq != 0) they read q6/dq > 1 and q6/dq < -1, which under |dq| < |q6| are the signs of q6 and
-// dq agreeing (move left) or not (move right).  At the ties a rounding could decide, both branches
-// give the same parabola.  3 q - 2 R = q - 2 (R - q) and 3 q - 2 L = q + 2 (q - L).
+// the cell with doubled mean Q2, in the offsets u = R - q, v = q - L: the reference's extremum
+// test (R - q)(q - L) <= 0 flattens the cell; otherwise (u, v of one sign; dq = u + v and
+// q6 = 3 (v - u)) its overshoot tests |dq| < |q6| and dq (q - (R + L)/2) >< +-dq^2/6 hold exactly
+// when |v| > 2|u| (L moves to 3q - 2R = q - 2u) or |u| > 2|v| (R moves to 3q - 2L = q + 2v).  At
+// the ties a rounding could decide, both branches give the same parabola.
 template <class V>
 __device__ __forceinline__ void cw84_limit2(V Q2, V &L2, V &R2) {
-    const V dq = vsub(R2, L2);
-    const V q6 = vmul(vsub(vadd(Q2, Q2), vadd(R2, L2)), bc<V>(3.f));
     const V u = vsub(R2, Q2), v = vsub(Q2, L2);
+    const V u2 = vadd(u, u), v2 = vadd(v, v);
     const V pf = vmul(u, v);
-    const V Ln = vsub(Q2, vadd(u, u)), Rn = vadd(Q2, vadd(v, v));
+    const V Ln = vsub(Q2, u2), Rn = vadd(Q2, v2);
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
         const bool flat = lane(pf, l) <= 0.f;
-        const bool over = !flat && fabsf(lane(dq, l)) < fabsf(lane(q6, l));
-        const bool same = (__float_as_int(lane(dq, l)) ^ __float_as_int(lane(q6, l))) >= 0;
-        const bool ml = over && same;
-        const bool mr = over && !same;
+        const bool ml = !flat && fabsf(lane(v, l)) > fabsf(lane(u2, l));
+        const bool mr = !flat && fabsf(lane(u, l)) > fabsf(lane(v2, l));
         set_lane(L2, l, flat ? lane(Q2, l) : (ml ? lane(Ln, l) : lane(L2, l)));
         set_lane(R2, l, flat ? lane(Q2, l) : (mr ? lane(Rn, l) : lane(R2, l)));
     }
