@@ -228,49 +228,51 @@ __device__ __forceinline__ double cw84_slope_d(double a, double b, double c) {
 __device__ __forceinline__ double cw84_edge_d(double qa, double qb, double sa, double sb) {
     return fma(-(sb - sa), 1.0 / 6.0, pow2_scale<-1>(qb + qa));
 }
-// The limiter in the offsets u = R - qc, v = qc - L.  The reference's tests (reconstruction_1d.py:
-// 102-153) with dq = u + v and q6 = 3 (v - u): flattened when u v <= 0 (the extremum test); for a
-// cell that is not flattened (u, v of one sign) the overshoot tests |dq| < |q6| and
-// dq (qc - (R + L)/2) >< +-dq^2/6 hold exactly when |v| > 2|u| (L moves to 3 qc - 2 R = qc - 2u)
-// or |u| > 2|v| (R moves to 3 qc - 2 L = qc + 2v).  At the ties a rounding could decide, both
-// branches give the same parabola (|v| = 2|u| makes qc - 2u = L).  FP64 work: u, v and the
-// moved edge; the rest is integer work on the bit patterns (2|u|, 2|v| exact on the exponent).
-__device__ __forceinline__ void cw84_limit_d(double qc, double &L, double &R) {
-    const double u = R - qc, v = qc - L;
+// The limiter in the offsets u = R - qc, v = qc - L of a cell's parabola.  The reference's tests
+// (reconstruction_1d.py:102-153) with dq = u + v and q6 = 3 (v - u): flattened when u v <= 0 (the
+// extremum test); for a cell that is not flattened (u, v of one sign) the overshoot tests
+// |dq| < |q6| and dq (qc - (R + L)/2) >< +-dq^2/6 hold exactly when |v| > 2|u| (L moves to
+// 3 qc - 2 R, i.e. v becomes 2u) or |u| > 2|v| (R moves to 3 qc - 2 L, u becomes 2v).  At the
+// ties a rounding could decide, both branches give the same parabola.  No FP64 instruction: the
+// tests, 2|u|, 2|v| and the selections are integer work on the bit patterns.
+__device__ __forceinline__ void cw84_limit_ofs(double u, double v, double &uo, double &vo) {
     const Bits bu(u), bv(v);
     const bool flat = !((bu.h ^ bv.h) >= 0 && !bu.zero() && !bv.zero());  // u v <= 0
     const Bits mu(bu.mh(), bu.l), mv(bv.mh(), bv.l);                     // |u|, |v|
-    const bool ml = !flat && mag_lt(mag_scale<1>(mu), mv);              // |v| > 2|u|
-    const bool mr = !flat && mag_lt(mag_scale<1>(mv), mu);              // |u| > 2|v|
-    const double T = qc - dsel(ml, pow2_scale<1>(u), neg_d(pow2_scale<1>(v)));  // qc - 2u or qc + 2v
-    const double Lk = dsel(ml, T, L), Rk = dsel(mr, T, R);
-    L = dsel(flat, qc, Lk);
-    R = dsel(flat, qc, Rk);
+    const bool ml = mag_lt(mag_scale<1>(mu), mv);                        // |v| > 2|u|
+    const bool mr = mag_lt(mag_scale<1>(mv), mu);                        // |u| > 2|v|
+    uo = dsel(flat, 0.0, dsel(mr, pow2_scale<1>(v), u));
+    vo = dsel(flat, 0.0, dsel(ml, pow2_scale<1>(u), v));
 }
 
 // Marching reconstruction: init() with the window of the first cell, then cell() once per
 // cell (window w[0..4] = q[m-2..m+2]) gives the cell's (L, R) and advances.
 template <class real, int REC>
 struct March;
+// FP64 CW84 in offsets: per cell the limited u' = R - q and v' = q - L (cw84_limit_ofs) instead
+// of the edge values.  With d = q(m+1) - q(m) and ds = s(m+1) - s(m) the edge value between them,
+// E = (q(m) + q(m+1))/2 - ds/6, gives u(m) = E - q(m) = d/2 - ds/6 and v(m+1) = q(m+1) - E =
+// d/2 + ds/6: two fused operations per edge, and the limiter needs no FP64 arithmetic.
 template <>
 struct March<double, REC_CW84> {
-    double s, E, dd;  // slope of the current cell; edge value at its left edge; w[3] - w[2]
+    double s, dd, vm;  // slope of the current cell; w[3] - w[2]; q(m) - E(m - 1/2) of the current cell
     __device__ __forceinline__ void init(const double w[5]) {
         const double d01 = w[1] - w[0], d12 = w[2] - w[1], d23 = w[3] - w[2];
         const double sp = cw84_slope_d(w[2] - w[0], d12, d01);
         s = cw84_slope_d(w[3] - w[1], d23, d12);
-        E = cw84_edge_d(w[1], w[2], sp, s);
+        vm = fma(s - sp, 1.0 / 6.0, pow2_scale<-1>(d12));
         dd = d23;
     }
-    __device__ __forceinline__ void cell(const double w[5], double &L, double &R) {
+    // the limited offsets (uo, vo) of the window's centre cell; advances
+    __device__ __forceinline__ void cell(const double w[5], double &uo, double &vo) {
         const double b = w[4] - w[3];
         const double sn = cw84_slope_d(w[4] - w[2], b, dd);
-        const double En = cw84_edge_d(w[2], w[3], s, sn);
-        L = E;
-        R = En;
-        cw84_limit_d(w[2], L, R);
+        const double ds = sn - s, hd = pow2_scale<-1>(dd);
+        const double u = fma(-ds, 1.0 / 6.0, hd);
+        const double vn = fma(ds, 1.0 / 6.0, hd);
+        cw84_limit_ofs(u, vm, uo, vo);
         s = sn;
-        E = En;
+        vm = vn;
         dd = b;
     }
 };
@@ -330,7 +332,7 @@ struct Line {
     const real *s;
     int ss;
     const V *e, *c;
-    const V *f;     // flux coefficients of edge m: {alpha, beta} at f[m * P], {gamma, 0} at f[m * P + fo]
+    const V *f;     // flux coefficients of edge m: {alpha, beta} at f[m * P], {gamma, sigma} at f[m * P + fo]
     long long fo;   // (flux_coefs and put_record, wind.cu)
 };
 
@@ -364,6 +366,9 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
     // FP64 with AVLT splitting: the cell records carry dt/dx (1/g) (k_cell_records), and the
     // split's (dt/dx / 2)(1/g) is half of it, exactly
     const bool HDT = sizeof(real) == 8 && split == SP_AVLT;
+    // FP64 CW84: the cells' parabolas as limited offsets (u', v') from the mean, and the flux as
+    // sigma mean + alpha u' - beta v' with sigma = alpha + beta + gamma (the record's second word)
+    constexpr bool OFS = sizeof(real) == 8 && REC == REC_CW84;
     real w[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) w[k] = ln.s[(ma - 3 + k) * ln.ss];
@@ -371,7 +376,7 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
     rc.init(w);
     V eA = ln.e[(ma - 1) * P], eN = eA;                          // edge m (m+1 loaded in the loop)
     V fA = ln.f[(ma - 1) * P], fN = fA;                          // its flux coefficients
-    real gA = ln.f[(ma - 1) * P + ln.fo].x, gN = gA;
+    real gA = OFS ? ln.f[(ma - 1) * P + ln.fo].y : ln.f[(ma - 1) * P + ln.fo].x, gN = gA;
     V cC = ln.c[(ma - 1) * P], cN = cC;                          // cell m
     real nw4 = real(0);
     real pL = real(0), pR = real(0), pQ = real(0);  // previous cell's parabola
@@ -382,12 +387,12 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
             nw4 = ln.s[(m + 3) * ln.ss];
             eN = ln.e[(m + 1) * P];
             fN = ln.f[(m + 1) * P];
-            gN = ln.f[(m + 1) * P + ln.fo].x;
+            gN = OFS ? ln.f[(m + 1) * P + ln.fo].y : ln.f[(m + 1) * P + ln.fo].x;
             cN = ln.c[(m + 1) * P];
         }
         const real gl = O::ab(eA.y), gcm = cC.x;
-        real L, R;
-        rc.cell(w, L, R);
+        real L, R;  // the cell's parabola (OFS: R holds u', L holds v')
+        rc.cell(w, OFS ? R : L, OFS ? L : R);
         if (m >= ma) {
             // upwind PPM flux through edge m (flux.py:20-128) from the parabola (q_L, q_R, mean) of
             // the upwind cell (m-1 when the wind is >= 0): F = alpha q_R + beta q_L + gamma mean,
@@ -398,7 +403,8 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
             const bool up = !signbit(eA.y);
             const real ig = igp;
             const real eL = dsel(up, pL, L), eR = dsel(up, pR, R), eQ = dsel(up, pQ, w[2]);
-            const real F = fma(gA, eQ, fma(fA.y, eL, fA.x * eR));
+            // OFS: (eR, eL) are the upwind cell's (u', v')
+            const real F = OFS ? fma(fA.x, eR, fma(-fA.y, eL, gA * eQ)) : fma(gA, eQ, fma(fA.y, eL, fA.x * eR));
             const real cm = split == SP_AVLT ? real(0) : gl * (u * dtdx);  // g u dt/dx at edge m (SP-L04, SP-PL07)
             if (m > ma) {
                 const int k = m - 1;

@@ -63,7 +63,7 @@ struct SweepSolve {
     // edge records {departure-point wind, +-metric at the edge; the sign is the upwind flag,
     // + when the wind is >= 0}: x-edges natural (row i, column j), y-edges transposed (row j,
     // column i); per panel plane, element type vec2 of the state's precision.  FP64: the edges'
-    // flux coefficients {alpha, beta} at erx + ecofs and {gamma, 0} at erx + 2 ecofs (units of
+    // flux coefficients {alpha, beta} at erx + ecofs and {gamma, alpha + beta + gamma} at erx + 2 ecofs (units of
     // double2; flux_coefs and put_record in wind.cu); ecofs 0 in the FP32 form, which has none
     const void *erx, *ery;
     long long ecofs;

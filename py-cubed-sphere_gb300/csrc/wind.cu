@@ -100,7 +100,7 @@ __device__ __forceinline__ void flux_coefs(W u, W g, bool up, W dtdx, const Upwi
 }
 
 // FP64 records: {u, +-g} (the sign carries the upwind choice) at rec[idx], the coefficients
-// {alpha, beta} at rec[idx + cofs] and {gamma, 0} at rec[idx + 2 cofs]; `coefs` false: zero
+// {alpha, beta} at rec[idx + cofs] and {gamma, alpha + beta + gamma} at rec[idx + 2 cofs]; `coefs` false: zero
 // coefficients (an edge no flux goes through)
 __device__ __forceinline__ void put_record(double2 *rec, long long idx, long long cofs, double wind, double g, bool up,
                                            double dtdx, const UpwindMetric<double> &um, const Dims &d, int m, int col,
@@ -109,7 +109,7 @@ __device__ __forceinline__ void put_record(double2 *rec, long long idx, long lon
     double al = 0.0, be = 0.0, ga = 0.0;
     if (coefs) flux_coefs(wind, g, up, dtdx, um, d, m, col, al, be, ga);
     rec[idx + cofs] = make_double2(al, be);
-    rec[idx + 2 * cofs] = make_double2(ga, 0.0);
+    rec[idx + 2 * cofs] = make_double2(ga, (al + be) + ga);  // sigma: the FP64 CW84 march's mean coefficient
 }
 // FP32 records {u, +-g}: the paired kernel forms the flux terms of both tracers of a pair itself
 // (once per pair, in FP32), which measured faster than loading coefficient records
