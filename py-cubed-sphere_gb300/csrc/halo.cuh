@@ -8,12 +8,10 @@
 
 namespace csadv {
 
-// the true state Q* + g corr of a cell with a pending MF-PR correction, rounded as the
-// reference rounds Q - dt (div - g m0/a2) split into its two parts
-__device__ __forceinline__ float corrected(float v, float g, float corr) { return __fadd_rn(v, __fmul_rn(g, corr)); }
-__device__ __forceinline__ double corrected(double v, double g, double corr) {
-    return __dadd_rn(v, __dmul_rn(g, corr));
-}
+// the true state Q* + g corr of a cell with a pending MF-PR correction, one fused rounding (the
+// same function everywhere the correction is applied: on load, in the ghost cells, on read-out)
+__device__ __forceinline__ float corrected(float v, float g, float corr) { return __fmaf_rn(g, corr, v); }
+__device__ __forceinline__ double corrected(double v, double g, double corr) { return __fma_rn(g, corr, v); }
 
 // Source values of the ghost-cell interpolation.  With a pending MF-PR correction
 // (fused engine) the stored interior value is Q* and the true value is Q* + g corr,

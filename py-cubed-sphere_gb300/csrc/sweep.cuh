@@ -380,7 +380,8 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
     V cC = ln.c[(ma - 1) * P], cN = cC;                          // cell m
     real nw4 = real(0);
     real pL = real(0), pR = real(0), pQ = real(0);  // previous cell's parabola
-    real Fp = real(0), cp = real(0), gcp = real(0), igp = real(0), acc = real(0), accm = real(0);
+    real Fp = real(0), cp = real(0), gcp = real(0), igp = real(0), accm = real(0);
+    real Fa = real(0);  // the flux through edge ma (the MF-PR sum telescopes to F(mb) - F(ma))
 #pragma unroll SWEEP_UNROLL
     for (int m = ma - 1; m <= mb; ++m) {
         if (m < mb) {
@@ -425,9 +426,9 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
                     const real sdiv = (F - Fp) + dY[k * os];
                     const real qn = fma(-sdiv, HDT ? ig : dtdx * ig, Qc[k * qs]);
                     qout[(long long)k * P] = qn;
-                    if (mfpr) acc += sdiv;  // sum(div g) = sum(sdiv) / dx: div = sdiv / (dx g)
                 }
             }
+            if (m == ma) Fa = F;
             Fp = F;
             cp = cm;
         }
@@ -446,7 +447,11 @@ __device__ __forceinline__ LineSums<real> march(const Line<real> &ln, int P, int
         w[3] = w[4];
         w[4] = nw4;
     }
-    return LineSums<real>{acc * irdx, accm};
+    // MF-PR: sum(div g) = sum(sdiv) / dx (div = sdiv / (dx g)), and over a segment the x part of
+    // sdiv = (F(k+1) - F(k)) + dY(k) sums to F(mb) - F(ma); the y-flux differences dY are summed the
+    // same way by the P2 lines that form them (MARCH_DIFF), so no per-cell addition is needed
+    const real tele = mfpr && MODE != MARCH_SPLIT ? Fp - Fa : real(0);
+    return LineSums<real>{tele * irdx, accm};
 }
 
 // CTAs per SM the register allocation is sized for: two, so that the FP64 pipe (on GB300 its
@@ -542,6 +547,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
                 }
             }
             __syncthreads();
+            real acc = real(0);  // MF-PR: this thread's share of the tile's sum(div g) (P2 and P3 lines)
             // P2: y-lines of Qx over rows [0, ni): y-flux differences -> sDy
             {
                 const int LY = ni;  // jobs packed densely
@@ -552,13 +558,12 @@ __global__ void __launch_bounds__(SWEEP_THREADS, SweepMinBlocks<real>::value) k_
                     if (r >= ni || ma >= mb) continue;
                     const long long g0 = (long long)J0 * P + I0 + r;
                     Line<real> ln{sQx + r * L.QJp + 3, 1, ery + g0, cry + g0, efy + g0, S.ecofs};
-                    march<real, REC, MARCH_DIFF>(ln, P, ma, mb, dtdx, irdx, mt, split, false, sDy + r * L.TJp, 1,
-                                                 nullptr, nullptr, 0, nullptr);
+                    acc += march<real, REC, MARCH_DIFF>(ln, P, ma, mb, dtdx, irdx, mt, split, mfpr, sDy + r * L.TJp,
+                                                        1, nullptr, nullptr, 0, nullptr).div;
                 }
             }
             __syncthreads();
             // P3: x-lines of Qy over columns [0, nj): x fluxes, div, update, MF-PR partials
-            real acc = real(0);
             {
                 const int LX = nj;  // jobs packed densely
                 const int jx = S.s2x * LX;
