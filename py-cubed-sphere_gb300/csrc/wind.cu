@@ -64,7 +64,6 @@ struct UpwindMetric {
     const typename Vec2<W>::type *gc;     // cell records {g, 1/g} in the same orientation
     int n;                                // rows of the orientation: edges 0..n, cells 0..n-1
     int pl07;                             // MT-PL07: every weight is the edge's metric
-    int sigma;                            // CW84: the march needs alpha, beta and sigma = alpha + beta + gamma only
 };
 
 // the upwind choice of an edge: wind >= 0 (flux.py:48-61), for FP64 on the integer pipe with 32-bit
@@ -77,7 +76,7 @@ __device__ __forceinline__ bool wind_up(double u) {
 
 template <class W>
 __device__ __forceinline__ void flux_coefs(W u, W g, bool up, W dtdx, const UpwindMetric<W> &um, const Dims &d, int m,
-                                           int col, W &al, W &be, W &ga, W &sg) {
+                                           int col, W &al, W &be, W &ga) {
     W gL = g, gR = g, gC = g;
     if (!um.pl07) {  // the upwind cell: m - 1 (wind >= 0) or m, clamped to the plane
         const int cm = up ? (m > 0 ? m - 1 : 0) : (m < um.n ? m : um.n - 1);
@@ -96,29 +95,21 @@ __device__ __forceinline__ void flux_coefs(W u, W g, bool up, W dtdx, const Upwi
     const W P = us * s, R = uc * s;
     al = gR * (up ? P : R);
     be = gL * (up ? neg_bits(R) : P);
-    const W t = fma(W(2), R, uc);
-    if (um.sigma) {  // sigma = alpha + beta +- gC t in one fused step (gamma itself is not needed)
-        sg = fma(up ? gC : neg_bits(gC), t, al + be);
-        ga = sg;
-    } else {
-        const W G = gC * t;
-        ga = up ? G : neg_bits(G);
-        sg = (al + be) + ga;
-    }
+    const W G = gC * fma(W(2), R, uc);
+    ga = up ? G : neg_bits(G);
 }
 
 // FP64 records: {u, +-g} (the sign carries the upwind choice) at rec[idx], the coefficients
-// {alpha, beta} at rec[idx + cofs] and {gamma, sigma = alpha + beta + gamma} at rec[idx + 2 cofs]
-// (for CW84, which reads sigma only, both words hold sigma); `coefs` false: zero coefficients (an
-// edge no flux goes through)
+// {alpha, beta} at rec[idx + cofs] and {gamma, alpha + beta + gamma} at rec[idx + 2 cofs]; `coefs` false: zero
+// coefficients (an edge no flux goes through)
 __device__ __forceinline__ void put_record(double2 *rec, long long idx, long long cofs, double wind, double g, bool up,
                                            double dtdx, const UpwindMetric<double> &um, const Dims &d, int m, int col,
                                            bool coefs = true) {
     rec[idx] = edge_record<double2>(wind, g, up);
-    double al = 0.0, be = 0.0, ga = 0.0, sg = 0.0;
-    if (coefs) flux_coefs(wind, g, up, dtdx, um, d, m, col, al, be, ga, sg);
+    double al = 0.0, be = 0.0, ga = 0.0;
+    if (coefs) flux_coefs(wind, g, up, dtdx, um, d, m, col, al, be, ga);
     rec[idx + cofs] = make_double2(al, be);
-    rec[idx + 2 * cofs] = make_double2(ga, sg);
+    rec[idx + 2 * cofs] = make_double2(ga, (al + be) + ga);  // sigma: the FP64 CW84 march's mean coefficient
 }
 // FP32 records {u, +-g}: the paired kernel forms the flux terms of both tracers of a pair itself
 // (once per pair, in FP32), which measured faster than loading coefficient records
@@ -1068,9 +1059,8 @@ template <class W>
 static void upwind_metrics(const Options &o, const Dims &d, const void *gpu, const void *gpvT, const void *crx,
                            const void *cry, UpwindMetric<W> &mx, UpwindMetric<W> &my) {
     using V = typename Vec2<W>::type;
-    const int sig = o.recon == REC_CW84 ? 1 : 0;
-    mx = UpwindMetric<W>{(const W *)gpu, (const V *)crx, d.n, o.mt == MT_PL07 ? 1 : 0, sig};
-    my = UpwindMetric<W>{(const W *)gpvT, (const V *)cry, d.n, o.mt == MT_PL07 ? 1 : 0, sig};
+    mx = UpwindMetric<W>{(const W *)gpu, (const V *)crx, d.n, o.mt == MT_PL07 ? 1 : 0};
+    my = UpwindMetric<W>{(const W *)gpvT, (const V *)cry, d.n, o.mt == MT_PL07 ? 1 : 0};
 }
 
 template <class real, class V>
