@@ -268,7 +268,8 @@ struct Marcher {
     Recon<REC, V> rc;
     float2 eA, eB, cC, cP;  // edges m, m+1; cells m, m-1
     float2 eC, cD;          // edge m+2, cell m+1 (deeper lookahead)
-    V pL, pR, pQ, Fp;       // previous cell's (metric-weighted) parabola and mean; flux through edge m-1
+    V pU, pV, pQ, Fp;       // previous cell's (metric-weighted) parabola as offsets from its mean, the mean;
+                            // flux through edge m-1
     float cmp;              // g u dt/dx at edge m-1 (SP-L04, SP-PL07)
     V *out;
     const V *dy, *qc;
@@ -318,27 +319,28 @@ struct Marcher {
         } else {
             cQ = vadd(w[2], w[2]);
         }
+        // the weighted parabola as offsets from its weighted mean: cu = R - q, cv = q - L
+        const V cu = vsub(cR, cQ), cv = vsub(cQ, cL);
         if (FLUX) {
             // upwind PPM flux through edge m (flux.py:20-128): the parabola of cell m-1 when the
-            // wind is >= 0, of cell m otherwise; F = e + c/2 (q6 -+ dq) - q6 c^2 / 3 in doubled
+            // wind is >= 0, of cell m otherwise.  The reference's e + c/2 (q6 -+ dq) - q6 c^2/3 with
+            // dq = u + v and q6 = 3 (v - u) in the upwind cell's offsets is q + A u + B v with
+            // A = (1 - c)^2, B = c (1 - c) (wind >= 0) or A = c (1 + c), B = -(1 + c)^2; doubled
             // units, times u / 2
             const float u = eA.x;
             const bool up = !signbit(eA.y);
             const float c = __fmul_rn(u, dtdx);
-            const float hc = __fmul_rn(0.5f, c);
-            const float hs = up ? hc : -hc;
-            const float c3 = __fmul_rn(__fmul_rn(c, c), 1.0f / 3.0f);
-            V e, e2, eQ;
+            const float sc = up ? __fsub_rn(1.f, c) : __fadd_rn(1.f, c);
+            const float ss = __fmul_rn(sc, sc), cs = __fmul_rn(c, sc);
+            const float A = up ? ss : cs, B = up ? cs : -ss;
+            V eu, ev, eQ;
 #pragma unroll
             for (int l = 0; l < Lanes<V>::n; ++l) {
-                set_lane(e, l, up ? lane(pR, l) : lane(cL, l));
-                set_lane(e2, l, up ? lane(pL, l) : lane(cR, l));
+                set_lane(eu, l, up ? lane(pU, l) : lane(cu, l));
+                set_lane(ev, l, up ? lane(pV, l) : lane(cv, l));
                 set_lane(eQ, l, up ? lane(pQ, l) : lane(cQ, l));
             }
-            const V sdq = vsub(e, e2);
-            const V q6 = vmul(vsub(vadd(eQ, eQ), vadd(e, e2)), bc<V>(3.f));
-            const V t1 = vmul(vsub(q6, sdq), bc<V>(hs));
-            V F = vfma(q6, bc<V>(-c3), vadd(e, t1));
+            V F = vfma(ev, bc<V>(B), vfma(eu, bc<V>(A), eQ));
             F = vmul(F, bc<V>(MT0 ? __fmul_rn(0.5f, u) : __fmul_rn(__fmul_rn(0.5f, u), gl)));
             const float cm = __fmul_rn(gl, c);
             if (OUT) {
@@ -379,8 +381,8 @@ struct Marcher {
             Fp = F;
             cmp = cm;
         }
-        pL = cL;
-        pR = cR;
+        pU = cu;
+        pV = cv;
         pQ = cQ;
         cP = cC;
         eA = eB;
