@@ -122,31 +122,23 @@ __device__ __forceinline__ V times4(V x) {
     const V t = vadd(x, x);
     return vadd(t, t);
 }
-// twice the value at the edge between cells a and b from their means and doubled slopes:
-// (qa + qb) - (Sb - Sa) / 6
+// CW84 monotonicity limiter (reconstruction_1d.py:102-153) on the doubled offsets U = 2 (R - q),
+// Vv = 2 (q - L) of a cell's parabola: the reference's extremum test (R - q)(q - L) <= 0 flattens
+// the cell (both offsets 0); otherwise (U, Vv of one sign; dq = u + v and q6 = 3 (v - u)) its
+// overshoot tests |dq| < |q6| and dq (q - (R + L)/2) >< +-dq^2/6 hold exactly when |v| > 2|u|
+// (L moves to 3q - 2R: v becomes 2u) or |u| > 2|v| (R moves to 3q - 2L: u becomes 2v).  At the
+// ties a rounding could decide, both branches give the same parabola.
 template <class V>
-__device__ __forceinline__ V cw84_edge2(V qa, V qb, V Sa, V Sb) {
-    return vfma(vsub(Sb, Sa), bc<V>(-1.0f / 6.0f), vadd(qa, qb));
-}
-// CW84 monotonicity limiter (reconstruction_1d.py:102-153) on the doubled parabola (L2, R2) of
-// the cell with doubled mean Q2, in the offsets u = R - q, v = q - L: the reference's extremum
-// test (R - q)(q - L) <= 0 flattens the cell; otherwise (u, v of one sign; dq = u + v and
-// q6 = 3 (v - u)) its overshoot tests |dq| < |q6| and dq (q - (R + L)/2) >< +-dq^2/6 hold exactly
-// when |v| > 2|u| (L moves to 3q - 2R = q - 2u) or |u| > 2|v| (R moves to 3q - 2L = q + 2v).  At
-// the ties a rounding could decide, both branches give the same parabola.
-template <class V>
-__device__ __forceinline__ void cw84_limit2(V Q2, V &L2, V &R2) {
-    const V u = vsub(R2, Q2), v = vsub(Q2, L2);
-    const V u2 = vadd(u, u), v2 = vadd(v, v);
-    const V pf = vmul(u, v);
-    const V Ln = vsub(Q2, u2), Rn = vadd(Q2, v2);
+__device__ __forceinline__ void cw84_limit_ofs2(V U, V Vv, V &uo, V &vo) {
+    const V U2 = vadd(U, U), V2 = vadd(Vv, Vv);
+    const V pf = vmul(U, Vv);
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
         const bool flat = lane(pf, l) <= 0.f;
-        const bool ml = !flat && fabsf(lane(v, l)) > fabsf(lane(u2, l));
-        const bool mr = !flat && fabsf(lane(u, l)) > fabsf(lane(v2, l));
-        set_lane(L2, l, flat ? lane(Q2, l) : (ml ? lane(Ln, l) : lane(L2, l)));
-        set_lane(R2, l, flat ? lane(Q2, l) : (mr ? lane(Rn, l) : lane(R2, l)));
+        const bool ml = !flat && fabsf(lane(Vv, l)) > fabsf(lane(U2, l));
+        const bool mr = !flat && fabsf(lane(U, l)) > fabsf(lane(V2, l));
+        set_lane(uo, l, flat ? 0.f : (mr ? lane(V2, l) : lane(U, l)));
+        set_lane(vo, l, flat ? 0.f : (ml ? lane(U2, l) : lane(Vv, l)));
     }
 }
 // twice the L04 monotone slope of the cell q0 between qm and qp (reconstruction_1d.py:155-172)
@@ -191,7 +183,9 @@ __device__ __forceinline__ V ppm0_edge2(V qam, V qa, V qb, V qbp) {
 // the window w = q(m-2..m+2) gives the doubled parabola (L2, R2) of cell m and advances.
 template <int REC, class V>
 struct Recon {
-    V s, E, dp, D1;  // doubled slope of the current cell, doubled left edge value; q(m+1) - q(m), 4 times it
+    // doubled slope of the current cell; doubled left edge value (CW84: the doubled offset
+    // 2 (q - L) of the current cell instead); q(m+1) - q(m), 4 times it
+    V s, E, dp, D1;
     __device__ __forceinline__ void init(const V w[5]) {
         if (REC == REC_CW84) {
             const V dpa = vsub(w[2], w[1]), dma = vsub(w[1], w[0]);
@@ -200,7 +194,7 @@ struct Recon {
             dp = vsub(w[3], w[2]);
             D1 = times4(dp);
             s = cw84_slope2(w[1], w[3], dp, D1, dpa, D1a);
-            E = cw84_edge2(w[1], w[2], sa, s);
+            E = vfma(vsub(s, sa), bc<V>(1.0f / 6.0f), dpa);  // 2 (q(m) - E(m - 1/2))
         } else if (REC == REC_L04) {
             const V sa = l04_mono2(w[0], w[1], w[2]);
             s = l04_mono2(w[1], w[2], w[3]);
@@ -209,17 +203,19 @@ struct Recon {
             E = ppm0_edge2(w[0], w[1], w[2], w[3]);
         }
     }
+    // the cell's doubled parabola (L, R); CW84: its doubled limited offsets (L <- 2 (q - L'),
+    // R <- 2 (R' - q)).  With d = q(m+1) - q(m) and dS the doubled slopes' difference, the doubled
+    // edge value between the cells gives 2 (E - q(m)) = d - dS/6 and 2 (q(m+1) - E) = d + dS/6.
     __device__ __forceinline__ void cell(const V w[5], V &L, V &R) {
         if (REC == REC_CW84) {
             const V dpn = vsub(w[4], w[3]);
             const V D1n = times4(dpn);
             const V sn = cw84_slope2(w[2], w[4], dpn, D1n, dp, D1);
-            const V En = cw84_edge2(w[2], w[3], s, sn);
-            L = E;
-            R = En;
-            cw84_limit2(vadd(w[2], w[2]), L, R);
+            const V dS = vsub(sn, s);
+            const V U = vfma(dS, bc<V>(-1.0f / 6.0f), dp), Vn = vfma(dS, bc<V>(1.0f / 6.0f), dp);
+            cw84_limit_ofs2(U, E, R, L);
             s = sn;
-            E = En;
+            E = Vn;
             dp = dpn;
             D1 = D1n;
         } else if (REC == REC_L04) {
@@ -308,19 +304,36 @@ struct Marcher {
         const float2 cN = __ldg(cf);
         cf += P;
 
-        V L, R;  // doubled
+        V L, R;  // doubled (CW84: the doubled offsets, L <- 2 (q - L), R <- 2 (R - q))
         rc.cell(w, L, R);
-        V cL = L, cR = R, cQ;
         const float gl = fabsf(eA.y);
-        if (MT0) {  // flux.py:28-31
-            cL = vmul(L, bc<V>(gl));
-            cR = vmul(R, bc<V>(fabsf(eB.y)));
-            cQ = vmul(w[2], bc<V>(__fadd_rn(cC.x, cC.x)));
+        // the (MT-0: metric-weighted, flux.py:28-31) parabola as offsets from its weighted mean:
+        // cu = R - q, cv = q - L, doubled; cQ the weighted doubled mean
+        V cu, cv, cQ;
+        if (REC == REC_CW84) {
+            const V Q2 = vadd(w[2], w[2]);
+            if (MT0) {  // gR (q + u) - g q = gR u + (gR - g) q, g q - gL (q - v) = gL v + (g - gL) q
+                const float gr = fabsf(eB.y), g = cC.x;
+                cQ = vmul(Q2, bc<V>(g));
+                cu = vfma(R, bc<V>(gr), vmul(Q2, bc<V>(__fsub_rn(gr, g))));
+                cv = vfma(L, bc<V>(gl), vmul(Q2, bc<V>(__fsub_rn(g, gl))));
+            } else {
+                cQ = Q2;
+                cu = R;
+                cv = L;
+            }
         } else {
-            cQ = vadd(w[2], w[2]);
+            V cL = L, cR = R;
+            if (MT0) {
+                cL = vmul(L, bc<V>(gl));
+                cR = vmul(R, bc<V>(fabsf(eB.y)));
+                cQ = vmul(w[2], bc<V>(__fadd_rn(cC.x, cC.x)));
+            } else {
+                cQ = vadd(w[2], w[2]);
+            }
+            cu = vsub(cR, cQ);
+            cv = vsub(cQ, cL);
         }
-        // the weighted parabola as offsets from its weighted mean: cu = R - q, cv = q - L
-        const V cu = vsub(cR, cQ), cv = vsub(cQ, cL);
         if (FLUX) {
             // upwind PPM flux through edge m (flux.py:20-128): the parabola of cell m-1 when the
             // wind is >= 0, of cell m otherwise.  The reference's e + c/2 (q6 -+ dq) - q6 c^2/3 with
