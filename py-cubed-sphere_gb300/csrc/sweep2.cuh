@@ -79,6 +79,13 @@ __device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) {
     return d;
 }
 
+// min(a, b, c) of three non-NaN floats, one three-input instruction (sm_100 and later)
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 template <class V> struct Lanes;
 template <> struct Lanes<float> { static constexpr int n = 1; };
 template <> struct Lanes<float2> { static constexpr int n = 2; };
@@ -112,7 +119,7 @@ __device__ __forceinline__ V cw84_slope2(V qm, V qp, V dp, V D1, V dm, V D2) {
     V s;
 #pragma unroll
     for (int l = 0; l < Lanes<V>::n; ++l) {
-        const float m = fminf(fminf(fabsf(lane(D0, l)), fabsf(lane(D1, l))), fabsf(lane(D2, l)));
+        const float m = fmin3(fabsf(lane(D0, l)), fabsf(lane(D1, l)), fabsf(lane(D2, l)));
         set_lane(s, l, lane(pr, l) > 0.f ? copysignf(m, lane(D0, l)) : 0.f);
     }
     return s;
