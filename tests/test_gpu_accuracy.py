@@ -74,6 +74,7 @@ def test_one_revolution_N48_fp64_and_fp32():
           "FP64 vs oracle %.2e, FP32 vs oracle %.2e; mass change FP64 %.2e FP32 %.2e"
           % (nsteps, dt, e64, eo, e32, rel(q64, s.Q[it]), rel(q32, s.Q[it]), dm64, dm32))
     assert rel(q64, s.Q[it]) <= 1e-12
+    assert rel(q32, s.Q[it]) < 1e-4  # the FP32 form against the oracle directly
     np.testing.assert_allclose(e64, eo, rtol=1e-9)
     assert dm64 < 1e-13
     assert abs(e32[2] - e64[2]) <= 0.01 * e64[2]
