@@ -345,9 +345,12 @@ struct LineSums {
 };
 
 #ifndef CSADV_SWEEP_UNROLL
-#define CSADV_SWEEP_UNROLL 2
+#define CSADV_SWEEP_UNROLL 1
 #endif
-constexpr int SWEEP_UNROLL = CSADV_SWEEP_UNROLL;  // march loop unrolling (2: measured best, FP32 and FP64)
+// march loop unrolling: 1, measured best for the FP64 form since the march works in edge offsets
+// (0.297 ms per N=384 two-tracer step against 0.303 ms unrolled 2x and 0.304 ms 3x: fewer spilled
+// values; the FP64 pipe is the bound either way)
+constexpr int SWEEP_UNROLL = CSADV_SWEEP_UNROLL;
 
 // March over cells [ma - 1, mb]: fluxes through edges [ma, mb], outputs for cells [ma, mb).
 //   MARCH_SPLIT : split field of the first pass -> out[k * os]
