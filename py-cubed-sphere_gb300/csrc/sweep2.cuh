@@ -353,14 +353,12 @@ struct Marcher {
             const float sc = up ? __fsub_rn(1.f, c) : __fadd_rn(1.f, c);
             const float ss = __fmul_rn(sc, sc), cs = __fmul_rn(c, sc);
             const float A = up ? ss : cs, B = up ? cs : -ss;
-            V eu, ev, eQ;
+            // both cells' candidates in packed arithmetic, then one selection per lane
+            const V Fu = vfma(pV, bc<V>(B), vfma(pU, bc<V>(A), pQ));
+            const V Fd = vfma(cv, bc<V>(B), vfma(cu, bc<V>(A), cQ));
+            V F;
 #pragma unroll
-            for (int l = 0; l < Lanes<V>::n; ++l) {
-                set_lane(eu, l, up ? lane(pU, l) : lane(cu, l));
-                set_lane(ev, l, up ? lane(pV, l) : lane(cv, l));
-                set_lane(eQ, l, up ? lane(pQ, l) : lane(cQ, l));
-            }
-            V F = vfma(ev, bc<V>(B), vfma(eu, bc<V>(A), eQ));
+            for (int l = 0; l < Lanes<V>::n; ++l) set_lane(F, l, up ? lane(Fu, l) : lane(Fd, l));
             F = vmul(F, bc<V>(MT0 ? __fmul_rn(0.5f, u) : __fmul_rn(__fmul_rn(0.5f, u), gl)));
             const float cm = __fmul_rn(gl, c);
             if (OUT) {
