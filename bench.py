@@ -18,10 +18,11 @@ Timed steps run as CUDA graphs; L2 is flushed (256 MB write) before every timed 
 step is timed alone with CUDA events on the launching stream.  N > 1 (torchrun): every rank
 runs an independent replica (the solve does not shard; "replicas only"), max time over ranks.
 
-Further sub-objects: `accuracy` (one revolution at N = 48 and the deformational flow at
-N = 384 to t = T, FP64 and FP32, error norms against the exact solution), `batched` (256
-solves, 200 steps), `large` (N = 1536, 8 tracers, 500 steps), `serving` (the Poisson request
-stream) and `cpu_baseline` (the oracle on one host core).
+Further sub-objects, in the one-GPU job only: `accuracy` (one revolution at N = 48 and the
+deformational flow at N = 384 to t = T, FP64 and FP32, error norms against the exact solution),
+`batched` (256 solves, 200 steps), `large` (N = 1536, 8 tracers, 500 steps), `serving` (the
+Poisson request stream, 10^4 requests: several minutes) and `cpu_baseline` (the oracle on one
+host core).
 
 --impl reference times the reference algorithm on the host cores: the CPU oracle (a numpy
 restatement of the reference, test infrastructure) advancing one independent replica of the
@@ -714,14 +715,17 @@ def bench_gpu(args):
                          "h2d_bytes_per_step": h2d32, "d2h_bytes_per_step": d2h32},
                  "roofline": roof32, "issue_roofline": issue32},
     }
-    if not args.no_accuracy:
+    # the single-GPU legs (accuracy runs, batch, N=1536, serving) run in the one-GPU job only: under
+    # torchrun the other ranks have finished, and their GPUs would wait for rank 0
+    single = world == 1
+    if single and not args.no_accuracy:
         line["accuracy"] = run_accuracy(stream)
-    if not args.no_batched:
+    if single and not args.no_batched:
         line["batched"] = run_batched(torch, args.warmup, stream, hbm)
         line["batched"]["vs_fp64_single"] = round(line["batched"]["value"] / v64, 2)
-    if not args.no_large:
+    if single and not args.no_large:
         line["large"] = run_large(torch, args.warmup, stream, hbm, args.large_steps)
-    if args.serve_requests > 0:
+    if single and args.serve_requests > 0:
         line["serving"] = run_serving(torch, args.serve_requests, stream)
     if world == 1 and not args.no_cpu:
         k = 2
