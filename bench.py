@@ -49,6 +49,8 @@ WIND = 102           # deformational (Nair-Lauritzen 2010 case 4)
 WIND_PARAM = (0.48, 5.0, 0.0, 0.0)   # k = 2.4 R / T with R = 1, T = 5
 ICS = (102, 103)     # cosine bells; smooth bells
 CFL = 0.5
+E2E_CALL = ("csadv_advance_host per step (page-locked host arrays: upload both tracers, step, read both out; "
+            "separate_calls: csadv_set_tracer x2, csadv_advance, csadv_get_tracer x2)")
 METRIC = "tracer cell-steps/s"
 
 
@@ -232,9 +234,11 @@ def run_form(torch, precision, steps, warmup, flush, stream, world=1):
     return res
 
 
-def run_e2e(torch, precision, steps, stream, world=1):
+def run_e2e(torch, precision, steps, stream, world=1, one_call=True):
     """Through the C ABI with host buffers: per step, upload both tracers from pinned host
-    memory (reference layout, full arrays), advance, download both tracers."""
+    memory (reference layout, full arrays), advance, download both tracers.  one_call: the
+    drop-in call for a host-resident state, csadv_advance_host (the copies on the copy engines
+    beside per-tracer step kernels); else csadv_set_tracer, csadv_advance and csadv_get_tracer."""
     import ctypes
     import numpy as np
     from csadv import Plan, _lib
@@ -260,7 +264,13 @@ def run_e2e(torch, precision, steps, stream, world=1):
     L = _lib.lib()
     sh = pl.stream
 
+    ins = (ctypes.c_void_p * NTRACERS)(*[b[0].value for b in bufs])
+    outs = (ctypes.c_void_p * NTRACERS)(*[b[1].value for b in bufs])
+
     def one_step():
+        if one_call:
+            _lib.check(L.csadv_advance_host(pl._h, 1, ins, _lib.LAYOUT_FULL, outs, _lib.LAYOUT_INTERIOR, sh))
+            return
         for t in range(NTRACERS):
             _lib.check(L.csadv_set_tracer(pl._h, t, bufs[t][0], _lib.LAYOUT_FULL, sh))
         _lib.check(L.csadv_advance(pl._h, 1, sh))
@@ -680,10 +690,13 @@ def bench_gpu(args):
         f32 = run_form(torch, 32, args.steps, args.warmup, flush, stream, world)
     e64_sec, h2d64, d2h64 = run_e2e(torch, 64, max(3, args.steps // 2), stream, world)
     e32_sec, h2d32, d2h32 = run_e2e(torch, 32, max(3, args.steps // 2), stream, world)
+    s64_sec = run_e2e(torch, 64, max(3, args.steps // 2), stream, world, one_call=False)[0]
+    s32_sec = run_e2e(torch, 32, max(3, args.steps // 2), stream, world, one_call=False)[0]
     rate = ctypes.c_double()
     _lib.check(_lib.lib().csadv_fp64_rate(512, ctypes.byref(rate), _lib.stream_handle(stream)), "csadv_fp64_rate")
 
-    ms64, ms32, e64_sec, e32_sec = max_over_ranks([f64["ms_per_step"], f32["ms_per_step"], e64_sec, e32_sec], world)
+    ms64, ms32, e64_sec, e32_sec, s64_sec, s32_sec = max_over_ranks(
+        [f64["ms_per_step"], f32["ms_per_step"], e64_sec, e32_sec, s64_sec, s32_sec], world)
     cells = NTRACERS * 6 * N_CELLS * N_CELLS
     if rank != 0:
         return
@@ -702,7 +715,8 @@ def bench_gpu(args):
         "timing": {"l2": "flushed (256 MB write) before every timed step", "execution": "CUDA graph per step",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": round(job_rate(cells, world, e64_sec * 1e3), 1), "unit": "tracer cell-steps/s",
-                "h2d_bytes_per_step": h2d64, "d2h_bytes_per_step": d2h64},
+                "h2d_bytes_per_step": h2d64, "d2h_bytes_per_step": d2h64, "call": E2E_CALL,
+                "separate_calls": round(job_rate(cells, world, s64_sec * 1e3), 1)},
         "gpu_launches": int(f64["stats"]["kernel_launches"]),
         "kernels_per_step": int(f64["stats"]["kernels_per_step"]),
         "roofline": roof64,
@@ -712,7 +726,8 @@ def bench_gpu(args):
                  "gpu_launches": int(f32["stats"]["kernel_launches"]),
                  "kernels_per_step": int(f32["stats"]["kernels_per_step"]),
                  "e2e": {"value": round(job_rate(cells, world, e32_sec * 1e3), 1), "unit": "tracer cell-steps/s",
-                         "h2d_bytes_per_step": h2d32, "d2h_bytes_per_step": d2h32},
+                         "h2d_bytes_per_step": h2d32, "d2h_bytes_per_step": d2h32, "call": E2E_CALL,
+                         "separate_calls": round(job_rate(cells, world, s32_sec * 1e3), 1)},
                  "roofline": roof32, "issue_roofline": issue32},
     }
     # the single-GPU legs (accuracy runs, batch, N=1536, serving) run in the one-GPU job only: under

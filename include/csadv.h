@@ -131,6 +131,19 @@ int csadv_update_winds(csadv_plan *plan, double t, void *stream);
 /* nsteps iterations of the time loop of adv_sphere (advection_sphere.py:45-57):
  * time step k then update_adv(k*dt), k = current_step+1 ... current_step+nsteps. */
 int csadv_advance(csadv_plan *plan, int nsteps, void *stream);
+/* The same time loop on a state held in host memory, as the reference keeps it (the numpy
+ * arrays that adv_sphere's loop updates, advection_sphere.py:45-57): every tracer t is read from
+ * in[t] (layout in_layout, as csadv_set_tracer), nsteps iterations run as csadv_advance runs them,
+ * and every tracer is written to out[t] (out_layout, as csadv_get_tracer).  Returns when out[]
+ * holds the fields; in or out may be NULL (no upload, no read-out), and in[t] may equal out[t].
+ * With the line-marching fused engine the copies run on the copy engines beside the steps: the
+ * step kernel is launched once per tracer in the first and the last step, tracer t+1's upload
+ * overlaps tracer t's first step and tracer t's read-out overlaps tracer t+1's last step.  The
+ * results equal those of csadv_set_tracer, csadv_advance and csadv_get_tracer bit for bit.  The
+ * overlap needs page-locked host arrays (csadv_host_alloc, cudaHostRegister); with pageable ones
+ * the copies wait for each other.  Other engines run those three calls in turn. */
+int csadv_advance_host(csadv_plan *plan, int nsteps, const double *const *in, int in_layout,
+                       double *const *out, int out_layout, void *stream);
 
 /* mass_computation (diagnostics.py:14-26): sum over the interior of Q*sqrt(g)*dx*dy, FP64. */
 int csadv_mass(csadv_plan *plan, int tracer, double *mass, void *stream);

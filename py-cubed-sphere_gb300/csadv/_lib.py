@@ -72,6 +72,7 @@ _SIGS = {
     "csadv_time_step": ([_vp, _c_int, _vp], _c_int),
     "csadv_update_winds": ([_vp, _c_double, _vp], _c_int),
     "csadv_advance": ([_vp, _c_int, _vp], _c_int),
+    "csadv_advance_host": ([_vp, _c_int, _vp, _c_int, _vp, _c_int, _vp], _c_int),
     "csadv_mass": ([_vp, _c_int, _dp, _vp], _c_int),
     "csadv_errors": ([_vp, _c_int, _c_int, _dp, _c_double, _dp, _vp], _c_int),
     "csadv_get_cfl": ([_vp, _dp], _c_int),

@@ -1,9 +1,25 @@
 """Object wrapper over one csadv plan (one solve: grid + winds + tracers on the GPU)."""
 import ctypes
+import weakref
 
 import numpy as np
 
 from . import _lib as L
+
+
+def host_array(shape):
+    """A zeroed FP64 numpy array in page-locked host memory (csadv_host_alloc), freed when the
+    last array that uses it is collected.  The tracer copies read and write such arrays in place
+    (Plan.set_tracer, get_tracer, advance_host), and advance_host overlaps their copies with the
+    steps."""
+    count = max(int(np.prod(shape)), 1)
+    ptr = ctypes.c_void_p()
+    L.check(L.lib().csadv_host_alloc(ctypes.byref(ptr), count * 8), "csadv_host_alloc")
+    cbuf = (ctypes.c_double * count).from_address(ptr.value)
+    weakref.finalize(cbuf, L.lib().csadv_host_free, ptr.value)
+    arr = np.ctypeslib.as_array(cbuf)[:int(np.prod(shape))].reshape(shape)
+    arr[...] = 0.0
+    return arr
 
 
 class Plan:
@@ -105,6 +121,43 @@ class Plan:
 
     def advance(self, nsteps):
         L.check(L.lib().csadv_advance(self._h, int(nsteps), self.stream), "csadv_advance")
+
+    def advance_host(self, nsteps, Q_in=None, Q_out=None, full_out=False):
+        """csadv_advance_host: `nsteps` steps of a state held in host memory.  Q_in: one FP64
+        array per tracer, (N+8, N+8, 6) or (N, N, 6), uploaded first (None: keep the device
+        state); Q_out: one array per tracer to write at the end, or True for new arrays of the
+        full (full_out) or interior shape, or None for no read-out.  Page-locked arrays
+        (host_array) let the copies overlap the steps.  Returns the output arrays (or None)."""
+        T = self.ntracers
+        in_ptrs = out_ptrs = None
+        lin = lout = L.LAYOUT_INTERIOR
+        keep = []
+        if Q_in is not None:
+            if len(Q_in) != T:
+                raise ValueError("Q_in needs one array per tracer")
+            shp = {np.shape(q) for q in Q_in}
+            if len(shp) != 1 or shp.pop() not in ((self.n, self.n, 6), (self.N, self.N, 6)):
+                raise ValueError("every Q_in array must have shape (N+8, N+8, 6) or (N, N, 6)")
+            arrs = [np.ascontiguousarray(q, dtype=np.float64) for q in Q_in]
+            keep += arrs
+            lin = L.LAYOUT_FULL if arrs[0].shape[0] == self.n else L.LAYOUT_INTERIOR
+            in_ptrs = (ctypes.c_void_p * T)(*[a.ctypes.data for a in arrs])
+        if Q_out is True:
+            shp = (self.n, self.n, 6) if full_out else (self.N, self.N, 6)
+            Q_out = [np.empty(shp, dtype=np.float64) for _ in range(T)]
+        if Q_out is not None:
+            if len(Q_out) != T:
+                raise ValueError("Q_out needs one array per tracer")
+            shapes = {q.shape for q in Q_out}
+            ok = all(q.dtype == np.float64 and q.flags.c_contiguous for q in Q_out)
+            if not ok or len(shapes) != 1 or shapes.pop() not in ((self.n, self.n, 6), (self.N, self.N, 6)):
+                raise ValueError("Q_out arrays must be C-contiguous FP64 of shape (N+8, N+8, 6) or (N, N, 6)")
+            lout = L.LAYOUT_FULL if Q_out[0].shape[0] == self.n else L.LAYOUT_INTERIOR
+            out_ptrs = (ctypes.c_void_p * T)(*[q.ctypes.data for q in Q_out])
+        L.check(L.lib().csadv_advance_host(self._h, int(nsteps), in_ptrs, lin, out_ptrs, lout, self.stream),
+                "csadv_advance_host")
+        del keep
+        return Q_out
 
     @property
     def step(self):

@@ -471,6 +471,92 @@ static int tracer_download(csadv_plan *pl, int tracer, double *dst, int layout, 
     return tracer_io<real>(pl->grid, (real *)pl->tracer(tracer), dst, layout, false, st, &x);
 }
 
+// ---------------------------------------------------------------- host-resident state (csadv_advance_host)
+int ensure_host_pipeline(csadv_plan *pl, cudaStream_t st) {
+    if (!pl->up) {
+        CSADV_CUDA(cudaStreamCreateWithFlags(&pl->up, cudaStreamNonBlocking));
+        CSADV_CUDA(cudaStreamCreateWithFlags(&pl->down, cudaStreamNonBlocking));
+        // the first and last steps' kernels at the highest priority: the next step's wind
+        // records (side stream) start at once and fill the wait for the first upload, and the
+        // step kernels take the SMs back as soon as their tracer has arrived
+        int least = 0, greatest = 0;
+        CSADV_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CSADV_CUDA(cudaStreamCreateWithPriority(&pl->hp, cudaStreamNonBlocking, greatest));
+        pl->hev.assign(2 * (size_t)pl->T + 4, nullptr);
+        for (auto &e : pl->hev) CSADV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    if (pl->hstage) return CSADV_OK;
+    pl->mem.set_stream(st);
+    const long long n = pl->grid.d.n;
+    pl->hstage = pl->mem.alloc<double>(2LL * pl->T * NFACE * n * n);
+    return pl->mem.ok() ? CSADV_OK : CSADV_ERR_OOM;
+}
+
+// tracer t of Qbuf[buf] -> dst (layout), with the tracer's pending MF-PR correction applied
+template <class real>
+int stage_tracer_out(csadv_plan *pl, int buf, int t, double *dst, int layout, cudaStream_t st) {
+    FusedState &f = pl->f;
+    IoLazy<real> x;
+    if (pl->opt.mf == MF_PR) {
+        x.g = (const real *)f.g_pc;
+        x.corr = f.corr[buf] + t;
+    }
+    real *Q = (real *)((char *)f.Qbuf[buf] + (size_t)t * pl->grid.d.field * sizeof(real));
+    return tracer_io<real>(pl->grid, Q, dst, layout, false, st, &x);
+}
+
+// One step of the fused engine with the step kernel launched once per tracer.  On `st`, tracer
+// t's kernel follows in(t) and, for t > 0, out(t - 1, cur); out(T - 1, cur) follows the last
+// kernel (cur: the step's input buffer; the results are in 1 - cur).  The side stream ticks the
+// clock and makes the next step's records (pipelined winds) beside the kernels, as in
+// fused_step_work.  With `upload` (in(0) waits for a copy) they run in two launches: the
+// x-edges' records at once, filling the wait for the first tracer's upload, and the y-edges'
+// records behind in(0) (one launch of every record would still hold the SMs when the first
+// kernel is ready, its CTAs living for a whole wave).
+template <class In, class Out>
+int split_step(csadv_plan *pl, cudaStream_t st, bool upload, In in, Out out) {
+    FusedState &f = pl->f;
+    int rc = ensure_side(pl);
+    if (rc) return rc;
+    if (f.wpipe && !f.rec_ready) {  // this step's records first
+        rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, pl->cur, st);
+        if (rc) return rc;
+        f.rec_ready = true;
+    }
+    const int cur = pl->cur, T = pl->T;
+    cudaStream_t sd = pl->side;
+    CSADV_CUDA(cudaEventRecord(pl->sev[0], st));
+    CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[0], 0));
+    rc = do_update_winds(pl, true, 0, 0.0, sd);
+    if (!rc && f.wpipe) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, 1 - cur, sd, upload ? 0 : -1);
+    if (rc) return rc;
+    for (int t = 0; t < T; ++t) {
+        rc = in(t);
+        if (!rc && t == 0) {
+            if (f.wpipe && upload) {
+                CSADV_CUDA(cudaEventRecord(pl->sev[1], st));
+                CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[1], 0));
+                rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, 1 - cur, sd, 1);
+                if (rc) return rc;
+            }
+            CSADV_CUDA(cudaEventRecord(pl->sev[3], sd));
+        }
+        if (!rc && t > 0) rc = out(t - 1, cur);
+        if (!rc) rc = fused_kernel_tracer(pl->opt, T, f, cur, t, st);
+        if (rc) return rc;
+    }
+    rc = out(T - 1, cur);
+    if (rc) return rc;
+    CSADV_CUDA(cudaStreamWaitEvent(st, pl->sev[3], 0));
+    pl->cur = 1 - cur;
+    f.settled = false;
+    const int kernels = T + 1 + (f.wpipe ? (upload ? 2 : 1) : 0);  // step kernels, clock tick, records
+    pl->stats.steps += 1;
+    pl->stats.kernel_launches += kernels;
+    pl->stats.kernels_per_step = kernels;
+    return CSADV_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -680,6 +766,94 @@ int csadv_get_tracer(csadv_plan *pl, int tracer, double *host, int layout, void 
     if (rc) return rc;
     if (!dst)
         CSADV_CUDA(cudaMemcpyAsync(host, pl->stage, (size_t)NFACE * m * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CSADV_CUDA(cudaStreamSynchronize(st));
+    return CSADV_OK;
+}
+
+int csadv_advance_host(csadv_plan *pl, int nsteps, const double *const *in, int in_layout, double *const *out,
+                       int out_layout, void *stream) {
+    if (!pl || nsteps < 0) return CSADV_ERR_ARG;
+    const int T = pl->T;
+    for (int t = 0; t < T; ++t)
+        if ((in && !in[t]) || (out && !out[t])) return CSADV_ERR_ARG;
+    auto bad = [](int l) { return l != CSADV_LAYOUT_FULL && l != CSADV_LAYOUT_INTERIOR; };
+    if ((in && bad(in_layout)) || (out && bad(out_layout))) return CSADV_ERR_ARG;
+    cudaStream_t st = S(stream);
+    FusedState &f = pl->f;
+    const bool overlap = f.on && f.sweep && f.inline_ghosts && !pl->prof && nsteps >= 1 &&
+                         (f.wpipe || !wind_time_dependent(pl->opt));
+    int rc = CSADV_OK;
+    if (!overlap) {  // the same calls one after another
+        for (int t = 0; in && !rc && t < T; ++t) rc = csadv_set_tracer(pl, t, in[t], in_layout, stream);
+        if (!rc) rc = csadv_advance(pl, nsteps, stream);
+        for (int t = 0; out && !rc && t < T; ++t) rc = csadv_get_tracer(pl, t, out[t], out_layout, stream);
+        if (!rc) CSADV_CUDA(cudaStreamSynchronize(st));
+        return rc;
+    }
+    rc = ensure_host_pipeline(pl, st);
+    if (rc) return rc;
+    const Dims d = pl->grid.d;
+    const size_t slot = (size_t)NFACE * d.n * d.n;  // doubles per staging array (full layout)
+    auto cells = [&](int l) { return (size_t)NFACE * (l == CSADV_LAYOUT_FULL ? (size_t)d.n * d.n : (size_t)d.N * d.N); };
+    double *sin = pl->hstage, *sout = pl->hstage + (size_t)T * slot;
+    cudaEvent_t *uploaded = pl->hev.data(), *converted = pl->hev.data() + T;
+    cudaEvent_t fork = pl->hev[2 * T], downloaded = pl->hev[2 * T + 1], to_hp = pl->hev[2 * T + 2],
+                from_hp = pl->hev[2 * T + 3];
+    const bool f64 = pl->opt.precision == 64;
+    // uploads: copy engine, host -> staging, all tracers in order, behind the stream's earlier work
+    CSADV_CUDA(cudaEventRecord(fork, st));
+    if (in) {
+        CSADV_CUDA(cudaStreamWaitEvent(pl->up, fork, 0));
+        for (int t = 0; t < T; ++t) {
+            CSADV_CUDA(cudaMemcpyAsync(sin + t * slot, in[t], cells(in_layout) * sizeof(double), cudaMemcpyHostToDevice,
+                                       pl->up));
+            CSADV_CUDA(cudaEventRecord(uploaded[t], pl->up));
+        }
+    }
+    cudaStream_t hp = pl->hp;
+    auto convert_in = [&](int t) -> int {  // staging -> the tracer's field (layout conversion)
+        if (!in) return CSADV_OK;
+        CSADV_CUDA(cudaStreamWaitEvent(hp, uploaded[t], 0));
+        return f64 ? tracer_upload<double>(pl, t, sin + t * slot, in_layout, hp)
+                   : tracer_upload<float>(pl, t, sin + t * slot, in_layout, hp);
+    };
+    auto convert_out = [&](int t, int cur) -> int {  // the step's result -> staging -> host
+        if (!out) return CSADV_OK;
+        const int nb = 1 - cur;
+        int r = out_layout == CSADV_LAYOUT_FULL ? fused_ghosts_to_current(pl->opt, pl->grid, 1, f, nb, hp, t) : 0;
+        if (!r) r = f64 ? stage_tracer_out<double>(pl, nb, t, sout + t * slot, out_layout, hp)
+                        : stage_tracer_out<float>(pl, nb, t, sout + t * slot, out_layout, hp);
+        if (r) return r;
+        CSADV_CUDA(cudaEventRecord(converted[t], hp));
+        CSADV_CUDA(cudaStreamWaitEvent(pl->down, converted[t], 0));
+        CSADV_CUDA(cudaMemcpyAsync(out[t], sout + t * slot, cells(out_layout) * sizeof(double), cudaMemcpyDeviceToHost,
+                                   pl->down));
+        return CSADV_OK;
+    };
+    auto none_in = [](int) { return CSADV_OK; };
+    auto none_out = [](int, int) { return CSADV_OK; };
+    // the first and the last step on the high-priority stream, forked from and joined to `st`
+    auto on_hp = [&](bool up_step, auto in_fn, auto out_fn) -> int {
+        CSADV_CUDA(cudaEventRecord(to_hp, st));
+        CSADV_CUDA(cudaStreamWaitEvent(pl->hp, to_hp, 0));
+        const int r = split_step(pl, pl->hp, in != nullptr && up_step, in_fn, out_fn);
+        CSADV_CUDA(cudaEventRecord(from_hp, pl->hp));
+        CSADV_CUDA(cudaStreamWaitEvent(st, from_hp, 0));
+        return r;
+    };
+    for (int s = 0; s < nsteps && !rc; ++s) {
+        const bool first = s == 0, last = s == nsteps - 1;
+        if (first && last) rc = on_hp(true, convert_in, convert_out);
+        else if (first) rc = on_hp(true, convert_in, none_out);
+        else if (last) rc = on_hp(false, none_in, convert_out);
+        else rc = run_step(pl, 1, st);
+        if (!rc) pl->k += 1;
+    }
+    if (rc) return rc;
+    if (out) {
+        CSADV_CUDA(cudaEventRecord(downloaded, pl->down));
+        CSADV_CUDA(cudaStreamWaitEvent(st, downloaded, 0));
+    }
     CSADV_CUDA(cudaStreamSynchronize(st));
     return CSADV_OK;
 }

@@ -1,5 +1,7 @@
 // Host side of the fused engine: buffers, wind preparation, step sequencing, and the
 // lazy MF-PR correction.
+#include <vector>
+
 #include "halo.cuh"
 #include "internal.h"
 #include "tiles.h"
@@ -77,22 +79,24 @@ __global__ void k_copy_ghosts(const real *__restrict__ src, real *dst, Dims d) {
     dst[o] = src[o];
 }
 
-int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st) {
+int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st,
+                            int first) {
     const Dims d = g.d;
+    const size_t ofs = (size_t)first * d.field * (o.precision == 64 ? sizeof(double) : sizeof(float));
+    void *src = (char *)f.Qbuf[1 - cur] + ofs, *dst = (char *)f.Qbuf[cur] + ofs;
     if (f.sweep && f.inline_ghosts) {  // the step kernel kept its ghost cells on chip: fill the input's
         const bool pr = o.mf == MF_PR;
+        const double *corr = pr ? f.corr[1 - cur] + first : nullptr;
         int rc = o.precision == 64
-                     ? launch_halo_dg_tracers<double>((double *)f.Qbuf[1 - cur], T, g, pr ? f.corr[1 - cur] : nullptr,
-                                                      (const double *)f.g_pc, st)
-                     : launch_halo_dg_tracers<float>((float *)f.Qbuf[1 - cur], T, g, pr ? f.corr[1 - cur] : nullptr,
-                                                     (const float *)f.g_pc, st);
+                     ? launch_halo_dg_tracers<double>((double *)src, T, g, corr, (const double *)f.g_pc, st)
+                     : launch_halo_dg_tracers<float>((float *)src, T, g, corr, (const float *)f.g_pc, st);
         if (rc) return rc;
     }
     dim3 grid(ceil_div((long long)NFACE * d.n * d.n, 256), T);
     if (o.precision == 64)
-        k_copy_ghosts<double><<<grid, 256, 0, st>>>((const double *)f.Qbuf[1 - cur], (double *)f.Qbuf[cur], d);
+        k_copy_ghosts<double><<<grid, 256, 0, st>>>((const double *)src, (double *)dst, d);
     else
-        k_copy_ghosts<float><<<grid, 256, 0, st>>>((const float *)f.Qbuf[1 - cur], (float *)f.Qbuf[cur], d);
+        k_copy_ghosts<float><<<grid, 256, 0, st>>>((const float *)src, (float *)dst, d);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
@@ -147,6 +151,7 @@ int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedS
     f.cry = mem.alloc<char>(2 * d.plane * es);
     void *gpvT = mem.alloc<char>(d.plane * es);
     f.dsolve = mem.alloc<SweepSolve>(2);
+    f.dsolve_tr = mem.alloc<SweepSolve>(2 * T);
     if (o.precision == 32 && o.mf == MF_PR) {
         f.mass_target = mem.alloc<double>(T);
         const long long io_blocks = ceil_div((long long)d.n * d.n, IO_B);  // the full layout's upload
@@ -197,14 +202,15 @@ int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceA
 }
 
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, int buf,
-                     cudaStream_t st) {
-    if (f.sweep && w.nbasis) {
+                     cudaStream_t st, int part) {
+    if (f.sweep && w.nbasis) {  // the records of the x-edges (part 0), the y-edges (1) or both (-1)
         if (o.precision == 64)
             return wind_step<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT,
-                                     (double2 *)f.rec_x(buf), (double2 *)f.rec_y(buf), f.crx, f.cry, st);
+                                     (double2 *)f.rec_x(buf), (double2 *)f.rec_y(buf), f.crx, f.cry, st, part);
         return wind_step<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.rec_x(buf),
-                                (float2 *)f.rec_y(buf), nullptr, nullptr, st);
+                                (float2 *)f.rec_y(buf), nullptr, nullptr, st, part);
     }
+    if (part == 1) return CSADV_OK;  // the other preparations run whole (part -1 or 0)
     if (w.nbasis) {  // per-edge tile kernel on a basis wind: current and previous winds first
         int rc = wind_sync(o, g, w, st);
         if (rc) return rc;
@@ -287,7 +293,24 @@ int fused_set_tile(const Options &o, const Grid &g, int T, double dt, FusedState
     }
     f.nitems = NFACE * h[0].ntiles;
     f.smem = o.precision == 64 ? sweep_smem_bytes<double>(f.scfg) : sweep_smem_bytes<float>(f.scfg);
+    // one descriptor per buffer parity and tracer: the tracer's fields, pending corrections,
+    // partial sums and mass target (the arrival counter is shared: the launches are ordered)
+    std::vector<SweepSolve> ht(2 * (size_t)T);
+    const size_t fb = (size_t)g.d.field * (o.precision == 64 ? sizeof(double) : sizeof(float));
+    for (int b = 0; b < 2; ++b)
+        for (int t = 0; t < T; ++t) {
+            SweepSolve s = h[b];
+            s.T = 1;
+            s.Qin = (const char *)h[b].Qin + t * fb;
+            s.Qout = (char *)h[b].Qout + t * fb;
+            if (s.corr_in) s.corr_in += t;
+            if (s.corr_out) s.corr_out += t;
+            s.partials += (long long)t * f.nitems;
+            if (s.mass_target) s.mass_target += t;
+            ht[(size_t)b * T + t] = s;
+        }
     CSADV_CUDA(cudaMemcpyAsync(f.dsolve, h, sizeof(h), cudaMemcpyHostToDevice, st));
+    CSADV_CUDA(cudaMemcpyAsync(f.dsolve_tr, ht.data(), ht.size() * sizeof(SweepSolve), cudaMemcpyHostToDevice, st));
     CSADV_CUDA(cudaStreamSynchronize(st));
     (void)was;
     return CSADV_OK;
@@ -347,6 +370,14 @@ int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &
     if (ev1) CSADV_CUDA(cudaEventRecord(ev1, st));
     cur = 1 - cur;
     return CSADV_OK;
+}
+
+int fused_kernel_tracer(const Options &o, int T, const FusedState &f, int cur, int t, cudaStream_t st) {
+    if (!f.sweep || t < 0 || t >= T) return CSADV_ERR_UNSUPPORTED;
+    const SweepSolve *s = f.dsolve_tr + (size_t)cur * T + t;
+    return o.precision == 64 ? sweep_launch<double>(o.recon, o.opsplit, s, nullptr, f.nitems, f.nitems, f.smem, st, 0)
+                             : sweep_launch<float>(o.recon, o.opsplit, s, nullptr, f.nitems, f.nitems, f.smem, st,
+                                                   SWEEP_TG_ONE);
 }
 
 // sum over the interior of Q g (metric in the state's precision): per-block partials over a

@@ -128,9 +128,10 @@ int wind_set_dt(Winds &w, double dt, cudaStream_t st);
 int wind_basis_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, cudaStream_t st);
 // departure-point winds + upwind flags of the step from the basis (line-marching layouts); FP64:
 // with the edges' flux coefficients, from the cell records crx / cry
+// (part -1: every edge; 0: the x-edges only; 1: the y-edges only)
 template <class real, class V>
 int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
-              V *ery, const void *crx, const void *cry, cudaStream_t st);
+              V *ery, const void *crx, const void *cry, cudaStream_t st, int part = -1);
 // u_pu, v_pv, u_old, v_old <- the basis at the clock's times (before staged operators run)
 int wind_sync(const Options &o, const Grid &g, const Winds &w, cudaStream_t st);
 int wind_initial(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
@@ -174,6 +175,7 @@ struct FusedState {
     double crec_dtdx = 0.0;  // FP64 AVLT: the cell records hold {g, dtdx / g} for this dt/dx
     const void *gpvT = nullptr;           // y-edge metric transposed
     SweepSolve *dsolve = nullptr;  // [2]
+    SweepSolve *dsolve_tr = nullptr;  // [2][T]: the same launches restricted to one tracer each
     int nitems = 0;             // work items of one sweep launch (6 x tiles)
     bool inline_ghosts = false; // k_sweep evaluates the ET-DG ghost cells of its tiles (no ghost kernel)
     double *mass_target = nullptr;  // [T] FP32 + MF-PR: sum(Q g) of each tracer when it was set
@@ -186,7 +188,7 @@ int fused_supported(const Options &o);
 int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedState &f, cudaStream_t st);
 // departure-point winds of the step that reads Qbuf[buf] (edge records buffer buf when pipelined)
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, int buf,
-                     cudaStream_t st);
+                     cudaStream_t st, int part = -1);
 // step kernel with a time-dependent (basis) wind: allocate the second record buffer (the next
 // step's records are made while the step kernel runs)
 int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceArena &mem, FusedState &f,
@@ -196,6 +198,10 @@ int fused_ghosts(const Options &o, const Grid &g, int T, FusedState &f, int cur,
 // the fused kernel Qbuf[cur] -> Qbuf[1-cur]; cur flips
 int fused_kernel(const Options &o, const Grid &g, double dt, int T, FusedState &f, int &cur, cudaStream_t st,
                  cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
+// the line-marching step kernel on tracer t alone, Qbuf[cur] -> Qbuf[1-cur] (cur does not flip):
+// the tracers of one step in separate launches, so that the copies of one tracer overlap the
+// step of another
+int fused_kernel_tracer(const Options &o, int T, const FusedState &f, int cur, int t, cudaStream_t st);
 // set the dynamic shared-memory limit of the kernel a plan will launch (outside capture)
 int fused_prepare(const Options &o, int tile);
 // select the tile configuration of the fused engine (tile code as in csadv_options.tile,
@@ -214,8 +220,10 @@ int sweep_launch<float>(int recon, int split, const SweepSolve *dsolves, const i
 template <class real, class V>
 int wind_avgprep_t(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT,
                    V *erx, V *ery, const void *crx, const void *cry, cudaStream_t st);
-// ghost cells of Qbuf[cur] <- those of Qbuf[1-cur] (the halo the last step used)
-int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st);
+// ghost cells of Qbuf[cur] <- those of Qbuf[1-cur] (the halo the last step used), tracers
+// first .. first + T - 1
+int fused_ghosts_to_current(const Options &o, const Grid &g, int T, FusedState &f, int cur, cudaStream_t st,
+                            int first = 0);
 // FP32 form with MF-PR: record sum(Q g) of tracer t of Qbuf[cur] (no pending correction) as the
 // mass the step's correction restores
 int fused_anchor_mass(const Options &o, const Grid &g, FusedState &f, int cur, int t, cudaStream_t st);

@@ -61,6 +61,12 @@ struct csadv_plan {
     // second stream and fork/join events of the fused step
     cudaStream_t side = nullptr;
     cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // csadv_advance_host: copy streams, the high-priority stream of the split steps, events
+    // (uploaded[t], converted[t], fork, downloaded, to / from the high-priority stream) and the
+    // device staging arrays (full layout, one per tracer and direction)
+    cudaStream_t up = nullptr, down = nullptr, hp = nullptr;
+    std::vector<cudaEvent_t> hev;
+    double *hstage = nullptr;
     // profiling of the main kernel
     bool prof = false;
     cudaEvent_t pev[2] = {nullptr, nullptr};
@@ -77,6 +83,11 @@ struct csadv_plan {
         drop_graphs();
         if (cap) cudaStreamDestroy(cap);
         if (side) cudaStreamDestroy(side);
+        if (up) cudaStreamDestroy(up);
+        if (down) cudaStreamDestroy(down);
+        if (hp) cudaStreamDestroy(hp);
+        for (auto &e : hev)
+            if (e) cudaEventDestroy(e);
         for (auto &e : sev)
             if (e) cudaEventDestroy(e);
         for (auto &e : pev)

@@ -916,13 +916,14 @@ __global__ void __launch_bounds__(256) k_wind_rec(Dims d, const W *__restrict__ 
                                                   const Clock *__restrict__ clk, const W *__restrict__ gpu,
                                                   const W *__restrict__ gpvT, typename Vec2<W>::type *erx,
                                                   typename Vec2<W>::type *ery, int rk2, W c_half, long long cofs, W dtdx,
-                                                  UpwindMetric<W> mx, UpwindMetric<W> my) {
+                                                  UpwindMetric<W> mx, UpwindMetric<W> my, int zbase) {
     using V = typename Vec2<W>::type;
     constexpr bool F64 = sizeof(W) == 8;
     __shared__ W sx[34][33];  // extrapolated winds, rows ib-1 .. ib+32
     __shared__ W sn[32][33];  // winds now, rows ib .. ib+31
-    const bool ydir = blockIdx.z >= NFACE;
-    const int p = blockIdx.z - (ydir ? NFACE : 0);
+    const int z = blockIdx.z + zbase;
+    const bool ydir = z >= NFACE;
+    const int p = z - (ydir ? NFACE : 0);
     const W *B = ydir ? bvT : bu;
     const W *G = ydir ? gpvT : gpu;
     V *E = (ydir ? ery : erx) + p * d.plane;
@@ -1065,27 +1066,32 @@ static void upwind_metrics(const Options &o, const Dims &d, const void *gpu, con
 
 template <class real, class V>
 int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
-              V *ery, const void *crx, const void *cry, cudaStream_t st) {
+              V *ery, const void *crx, const void *cry, cudaStream_t st, int part) {
     const Dims d = g.d;
     if (!w.btabT) return CSADV_ERR_UNSUPPORTED;
     const real *bu = (const real *)w.btab[0], *bvT = (const real *)w.btabT;
     const Clock *clk = (const Clock *)w.clock;
-    dim3 g2(d.pitch / 32, ceil_div(d.n + 1, 32), 2 * NFACE);
+    // part -1: every edge; 0: the x-edges; 1: the y-edges (blockIdx.z + zbase = problem * 6 + panel)
+    dim3 g2(d.pitch / 32, ceil_div(d.n + 1, 32), part < 0 ? 2 * NFACE : NFACE);
+    const int zbase = part == 1 ? NFACE : 0;
     const real ch = (real)(dt * 0.5 / g.dx), dtdx = (real)(dt / g.dx);
     const long long cofs = record_coef_offset<real>(d);
     UpwindMetric<real> mx{}, my{};
     if (cofs) upwind_metrics<real>(o, d, gpu, gpvT, crx, cry, mx, my);
     if (w.nbasis == 4)
-        k_wind_rec<real, 4><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my);
+        k_wind_rec<real, 4><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my,
+                                                 zbase);
     else
-        k_wind_rec<real, 1><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my);
+        k_wind_rec<real, 1><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my,
+                                                 zbase);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
 template int wind_step<double, double2>(const Options &, const Grid &, const Winds &, double, const double *,
-                                        const double *, double2 *, double2 *, const void *, const void *, cudaStream_t);
+                                        const double *, double2 *, double2 *, const void *, const void *, cudaStream_t,
+                                        int);
 template int wind_step<float, float2>(const Options &, const Grid &, const Winds &, double, const float *,
-                                      const float *, float2 *, float2 *, const void *, const void *, cudaStream_t);
+                                      const float *, float2 *, float2 *, const void *, const void *, cudaStream_t, int);
 
 template <class W>
 static int sync_t(const Options &o, const Grid &g, const Winds &w, cudaStream_t st) {
