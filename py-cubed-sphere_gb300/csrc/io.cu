@@ -100,7 +100,20 @@ __global__ void __launch_bounds__(IO_B) k_io(Dims d, real *Q, double *host, int 
             if (last) {
                 __threadfence();
                 double a = 0.0;
-                for (int b = tid; b < (int)gridDim.x; b += IO_B) a = __dadd_rn(a, __ldcg(x.part + b));
+                // each thread adds its partials in block order; the loads of a batch are issued
+                // together (one L2 round trip per 8 partials, not one per partial)
+                constexpr int BATCH = 8;
+                for (int b0 = tid; b0 < (int)gridDim.x; b0 += BATCH * IO_B) {
+                    double v[BATCH];
+#pragma unroll
+                    for (int k = 0; k < BATCH; ++k) {
+                        const int b = b0 + k * IO_B;
+                        v[k] = b < (int)gridDim.x ? __ldcg(x.part + b) : 0.0;
+                    }
+#pragma unroll
+                    for (int k = 0; k < BATCH; ++k)
+                        if (b0 + k * IO_B < (int)gridDim.x) a = __dadd_rn(a, v[k]);
+                }
                 a = block_sum(a, ws);
                 if (tid == 0) {
                     *x.mass = a;
