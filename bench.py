@@ -15,7 +15,10 @@ arithmetic, so that it compares like for like with the reference arm.  The FP32 
 (tracer state, PPM and fluxes in float32; geometry, winds, Lagrange weights, mass and error
 sums in float64) is the `fp32` sub-object, with its own end-to-end rate and HBM roofline.
 Timed steps run as CUDA graphs; L2 is flushed (256 MB write) before every timed step and each
-step is timed alone with CUDA events on the launching stream.  N > 1 (torchrun): every rank
+step is timed alone with CUDA events on the launching stream.  `e2e` is the same step through
+the C ABI with page-locked host arrays: one `csadv_advance_host` call per step (upload both
+tracers, step, read both out, the copies beside the step), and `e2e.separate_calls` the same
+work as separate set / advance / get calls.  N > 1 (torchrun): every rank
 runs an independent replica (the solve does not shard; "replicas only"), max time over ranks.
 
 Further sub-objects, in the one-GPU job only: `accuracy` (one revolution at N = 48 and the
