@@ -476,13 +476,13 @@ int ensure_host_pipeline(csadv_plan *pl, cudaStream_t st) {
     if (!pl->up) {
         CSADV_CUDA(cudaStreamCreateWithFlags(&pl->up, cudaStreamNonBlocking));
         CSADV_CUDA(cudaStreamCreateWithFlags(&pl->down, cudaStreamNonBlocking));
-        // the first and last steps' kernels at the highest priority: the next step's wind
-        // records (side stream) start at once and fill the wait for the first upload, and the
-        // step kernels take the SMs back as soon as their tracer has arrived
+        // the split steps' kernels and the upload conversions at the highest priority: the next
+        // step's wind records (side stream) fill the SMs they leave free
         int least = 0, greatest = 0;
         CSADV_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         CSADV_CUDA(cudaStreamCreateWithPriority(&pl->hp, cudaStreamNonBlocking, greatest));
-        pl->hev.assign(2 * (size_t)pl->T + 4, nullptr);
+        CSADV_CUDA(cudaStreamCreateWithPriority(&pl->cv, cudaStreamNonBlocking, greatest));
+        pl->hev.assign(3 * (size_t)pl->T + 4, nullptr);
         for (auto &e : pl->hev) CSADV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     if (pl->hstage) return CSADV_OK;
@@ -505,52 +505,65 @@ int stage_tracer_out(csadv_plan *pl, int buf, int t, double *dst, int layout, cu
     return tracer_io<real>(pl->grid, Q, dst, layout, false, st, &x);
 }
 
+// The side stream's part of a step of the fused engine with pipelined winds, after event
+// `after`: the clock tick and the next step's records (part -1: all of them; 0: the x-edges',
+// the y-edges' to follow), into the buffer the current step does not read.
+int side_begin(csadv_plan *pl, cudaEvent_t after, int part) {
+    int rc = ensure_side(pl);
+    if (rc) return rc;
+    cudaStream_t sd = pl->side;
+    CSADV_CUDA(cudaStreamWaitEvent(sd, after, 0));
+    rc = do_update_winds(pl, true, 0, 0.0, sd);
+    if (!rc && pl->f.wpipe) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, 1 - pl->cur, sd, part);
+    return rc;
+}
+
 // One step of the fused engine with the step kernel launched once per tracer.  On `st`, tracer
-// t's kernel follows in(t) and, for t > 0, out(t - 1, cur); out(T - 1, cur) follows the last
-// kernel (cur: the step's input buffer; the results are in 1 - cur).  The side stream ticks the
-// clock and makes the next step's records (pipelined winds) beside the kernels, as in
-// fused_step_work.  With `upload` (in(0) waits for a copy) they run in two launches: the
-// x-edges' records at once, filling the wait for the first tracer's upload, and the y-edges'
-// records behind in(0) (one launch of every record would still hold the SMs when the first
-// kernel is ready, its CTAs living for a whole wave).
+// t's kernel follows out(t - 1, cur) (t > 0) and in(t); out(T - 1, cur) follows the last kernel
+// (cur: the step's input buffer; the results are in 1 - cur).  The side stream ticks the clock and
+// makes the next step's records beside the kernels, as in fused_step_work: started here, or
+// (side_started) by the caller with side_begin(part 0) when the first tracer arrives by upload:
+// the x-edges' records then fill the wait for that upload, and the y-edges' follow the last
+// kernel, beside the last read-out (records CTAs cannot be preempted: launched beside a step
+// kernel or a conversion they slow it, and one launch of all records would still hold the SMs
+// when the first tracer is in place).
 template <class In, class Out>
-int split_step(csadv_plan *pl, cudaStream_t st, bool upload, In in, Out out) {
+int split_step(csadv_plan *pl, cudaStream_t st, bool side_started, In in, Out out) {
     FusedState &f = pl->f;
     int rc = ensure_side(pl);
     if (rc) return rc;
-    if (f.wpipe && !f.rec_ready) {  // this step's records first
+    if (f.wpipe && !f.rec_ready) {  // this step's records first (before the clock ticks)
+        if (side_started) return CSADV_ERR_CUDA;
         rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, pl->cur, st);
         if (rc) return rc;
         f.rec_ready = true;
     }
     const int cur = pl->cur, T = pl->T;
     cudaStream_t sd = pl->side;
-    CSADV_CUDA(cudaEventRecord(pl->sev[0], st));
-    CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[0], 0));
-    rc = do_update_winds(pl, true, 0, 0.0, sd);
-    if (!rc && f.wpipe) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, 1 - cur, sd, upload ? 0 : -1);
-    if (rc) return rc;
+    if (!side_started) {
+        CSADV_CUDA(cudaEventRecord(pl->sev[0], st));
+        rc = side_begin(pl, pl->sev[0], -1);
+        if (rc) return rc;
+    }
     for (int t = 0; t < T; ++t) {
-        rc = in(t);
-        if (!rc && t == 0) {
-            if (f.wpipe && upload) {
-                CSADV_CUDA(cudaEventRecord(pl->sev[1], st));
-                CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[1], 0));
-                rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, 1 - cur, sd, 1);
-                if (rc) return rc;
-            }
-            CSADV_CUDA(cudaEventRecord(pl->sev[3], sd));
-        }
-        if (!rc && t > 0) rc = out(t - 1, cur);
+        if (t > 0) rc = out(t - 1, cur);  // the previous tracer's read-out as early as possible
+        if (!rc) rc = in(t);
         if (!rc) rc = fused_kernel_tracer(pl->opt, T, f, cur, t, st);
         if (rc) return rc;
     }
+    if (f.wpipe && side_started) {  // the y-edges' records beside the last read-out
+        CSADV_CUDA(cudaEventRecord(pl->sev[1], st));
+        CSADV_CUDA(cudaStreamWaitEvent(sd, pl->sev[1], 0));
+        rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, 1 - cur, sd, 1);
+        if (rc) return rc;
+    }
+    CSADV_CUDA(cudaEventRecord(pl->sev[3], sd));
     rc = out(T - 1, cur);
     if (rc) return rc;
     CSADV_CUDA(cudaStreamWaitEvent(st, pl->sev[3], 0));
     pl->cur = 1 - cur;
     f.settled = false;
-    const int kernels = T + 1 + (f.wpipe ? (upload ? 2 : 1) : 0);  // step kernels, clock tick, records
+    const int kernels = T + 1 + (f.wpipe ? (side_started ? 2 : 1) : 0);  // step kernels, clock tick, records
     pl->stats.steps += 1;
     pl->stats.kernel_launches += kernels;
     pl->stats.kernels_per_step = kernels;
@@ -791,31 +804,49 @@ int csadv_advance_host(csadv_plan *pl, int nsteps, const double *const *in, int 
         return rc;
     }
     rc = ensure_host_pipeline(pl, st);
+    if (!rc) rc = ensure_side(pl);
     if (rc) return rc;
     const Dims d = pl->grid.d;
     const size_t slot = (size_t)NFACE * d.n * d.n;  // doubles per staging array (full layout)
     auto cells = [&](int l) { return (size_t)NFACE * (l == CSADV_LAYOUT_FULL ? (size_t)d.n * d.n : (size_t)d.N * d.N); };
     double *sin = pl->hstage, *sout = pl->hstage + (size_t)T * slot;
-    cudaEvent_t *uploaded = pl->hev.data(), *converted = pl->hev.data() + T;
-    cudaEvent_t fork = pl->hev[2 * T], downloaded = pl->hev[2 * T + 1], to_hp = pl->hev[2 * T + 2],
-                from_hp = pl->hev[2 * T + 3];
+    cudaEvent_t *uploaded = pl->hev.data(), *converted = pl->hev.data() + T, *arrived = pl->hev.data() + 2 * T;
+    cudaEvent_t fork = pl->hev[3 * T], downloaded = pl->hev[3 * T + 1], to_hp = pl->hev[3 * T + 2],
+                from_hp = pl->hev[3 * T + 3];
     const bool f64 = pl->opt.precision == 64;
-    // uploads: copy engine, host -> staging, all tracers in order, behind the stream's earlier work
+    cudaStream_t hp = pl->hp, cv = pl->cv;
+    if (f.wpipe && !f.rec_ready) {  // this step's records, while the clock holds its time
+        rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, pl->cur, st);
+        if (rc) return rc;
+        f.rec_ready = true;
+    }
     CSADV_CUDA(cudaEventRecord(fork, st));
+    // with an upload, the first step's side-stream work is queued first: the clock tick and the
+    // next step's x-edge records run while the first tracer is copied
+    if (in) rc = side_begin(pl, fork, 0);
+    if (rc) return rc;
     if (in) {
+        // copies on the copy engine (host -> staging), all tracers in order; each conversion
+        // (staging -> the tracer's field) on the conversion stream as its copy lands, so those of
+        // tracers 1.. run beside tracer 0's kernel
         CSADV_CUDA(cudaStreamWaitEvent(pl->up, fork, 0));
+        CSADV_CUDA(cudaStreamWaitEvent(cv, fork, 0));
         for (int t = 0; t < T; ++t) {
             CSADV_CUDA(cudaMemcpyAsync(sin + t * slot, in[t], cells(in_layout) * sizeof(double), cudaMemcpyHostToDevice,
                                        pl->up));
             CSADV_CUDA(cudaEventRecord(uploaded[t], pl->up));
         }
+        for (int t = 0; t < T; ++t) {
+            CSADV_CUDA(cudaStreamWaitEvent(cv, uploaded[t], 0));
+            rc = f64 ? tracer_upload<double>(pl, t, sin + t * slot, in_layout, cv)
+                     : tracer_upload<float>(pl, t, sin + t * slot, in_layout, cv);
+            if (rc) return rc;
+            CSADV_CUDA(cudaEventRecord(arrived[t], cv));
+        }
     }
-    cudaStream_t hp = pl->hp;
-    auto convert_in = [&](int t) -> int {  // staging -> the tracer's field (layout conversion)
-        if (!in) return CSADV_OK;
-        CSADV_CUDA(cudaStreamWaitEvent(hp, uploaded[t], 0));
-        return f64 ? tracer_upload<double>(pl, t, sin + t * slot, in_layout, hp)
-                   : tracer_upload<float>(pl, t, sin + t * slot, in_layout, hp);
+    auto wait_in = [&](int t) -> int {  // tracer t is in place
+        if (in) CSADV_CUDA(cudaStreamWaitEvent(hp, arrived[t], 0));
+        return CSADV_OK;
     };
     auto convert_out = [&](int t, int cur) -> int {  // the step's result -> staging -> host
         if (!out) return CSADV_OK;
@@ -833,18 +864,18 @@ int csadv_advance_host(csadv_plan *pl, int nsteps, const double *const *in, int 
     auto none_in = [](int) { return CSADV_OK; };
     auto none_out = [](int, int) { return CSADV_OK; };
     // the first and the last step on the high-priority stream, forked from and joined to `st`
-    auto on_hp = [&](bool up_step, auto in_fn, auto out_fn) -> int {
+    auto on_hp = [&](bool side_started, auto in_fn, auto out_fn) -> int {
         CSADV_CUDA(cudaEventRecord(to_hp, st));
-        CSADV_CUDA(cudaStreamWaitEvent(pl->hp, to_hp, 0));
-        const int r = split_step(pl, pl->hp, in != nullptr && up_step, in_fn, out_fn);
-        CSADV_CUDA(cudaEventRecord(from_hp, pl->hp));
+        CSADV_CUDA(cudaStreamWaitEvent(hp, to_hp, 0));
+        const int r = split_step(pl, hp, side_started, in_fn, out_fn);
+        CSADV_CUDA(cudaEventRecord(from_hp, hp));
         CSADV_CUDA(cudaStreamWaitEvent(st, from_hp, 0));
         return r;
     };
     for (int s = 0; s < nsteps && !rc; ++s) {
         const bool first = s == 0, last = s == nsteps - 1;
-        if (first && last) rc = on_hp(true, convert_in, convert_out);
-        else if (first) rc = on_hp(true, convert_in, none_out);
+        if (first && last) rc = on_hp(in != nullptr, wait_in, convert_out);
+        else if (first) rc = on_hp(in != nullptr, wait_in, none_out);
         else if (last) rc = on_hp(false, none_in, convert_out);
         else rc = run_step(pl, 1, st);
         if (!rc) pl->k += 1;

@@ -61,10 +61,11 @@ struct csadv_plan {
     // second stream and fork/join events of the fused step
     cudaStream_t side = nullptr;
     cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
-    // csadv_advance_host: copy streams, the high-priority stream of the split steps, events
-    // (uploaded[t], converted[t], fork, downloaded, to / from the high-priority stream) and the
-    // device staging arrays (full layout, one per tracer and direction)
-    cudaStream_t up = nullptr, down = nullptr, hp = nullptr;
+    // csadv_advance_host: copy streams, the high-priority streams of the split steps and of the
+    // upload conversions, events (uploaded[t], converted[t], arrived[t], fork, downloaded, to /
+    // from the high-priority stream) and the device staging arrays (full layout, one per tracer
+    // and direction)
+    cudaStream_t up = nullptr, down = nullptr, hp = nullptr, cv = nullptr;
     std::vector<cudaEvent_t> hev;
     double *hstage = nullptr;
     // profiling of the main kernel
@@ -86,6 +87,7 @@ struct csadv_plan {
         if (up) cudaStreamDestroy(up);
         if (down) cudaStreamDestroy(down);
         if (hp) cudaStreamDestroy(hp);
+        if (cv) cudaStreamDestroy(cv);
         for (auto &e : hev)
             if (e) cudaEventDestroy(e);
         for (auto &e : sev)
