@@ -825,27 +825,35 @@ int csadv_advance_host(csadv_plan *pl, int nsteps, const double *const *in, int 
     // next step's x-edge records run while the first tracer is copied
     if (in) rc = side_begin(pl, fork, 0);
     if (rc) return rc;
-    if (in) {
-        // copies on the copy engine (host -> staging), all tracers in order; each conversion
-        // (staging -> the tracer's field) on the conversion stream as its copy lands, so those of
-        // tracers 1.. run beside tracer 0's kernel
+    if (in) {  // copies on the copy engine (host -> staging), all tracers in order
         CSADV_CUDA(cudaStreamWaitEvent(pl->up, fork, 0));
-        CSADV_CUDA(cudaStreamWaitEvent(cv, fork, 0));
         for (int t = 0; t < T; ++t) {
             CSADV_CUDA(cudaMemcpyAsync(sin + t * slot, in[t], cells(in_layout) * sizeof(double), cudaMemcpyHostToDevice,
                                        pl->up));
             CSADV_CUDA(cudaEventRecord(uploaded[t], pl->up));
         }
-        for (int t = 0; t < T; ++t) {
-            CSADV_CUDA(cudaStreamWaitEvent(cv, uploaded[t], 0));
-            rc = f64 ? tracer_upload<double>(pl, t, sin + t * slot, in_layout, cv)
-                     : tracer_upload<float>(pl, t, sin + t * slot, in_layout, cv);
-            if (rc) return rc;
-            CSADV_CUDA(cudaEventRecord(arrived[t], cv));
-        }
     }
-    auto wait_in = [&](int t) -> int {  // tracer t is in place
-        if (in) CSADV_CUDA(cudaStreamWaitEvent(hp, arrived[t], 0));
+    auto convert_in = [&](int t, cudaStream_t s) -> int {  // staging -> the tracer's field
+        CSADV_CUDA(cudaStreamWaitEvent(s, uploaded[t], 0));
+        const int r = f64 ? tracer_upload<double>(pl, t, sin + t * slot, in_layout, s)
+                          : tracer_upload<float>(pl, t, sin + t * slot, in_layout, s);
+        if (r) return r;
+        CSADV_CUDA(cudaEventRecord(arrived[t], s));
+        return CSADV_OK;
+    };
+    // tracer t in place before its kernel: tracer 0 converted on the kernels' stream itself, the
+    // others on the conversion stream as their copies land (beside tracer 0's kernel), one after
+    // another (the FP32 form's mass sums share their partials)
+    auto wait_in = [&](int t) -> int {
+        if (!in) return CSADV_OK;
+        if (t == 0) {
+            int r = convert_in(0, hp);
+            if (r) return r;
+            CSADV_CUDA(cudaStreamWaitEvent(cv, arrived[0], 0));
+            for (int u = 1; u < T && !r; ++u) r = convert_in(u, cv);
+            return r;
+        }
+        CSADV_CUDA(cudaStreamWaitEvent(hp, arrived[t], 0));
         return CSADV_OK;
     };
     auto convert_out = [&](int t, int cur) -> int {  // the step's result -> staging -> host
