@@ -64,3 +64,10 @@ def test_plan_create_rejects_bad_arguments_before_touching_the_gpu(lib):
     assert lib.csadv_plan_create(16, 0.01, 0, ctypes.byref(o), None, ctypes.byref(h)) == _lib.ERR_ARG
     assert lib.csadv_plan_create(16, 0.01, 1, None, None, ctypes.byref(h)) == _lib.ERR_ARG
     assert not h.value
+
+
+def test_advance_host_rejects_a_missing_plan_without_gpu(lib):
+    from csadv import _lib
+    arr = (ctypes.c_void_p * 1)(None)
+    assert lib.csadv_advance_host(None, 1, None, 0, None, 0, None) == _lib.ERR_ARG
+    assert lib.csadv_advance_host(None, 1, arr, 0, arr, 1, None) == _lib.ERR_ARG
