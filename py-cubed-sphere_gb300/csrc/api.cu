@@ -533,7 +533,8 @@ int split_step(csadv_plan *pl, cudaStream_t st, bool side_started, In in, Out ou
     int rc = ensure_side(pl);
     if (rc) return rc;
     if (f.wpipe && !f.rec_ready) {  // this step's records first (before the clock ticks)
-        if (side_started) return CSADV_ERR_CUDA;
+        // a caller that starts the side stream itself has made them first (the tick is queued)
+        if (side_started) return CSADV_ERR_UNSUPPORTED;
         rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, f, pl->cur, st);
         if (rc) return rc;
         f.rec_ready = true;
