@@ -507,14 +507,19 @@ int stage_tracer_out(csadv_plan *pl, int buf, int t, double *dst, int layout, cu
 
 // The side stream's part of a step of the fused engine with pipelined winds, after event
 // `after`: the clock tick and the next step's records (part -1: all of them; 0: the x-edges',
-// the y-edges' to follow), into the buffer the current step does not read.
+// the y-edges' to follow), into the buffer the current step does not read.  The x-edges' records
+// come first, computing the next step's time factors themselves, and the tick after them: the
+// records start at once.
 int side_begin(csadv_plan *pl, cudaEvent_t after, int part) {
     int rc = ensure_side(pl);
     if (rc) return rc;
     cudaStream_t sd = pl->side;
     CSADV_CUDA(cudaStreamWaitEvent(sd, after, 0));
-    rc = do_update_winds(pl, true, 0, 0.0, sd);
-    if (!rc && pl->f.wpipe) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, 1 - pl->cur, sd, part);
+    const bool early = part == 0 && pl->f.wpipe;
+    if (early) rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, 1 - pl->cur, sd, 0, 1);
+    if (!rc) rc = do_update_winds(pl, true, 0, 0.0, sd);
+    if (!rc && pl->f.wpipe && !early)
+        rc = fused_prep_winds(pl->opt, pl->grid, pl->w, pl->dt, pl->f, 1 - pl->cur, sd, part);
     return rc;
 }
 

@@ -202,15 +202,16 @@ int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceA
 }
 
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, int buf,
-                     cudaStream_t st, int part) {
+                     cudaStream_t st, int part, int peek) {
     if (f.sweep && w.nbasis) {  // the records of the x-edges (part 0), the y-edges (1) or both (-1)
         if (o.precision == 64)
             return wind_step<double>(o, g, w, dt, (const double *)f.g_pu, (const double *)f.gpvT,
-                                     (double2 *)f.rec_x(buf), (double2 *)f.rec_y(buf), f.crx, f.cry, st, part);
+                                     (double2 *)f.rec_x(buf), (double2 *)f.rec_y(buf), f.crx, f.cry, st, part, peek);
         return wind_step<float>(o, g, w, dt, (const float *)f.g_pu, (const float *)f.gpvT, (float2 *)f.rec_x(buf),
-                                (float2 *)f.rec_y(buf), nullptr, nullptr, st, part);
+                                (float2 *)f.rec_y(buf), nullptr, nullptr, st, part, peek);
     }
-    if (part == 1) return CSADV_OK;  // the other preparations run whole (part -1 or 0)
+    if (peek) return CSADV_ERR_UNSUPPORTED;  // the other preparations run after the clock's tick
+    if (part == 1) return CSADV_OK;          // and whole (part -1 or 0)
     if (w.nbasis) {  // per-edge tile kernel on a basis wind: current and previous winds first
         int rc = wind_sync(o, g, w, st);
         if (rc) return rc;

@@ -128,10 +128,11 @@ int wind_set_dt(Winds &w, double dt, cudaStream_t st);
 int wind_basis_setup(const Options &o, const Grid &g, Winds &w, DeviceArena &mem, cudaStream_t st);
 // departure-point winds + upwind flags of the step from the basis (line-marching layouts); FP64:
 // with the edges' flux coefficients, from the cell records crx / cry
-// (part -1: every edge; 0: the x-edges only; 1: the y-edges only)
+// (part -1: every edge; 0: the x-edges only; 1: the y-edges only; peek: for the clock's next step,
+// before the clock ticks)
 template <class real, class V>
 int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
-              V *ery, const void *crx, const void *cry, cudaStream_t st, int part = -1);
+              V *ery, const void *crx, const void *cry, cudaStream_t st, int part = -1, int peek = 0);
 // u_pu, v_pv, u_old, v_old <- the basis at the clock's times (before staged operators run)
 int wind_sync(const Options &o, const Grid &g, const Winds &w, cudaStream_t st);
 int wind_initial(const Options &o, const Grid &g, Winds &w, cudaStream_t st);
@@ -188,7 +189,7 @@ int fused_supported(const Options &o);
 int fused_alloc(const Options &o, const Grid &g, int T, DeviceArena &mem, FusedState &f, cudaStream_t st);
 // departure-point winds of the step that reads Qbuf[buf] (edge records buffer buf when pipelined)
 int fused_prep_winds(const Options &o, const Grid &g, const Winds &w, double dt, FusedState &f, int buf,
-                     cudaStream_t st, int part = -1);
+                     cudaStream_t st, int part = -1, int peek = 0);
 // step kernel with a time-dependent (basis) wind: allocate the second record buffer (the next
 // step's records are made while the step kernel runs)
 int fused_wind_pipeline(const Options &o, const Grid &g, const Winds &w, DeviceArena &mem, FusedState &f,

@@ -916,7 +916,8 @@ __global__ void __launch_bounds__(256) k_wind_rec(Dims d, const W *__restrict__ 
                                                   const Clock *__restrict__ clk, const W *__restrict__ gpu,
                                                   const W *__restrict__ gpvT, typename Vec2<W>::type *erx,
                                                   typename Vec2<W>::type *ery, int rk2, W c_half, long long cofs, W dtdx,
-                                                  UpwindMetric<W> mx, UpwindMetric<W> my, int zbase) {
+                                                  UpwindMetric<W> mx, UpwindMetric<W> my, int zbase,
+                                                  WindParams wp, int tkind, int peek) {
     using V = typename Vec2<W>::type;
     constexpr bool F64 = sizeof(W) == 8;
     __shared__ W sx[34][33];  // extrapolated winds, rows ib-1 .. ib+32
@@ -931,14 +932,40 @@ __global__ void __launch_bounds__(256) k_wind_rec(Dims d, const W *__restrict__ 
     const int jb = blockIdx.x * 32, ib = blockIdx.y * 32, lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
     const int j = jb + lane;
     W hn[M], ho[M];
+    if (peek) {
+        // the records of the clock's next step before the clock has ticked: the time factors that
+        // k_clock_tick and clock_round will set (the same operations, so the same bits), while
+        // the clock still holds the current ones
+        __shared__ W ph[2][4];
+        if (threadIdx.x == 0) {
+            double h[4];
+            wind_basis_h(wp, tkind, (double)(clk->k + 1) * clk->dt, h);
+            for (int m = 0; m < M; ++m) {
+                if constexpr (F64) {
+                    ph[0][m] = h[m];
+                    ph[1][m] = 1.5 * h[m] - 0.5 * clk->hn[m];
+                } else {
+                    ph[0][m] = (float)h[m];
+                    ph[1][m] = (float)clk->hn[m];
+                }
+            }
+        }
+        __syncthreads();
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-        if constexpr (F64) {
-            hn[m] = clk->hn[m];
-            ho[m] = clk->hx[m];  // the extrapolation's time factors
-        } else {
-            hn[m] = clk->hnf[m];
-            ho[m] = clk->hof[m];
+        for (int m = 0; m < M; ++m) {
+            hn[m] = ph[0][m];
+            ho[m] = ph[1][m];
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            if constexpr (F64) {
+                hn[m] = clk->hn[m];
+                ho[m] = clk->hx[m];  // the extrapolation's time factors
+            } else {
+                hn[m] = clk->hnf[m];
+                ho[m] = clk->hof[m];
+            }
         }
     }
     constexpr int NQ = 5;  // rows wy + 8 q, q < 5, cover the 34 rows
@@ -1066,7 +1093,7 @@ static void upwind_metrics(const Options &o, const Dims &d, const void *gpu, con
 
 template <class real, class V>
 int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const real *gpu, const real *gpvT, V *erx,
-              V *ery, const void *crx, const void *cry, cudaStream_t st, int part) {
+              V *ery, const void *crx, const void *cry, cudaStream_t st, int part, int peek) {
     const Dims d = g.d;
     if (!w.btabT) return CSADV_ERR_UNSUPPORTED;
     const real *bu = (const real *)w.btab[0], *bvT = (const real *)w.btabT;
@@ -1080,18 +1107,19 @@ int wind_step(const Options &o, const Grid &g, const Winds &w, double dt, const 
     if (cofs) upwind_metrics<real>(o, d, gpu, gpvT, crx, cry, mx, my);
     if (w.nbasis == 4)
         k_wind_rec<real, 4><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my,
-                                                 zbase);
+                                                 zbase, wparams(o), w.tkind, peek);
     else
         k_wind_rec<real, 1><<<g2, 256, 0, st>>>(d, bu, bvT, clk, gpu, gpvT, erx, ery, o.dp == 2, ch, cofs, dtdx, mx, my,
-                                                 zbase);
+                                                 zbase, wparams(o), w.tkind, peek);
     CSADV_CUDA(cudaGetLastError());
     return CSADV_OK;
 }
 template int wind_step<double, double2>(const Options &, const Grid &, const Winds &, double, const double *,
                                         const double *, double2 *, double2 *, const void *, const void *, cudaStream_t,
-                                        int);
+                                        int, int);
 template int wind_step<float, float2>(const Options &, const Grid &, const Winds &, double, const float *,
-                                      const float *, float2 *, float2 *, const void *, const void *, cudaStream_t, int);
+                                      const float *, float2 *, float2 *, const void *, const void *, cudaStream_t, int,
+                                      int);
 
 template <class W>
 static int sync_t(const Options &o, const Grid &g, const Winds &w, cudaStream_t st) {
